@@ -1,0 +1,496 @@
+"""Benchmark: batched-ensemble DiReBM step on one GB300 (point-steps/s), one JSON line.
+
+Workload (the batched-ensemble configuration): 256 independent periodic 2D D2Q9 runs in one
+launch; point counts log-uniform in [4096, 262144] (seed 1); each run is a jittered grid (spacing
+h = dx = 1, jitter U(+-0.25)) in a periodic square of side round(sqrt(M)); tau U(0.55, 1.0);
+initial velocity = 8 random divergence-free Fourier modes (seed 100 + i) scaled to RMS 0.02;
+resampling radius 1.5h, thinning cell h; FP32-deviation store; CUDA graphs.  Synthetic data
+(no dataset is involved).  The state (~15.5 M moments, ~0.8 GB) is far larger than L2 (129 MB),
+so L2 is not flushed between steps.
+
+Keys beyond the base contract:
+  roofline      dominant kernel's algorithmic bytes / its CUDA-event duration vs measured HBM peak
+  step_roofline the whole step against the per-point-step byte model of the method
+  fp64          the same workload in the FP64 store (fewer steps: GB300 FP64 is slow)
+  accuracy      velocity L2 error vs the FP64 oracle on a 4096-point instance
+  lbm           hexagonal D2Q7 shear wave 1024x1024 (FP32DEV and FP64), node-steps/s
+  cpu_baseline  the CPU oracle (numpy restatement of the reference step) on the host cores
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_INST = 256
+M_MIN, M_MAX = 4096, 262144
+R_RES, CELL, DX = 1.5, 1.0, 1.0
+U_RMS = 0.02
+METRIC = "point-steps/s on 1 GB300, FP32 vs FP64 at equal L2 error; adjoint step/s"
+
+# Algorithmic bytes per unit for the roofline, FP32DEV D2Q9 2D (Q = 9, D = 2): each input read
+# once and each output written once; windows re-read from L1/L2 are not counted.
+Q9, D2 = 9, 2
+KERNEL_BYTES = {
+    # per moment: read rho + dev (40) + cell (4) + offsets (8); per occupied cell: start (4),
+    # write occupancy, refined cell, offsets (16)
+    "thin_refine": ("moment+cell", 4 * (1 + Q9) + 4 + 4 * D2, 4 + 16),
+    # per component: read offsets (8) + cell (4) once per moment, write sw (4); CP reads (12/CP)
+    "weights": ("moment+cp", 4 * D2 + 4 + 4 * Q9, 12),
+    # per moment: offsets + rho + dev + sw (8+4+36+36) + starts; per CP: cell+offsets (12) + cpf (72) + mask (4)
+    "gather": ("moment+cp", 4 * D2 + 4 * (1 + Q9) + 4 * Q9 + 4, 12 + 8 * Q9 + 4),
+    # per CP: read cpf (72) + mask (4) + cell/off (12); write rho + dev (40)
+    "emit": ("cp", 0, 8 * Q9 + 4 + 12 + 4 * (1 + Q9)),
+    # per moment: read rho + dev, write dev
+    "collide": ("moment", 4 * (1 + Q9) + 4 + 4 * Q9, 0),
+    # per CP: 3 passes x (hist read 4 + scatter read 8 + write 8) + compaction (8) + finalize (24)
+    "sort": ("cp", 0, 3 * 20 + 8 + 24),
+}
+
+# Per point-step byte model of the method (components materialised as 12-byte sort records):
+# B = M(Qs+b_p) + Nc k_b + 2 Nc k_b + 3(Nc k_b + M(Qs+b_p)) + 3 P b_p + P(Qs+b_p), with P ~ M,
+# s = 4, b_p = 8D (int cell + FP32 offset per axis), k_b = 12 -> 956 B for D2Q9 FP32.
+def step_bytes_per_point(Q=9, D=2, s=4):
+    bp = 8 * D
+    kb = 12
+    Nc = Q
+    return (Q * s + bp) + Nc * kb + 2 * Nc * kb + 3 * (Nc * kb + (Q * s + bp)) + 3 * bp + (Q * s + bp)
+
+
+# ---- workload ---------------------------------------------------------------------------------
+
+def ensemble_spec(n_inst=N_INST, seed=1):
+    rng = np.random.default_rng(seed)
+    M = np.exp(rng.uniform(np.log(M_MIN), np.log(M_MAX), n_inst))
+    sides = np.maximum(np.round(np.sqrt(M)).astype(int), 16)
+    taus = rng.uniform(0.55, 1.0, n_inst)
+    return sides, taus
+
+
+def fourier_velocity(x, n, seed, modes=8, u_rms=U_RMS):
+    rng = np.random.default_rng(seed)
+    u = np.zeros_like(x)
+    for _ in range(modes):
+        k = np.zeros(2)
+        while not k.any():
+            k = rng.integers(-4, 5, size=2).astype(np.float64)
+        e = np.array([-k[1], k[0]]) / np.linalg.norm(k)  # divergence-free direction
+        phase = rng.uniform(0, 2 * np.pi)
+        amp = rng.normal()
+        u += amp * e[None, :] * np.sin(2 * np.pi * (x @ k) / n + phase)[:, None]
+    rms = np.sqrt((u * u).sum(1).mean())
+    return u * (u_rms / max(rms, 1e-30))
+
+
+def instance_points(n, seed):
+    rng = np.random.default_rng(seed)
+    x = (np.indices((n, n)).reshape(2, -1).T[:, ::-1] + 0.5).astype(np.float64)
+    x += rng.uniform(-0.25, 0.25, size=x.shape)
+    return np.mod(x, n)
+
+
+def build_ensemble(sides, taus):
+    from direbm_gb300.lattices import D2Q9, equilibrium
+
+    xs, fs, ib = [], [], []
+    for i, n in enumerate(sides):
+        x = instance_points(int(n), 100 + i)
+        u = fourier_velocity(x, int(n), 100 + i)
+        xs.append(x)
+        fs.append(equilibrium(np.ones(len(x)), u, D2Q9))
+        ib.append(np.full(len(x), i, dtype=np.int32))
+    return np.concatenate(ib), np.concatenate(xs), np.concatenate(fs)
+
+
+def make_sim(sides, taus, precision, cap, graphs=True, device=None):
+    from direbm_gb300.sim import Instance, Simulation
+
+    insts = [Instance(dims=(int(n), int(n)), periodic=True, tau=float(t)) for n, t in zip(sides, taus)]
+    return Simulation(insts, lattice="D2Q9", precision=precision, dx=DX, r_res=R_RES, cell=CELL,
+                      moment_capacity=cap, graphs=graphs, device=device)
+
+
+# ---- clocks ------------------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        time.sleep(0.25)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [v.strip() for v in ln.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- measurement legs --------------------------------------------------------------------------
+
+def timed_steps(sim, steps, warmup):
+    import torch
+
+    for _ in range(warmup):
+        sim.step(1)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    from direbm_gb300 import _lib
+
+    l0 = _lib.launch_count()
+    ev0.record()
+    sim.step(steps)
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1), _lib.launch_count() - l0
+
+
+def roofline_from_profile(sim, M, P, peak):
+    prof = {k: [] for k in sim.STAGES}
+    for _ in range(3):
+        for k, v in sim.profile_step().items():
+            prof[k].append(v)
+    avg = {k: float(np.mean(v)) for k, v in prof.items()}
+    dom = max(avg, key=avg.get)
+    unit, per_m, per_c = KERNEL_BYTES[dom]
+    nbytes = per_m * M + per_c * (P if unit != "moment+cell" else sim.ncells)
+    achieved = nbytes / (avg[dom] * 1e-3) / 1e9
+    return dom, avg, {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                      "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": int(nbytes),
+                      "ms_per_launch": avg[dom], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+
+
+def velocity_l2(f, lat):
+    rho = f.sum(1)
+    return (f @ lat.C) / rho[:, None]
+
+
+def accuracy_leg(steps=10):
+    """FP32DEV and FP64 GPU vs the FP64 oracle on one 64x64 instance (the smallest ensemble size)."""
+    from oracle import grid_step
+    from oracle.lattices import D2Q9 as OD2Q9
+
+    n = 64
+    x = instance_points(n, 100)
+    u = fourier_velocity(x, n, 100)
+    from direbm_gb300.lattices import D2Q9, equilibrium
+
+    f = equilibrium(np.ones(len(x)), u, D2Q9)
+    spec = grid_step.GridSpec(lattice=OD2Q9, dx=DX, r_res=R_RES, cell=CELL, kappa_hard=4,
+                              instances=[grid_step.Instance(dims=(n, n), periodic=True, tau=0.8)])
+    st = grid_step.run(spec, grid_step.from_world(spec, np.zeros(len(x), int), x, f), steps)
+    _, xo, fo = grid_step.to_world(spec, st)
+    uo = velocity_l2(fo, OD2Q9)
+    out = {"instance": "64x64 periodic D2Q9, tau 0.8, 8 modes RMS 0.02", "steps": steps}
+    for prec in ("fp32dev", "fp64"):
+        sim = make_sim([n], [0.8], prec, 0)
+        sim.set_state(None, x, f)
+        sim.step(steps)
+        _, xg, fg = sim.state_numpy()
+        same = len(xg) == len(xo) and np.abs(xg - xo).max() < 1e-3
+        if same:
+            ug = velocity_l2(fg, OD2Q9)
+            err = float(np.sqrt(((ug - uo) ** 2).sum() / (uo ** 2).sum()))
+        else:
+            err = None
+        out[prec] = {"velocity_l2_rel": err, "points_match": bool(same), "moments": int(len(xg)),
+                     "max_pos_err": float(np.abs(xg - xo).max()) if len(xg) == len(xo) else None}
+        sim.close()
+    return out
+
+
+def lbm_leg(steps=100, warmup=5):
+    import torch
+
+    from direbm_gb300.lattices import D2Q7, equilibrium
+    from direbm_gb300.lbm import HexLBM
+
+    ni = nj = 1024
+    jrow = np.arange(nj, dtype=np.float64)
+    u = np.zeros((nj, ni, 2))
+    u[..., 0] = (0.01 * np.sin(2 * np.pi * jrow / nj))[:, None]
+    f_shear = equilibrium(np.ones((nj, ni)), u, D2Q7)
+    kk = 2 * np.pi / (nj * np.sqrt(3.0) / 2.0)
+    taus = np.linspace(0.55, 1.0, 8)
+    res = {"config": "hex D2Q7 shear wave 1024x1024, amplitude 0.01, 8 runs tau 0.55..1.0", "steps": steps}
+    for prec, s in (("fp32dev", 4), ("fp64", 8)):
+        lb = HexLBM(ni, nj, taus, precision=prec)
+        lb.set_f(f_shear)
+        a0 = lb.shear_amplitude()
+        lb.step(warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lb.step(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        a1 = lb.shear_amplitude()
+        lam = -np.log(a1 / a0) / (steps + warmup)
+        lam_ref = 0.25 * (taus - 0.5) * kk * kk  # nu k^2, nu = cs^2 (tau - 1/2)
+        nodes = ni * nj * len(taus)
+        gbs = nodes * steps * 2 * 7 * s / (ms * 1e-3) / 1e9
+        res[prec] = {"node_steps_per_s": nodes * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                     "achieved_gbs": gbs, "decay_rate_rel_err_max": float(np.abs(lam / lam_ref - 1).max())}
+    return res
+
+
+def e2e_leg(sim, ib, x, f, steps=2):
+    """Same metric through the public API with host buffers: every step copies the state from pinned
+    host memory, loads it, steps once, exports it and copies it back."""
+    import torch
+
+    M = len(x)
+    h_inst = torch.from_numpy(ib.astype(np.int32)).pin_memory()
+    h_pos = torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
+    h_f = torch.from_numpy(np.ascontiguousarray(f)).pin_memory()
+    d_inst = torch.empty(M, dtype=torch.int32, device="cuda")
+    d_pos = torch.empty((M, 2), dtype=torch.float64, device="cuda")
+    d_f = torch.empty((M, 9), dtype=torch.float64, device="cuda")
+    o_inst = torch.empty(M, dtype=torch.int32).pin_memory()
+    o_pos = torch.empty((M, 2), dtype=torch.float64).pin_memory()
+    o_f = torch.empty((M, 9), dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    points = 0
+    h2d = d2h = 0
+    for _ in range(steps):
+        d_inst.copy_(h_inst, non_blocking=True)
+        d_pos.copy_(h_pos, non_blocking=True)
+        d_f.copy_(h_f, non_blocking=True)
+        sim.set_state(d_inst, d_pos, d_f)
+        points += M
+        sim.step(1)
+        gi, gp, gf = sim.state()
+        m2 = gi.shape[0]
+        o_inst[:m2].copy_(gi, non_blocking=True)
+        o_pos[:m2].copy_(gp, non_blocking=True)
+        o_f[:m2].copy_(gf, non_blocking=True)
+        h2d += M * (4 + 16 + 72)
+        d2h += m2 * (4 + 16 + 72)
+    e1.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1)
+    return {"value": points / (ms * 1e-3), "unit": "point-steps/s", "h2d_bytes_per_step": int(h2d // steps),
+            "d2h_bytes_per_step": int(d2h // steps), "ms_per_step": ms / steps, "wall_s": wall,
+            "path": "Simulation.set_state/step/state (C ABI dbm_sim_*) with pinned host buffers"}
+
+
+# ---- CPU oracle legs -----------------------------------------------------------------------------
+
+def _oracle_instance_steps(args):
+    n, tau, seed, steps = args
+    from direbm_gb300.lattices import D2Q9, equilibrium
+    from oracle import grid_step
+    from oracle.lattices import D2Q9 as OD2Q9
+
+    x = instance_points(n, seed)
+    u = fourier_velocity(x, n, seed)
+    f = equilibrium(np.ones(len(x)), u, D2Q9)
+    spec = grid_step.GridSpec(lattice=OD2Q9, dx=DX, r_res=R_RES, cell=CELL, kappa_hard=4,
+                              instances=[grid_step.Instance(dims=(n, n), periodic=True, tau=tau)])
+    st = grid_step.from_world(spec, np.zeros(len(x), int), x, f)
+    t0 = time.perf_counter()
+    pts = 0
+    for _ in range(steps):
+        pts += len(st.cell)
+        st = grid_step.step(spec, st)
+    return pts, time.perf_counter() - t0
+
+
+def cpu_baseline_leg(n=128, steps=2):
+    pts, sec = _oracle_instance_steps((n, 0.8, 100, steps))
+    return {"value": pts / sec, "unit": "point-steps/s", "cores": 1, "kind": "port",
+            "sample": f"numpy oracle of the step, one {n}x{n} periodic D2Q9 instance, {steps} steps, {sec:.1f} s"}
+
+
+def run_reference(args):
+    """The reference arm: the CPU oracle (numpy restatement of the reference GPU step) on all host
+    cores, one independent ensemble instance per worker process."""
+    import multiprocessing as mp
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    sides, taus = ensemble_spec()
+    # bounded sample: the first `cores` instances clipped to 64x64 (smallest ensemble size)
+    jobs = [(64, float(taus[i % len(taus)]), 100 + i, 1) for i in range(cores)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_oracle_instance_steps, jobs)
+        t0 = time.perf_counter()
+        pts = 0
+        for _ in range(args.steps):
+            pts += sum(p for p, _ in pool.map(_oracle_instance_steps, jobs))
+        sec = time.perf_counter() - t0
+    value = pts / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batched ensemble, D2Q9, r 1.5h, cell h (CPU oracle sample)",
+                   "sample": f"{cores} x 64x64 instances, 1 step each per timed step"},
+        "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} worker processes x one 64x64 instance step"},
+        "e2e": {"value": value, "unit": "point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---- main ----------------------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+
+    from direbm_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+
+    sides, taus = ensemble_spec()
+    ib, x, f = build_ensemble(sides, taus)
+    M = len(x)
+    sim = make_sim(sides, taus, "fp32dev", M)
+    sim.set_state(ib, x, f)
+
+    clk = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk.start()
+    ms, launches = timed_steps(sim, args.steps, args.warmup)
+    clocks = clk.stop()
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    P = sim.count()
+    sim.check_status()
+    value = world * M * args.steps / (ms * 1e-3)
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    dom, stage_ms, roof = roofline_from_profile(sim, sim.count(), P, peak)
+    step_ms = ms / args.steps
+    bpp = step_bytes_per_point()
+    step_roof = {"bytes_per_point_step": bpp, "achieved": bpp * M / (step_ms * 1e-3) / 1e9, "peak": peak,
+                 "unit": "GB/s"}
+    step_roof["frac"] = step_roof["achieved"] / peak
+
+    e2e = e2e_leg(sim, ib, x, f, steps=2)
+    sim.close()
+
+    # FP64 store on the same workload
+    sim64 = make_sim(sides, taus, "fp64", M)
+    sim64.set_state(ib, x, f)
+    ms64, _ = timed_steps(sim64, 2, 1)
+    sim64.close()
+    fp64 = {"value": M * 2 / (ms64 * 1e-3), "unit": "point-steps/s", "ms_per_step": ms64 / 2, "steps": 2}
+
+    acc = accuracy_leg()
+    lbm = lbm_leg()
+    cpu = cpu_baseline_leg()
+    line = {
+        "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched ensemble: 256 periodic 2D D2Q9 runs, M log-uniform 4k-256k (seed 1), "
+                               "tau U(0.55,1), 8 Fourier modes RMS 0.02, r 1.5h, cell h, FP32-deviation store",
+                   "moments": int(M), "instances": N_INST, "store": "fp32dev", "graphs": True,
+                   "l2": "state (~0.8 GB) larger than L2, no flush"},
+        "roofline": roof, "stage_ms": stage_ms, "step_roofline": step_roof,
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
+        "fp64": fp64, "speedup_fp32dev_vs_fp64": value / world / fp64["value"], "accuracy": acc, "lbm": lbm,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1121 @@
+// The fused DiReBM step (replaces direbm/warp/simulator.py:50-73 and the propagation pipeline it
+// drives, direbm/warp/propagation.py:21-275).
+//
+// One step, all on the device, no host synchronisation:
+//   k_collide       BGK relaxation of every moment in place        (warp/physics.py:45-62)
+//   k_thin_refine   per cell: gather the components landing in it (cell thinning, centroid;
+//                   propagation.py:39-68,130-153), then refine the control point with the
+//                   components within r (kappa mask, exp(f)-weighted move; propagation.py:77-112)
+//   compaction      occupied cells -> (refined cell, origin cell) pairs, P on the device
+//   radix sort      stable sort of the pairs by refined cell (the next step's moment order)
+//   k_finalize      sorted control points -> next state's cells/offsets, + cell ranges
+//   k_weights       per component: sw = sum over control points within r of (r - d)
+//                   (propagation.py:166-178; the drop rule sw <= 0 is kept)
+//   k_gather        per control point and direction: sum (r - d)/sw * f over components within r
+//                   (propagation.py:179-186 as a gather: no float atomics, fixed order)
+//   k_emit          gap fill of empty directions + emit the next moments (propagation.py:189-218)
+//
+// Every sum runs in a fixed order inside one thread, so results are bitwise reproducible run to
+// run.  FP32DEV stores f as rho (FP32) + dev_k = f_k - rho*W_k (FP32), sums with compensated
+// (TwoSum/TwoProd) FP32 accumulators and forms the emitted rho and dev in double-float.
+#include <algorithm>
+#include <vector>
+
+#include "sim.cuh"
+#include "sortscan.cuh"
+
+namespace dbm {
+
+// ---- kernels ------------------------------------------------------------------------------------
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_collide(const __grid_constant__ Args<Q, D, P> A) {
+  using real = typename P::real;
+  const uint32_t M = *A.a.count;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const uint32_t g = A.a.cell[m];
+    const int b = find_instance(A.inst_base, A.n_inst, g);
+    const InstK I = A.inst[b];
+    if constexpr (std::is_same<P, PF64>::value) {
+      double f[Q];
+#pragma unroll
+      for (int k = 0; k < Q; ++k) f[k] = A.a.f64[(int64_t)k * A.mcap + m];
+      collide_moment<Q, D, double>(f, I.tau, A.L);
+#pragma unroll
+      for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + m] = f[k];
+    } else {
+      float dv[Q];
+#pragma unroll
+      for (int k = 0; k < Q; ++k) dv[k] = A.a.dev[(int64_t)k * A.mcap + m];
+      collide_moment_dev<Q, D>(A.a.rho[m], dv, (float)I.tau, A.L);
+#pragma unroll
+      for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + m] = dv[k];
+    }
+    if (!I.periodic) {  // every component must land inside a bounded box
+      int c[3];
+      decode_cell<D>(I, g, c);
+      bool out = false;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          real t = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
+          int x = c[a] + (int)floor(t);
+          out |= (x < 0) | (x >= I.dims[a]);
+        }
+      }
+      if (out) atomicOr(A.status, ST_OUT_OF_BOX);
+    }
+  }
+}
+
+template <int Q, int D, class P>
+__device__ __forceinline__ typename P::real fstar_at(const Args<Q, D, P>& A, uint32_t m, int k) {
+  if constexpr (std::is_same<P, PF64>::value) {
+    return A.a.f64[(int64_t)k * A.mcap + m];
+  } else {
+    return __fmaf_rn(A.a.rho[m], A.L.wf[k], A.a.dev[(int64_t)k * A.mcap + m]);
+  }
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Args<Q, D, P> A) {
+  using real = typename P::real;
+  const uint32_t F = blockIdx.x * blockDim.x + threadIdx.x;
+  if (F >= A.ncells) return;
+  const int b = find_instance(A.inst_base, A.n_inst, F);
+  const InstK I = A.inst[b];
+  int Fc[3];
+  decode_cell<D>(I, F, Fc);
+
+  // ---- thinning: components landing in F (2 candidate source cells per axis per direction) ----
+  uint32_t cnt = 0;
+  real sum[3] = {0, 0, 0};
+  CSum csum[3];
+#pragma unroll 1
+  for (int k = 0; k < Q; ++k) {
+    int lo[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) lo[a] = -(int)floor((real)A.L.cd[k][a]) - 1;
+#pragma unroll 1
+    for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz)
+#pragma unroll 1
+      for (int oy = 0; oy < 2; ++oy)
+#pragma unroll 1
+        for (int ox = 0; ox < 2; ++ox) {
+          const int so[3] = {lo[0] + ox, lo[1] + oy, D == 3 ? lo[2] + oz : 0};
+          uint32_t Sg;
+          if (!cell_at<D>(I, Fc[0] + so[0], Fc[1] + so[1], Fc[2] + so[2], &Sg)) continue;
+          const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
+          for (uint32_t m = m0; m < m1; ++m) {
+            real t[3];
+            bool land = true;
+#pragma unroll
+            for (int a = 0; a < D; ++a) {
+              t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
+              land &= (so[a] + (int)floor(t[a])) == 0;
+            }
+            if (land) {
+              ++cnt;
+#pragma unroll
+              for (int a = 0; a < D; ++a) {
+                real rel = rn_add((real)so[a], t[a]);
+                if constexpr (std::is_same<P, PF64>::value) sum[a] += rel; else csum[a].add(rel);
+              }
+            }
+          }
+        }
+  }
+  if (cnt == 0) {
+    A.occ[F] = 0u;
+    if (A.write_trace) { A.tcnt[F] = 0u; A.mask[F] = 0u; }
+    return;
+  }
+  real cen[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    real s;
+    if constexpr (std::is_same<P, PF64>::value) s = sum[a]; else s = csum[a].value();
+    cen[a] = s / (real)cnt;
+  }
+
+  // ---- refine: components within R of the centroid ---------------------------------------------
+  uint32_t mask = 0;
+  double swd = 0, sxd[3] = {0, 0, 0};
+  CSum sws, sxs[3];
+#pragma unroll 1
+  for (int k = 0; k < Q; ++k) {
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      real base = cen[a] - (real)A.L.cd[k][a];
+      lo[a] = (int)floor(base - A.R - A.tiny) - 1;
+      hi[a] = (int)floor(base + A.R + A.tiny);
+    }
+#pragma unroll 1
+    for (int sz = lo[2]; sz <= hi[2]; ++sz)
+#pragma unroll 1
+      for (int sy = lo[1]; sy <= hi[1]; ++sy)
+#pragma unroll 1
+        for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+          uint32_t Sg;
+          if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
+          const int dS[3] = {sx, sy, sz};
+          const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
+          for (uint32_t m = m0; m < m1; ++m) {
+            real t[3], q[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
+            const real d = canon_dist<D, real>(dS, t, cen, q);
+            if (d <= A.R) {
+              mask |= 1u << k;
+              const real w = exp(fstar_at<Q, D, P>(A, m, k));
+              if constexpr (std::is_same<P, PF64>::value) {
+                swd += w;
+#pragma unroll
+                for (int a = 0; a < D; ++a) sxd[a] += w * q[a];
+              } else {
+                sws.add(w);
+#pragma unroll
+                for (int a = 0; a < D; ++a) sxs[a].add_prod(w, q[a]);
+              }
+            }
+          }
+        }
+  }
+  const int kappa = __popc(mask);
+  real np[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    if (kappa <= A.kappa_hard) {
+      np[a] = cen[a];
+    } else if constexpr (std::is_same<P, PF64>::value) {
+      np[a] = sxd[a] / swd;
+    } else {
+      np[a] = sxs[a].value() / sws.value();
+    }
+  }
+  bool finite = true;
+#pragma unroll
+  for (int a = 0; a < D; ++a) finite &= isfinite(np[a]) && fabs(np[a]) < (real)64;
+  if (!finite) {  // exp(f) underflowed to zero weight: keep the centroid and report it
+    atomicOr(A.status, ST_NONFINITE);
+#pragma unroll
+    for (int a = 0; a < D; ++a) np[a] = cen[a];
+  }
+  int sh[3] = {0, 0, 0};
+  real off[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    real fl = floor(np[a]);
+    sh[a] = (int)fl;
+    off[a] = np[a] - fl;
+    if (off[a] >= (real)1) {
+      off[a] = 0;
+      sh[a] += 1;
+    }
+  }
+  uint32_t G;
+  const bool inside = cell_at<D>(I, Fc[0] + sh[0], Fc[1] + sh[1], Fc[2] + sh[2], &G);
+  if (!inside) atomicOr(A.status, ST_OUT_OF_BOX);
+  A.occ[F] = inside ? 1u : 0u;
+  A.fkey[F] = inside ? G : 0xffffffffu;
+#pragma unroll
+  for (int a = 0; a < D; ++a) A.foff[(int64_t)a * A.ncells + F] = off[a];
+  if (A.write_trace) {
+    A.tcnt[F] = cnt;
+    A.mask[F] = mask;
+#pragma unroll
+    for (int a = 0; a < D; ++a) A.cen[(int64_t)a * A.ncells + F] = cen[a];
+  }
+}
+
+// Sorted pairs -> next state's cells and offsets.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_finalize(const __grid_constant__ Args<Q, D, P> A) {
+  const uint32_t Pn = *A.d_P;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < Pn; j += gridDim.x * blockDim.x) {
+    const uint32_t src = A.svals[j];
+    A.b.cell[j] = A.skeys[j];
+#pragma unroll
+    for (int a = 0; a < D; ++a) A.b.off[(int64_t)a * A.ccap + j] = A.foff[(int64_t)a * A.ncells + src];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.b.count = Pn;
+}
+
+// start[c] = number of sorted keys < c, for c in [0, ncells].
+__global__ void __launch_bounds__(256) k_cell_start(const uint32_t* __restrict__ keys, const uint32_t* d_n,
+                                                    uint32_t ncells, uint32_t* __restrict__ start) {
+  const uint32_t n = *d_n;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c <= ncells; c += gridDim.x * blockDim.x) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (keys[mid] < c) lo = mid + 1; else hi = mid;
+    }
+    start[c] = lo;
+  }
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q, D, P> A) {
+  using real = typename P::real;
+  const uint32_t M = *A.a.count;
+  const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (m >= M) return;
+  const uint32_t g = A.a.cell[m];
+  const int b = find_instance(A.inst_base, A.n_inst, g);
+  const InstK I = A.inst[b];
+  int Sc[3];
+  decode_cell<D>(I, g, Sc);
+  real t[3] = {0, 0, 0};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
+    lo[a] = (int)floor(t[a] - A.R - A.tiny) - 1;
+    hi[a] = (int)floor(t[a] + A.R + A.tiny);
+  }
+  double swd = 0;
+  CSum sws;
+#pragma unroll 1
+  for (int gz = lo[2]; gz <= hi[2]; ++gz)
+#pragma unroll 1
+    for (int gy = lo[1]; gy <= hi[1]; ++gy)
+#pragma unroll 1
+      for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+        uint32_t Gg;
+        if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Gg)) continue;
+        const int dS[3] = {-gx, -gy, -gz};
+        const uint32_t c0 = A.b.start[Gg], c1 = A.b.start[Gg + 1];
+        for (uint32_t c = c0; c < c1; ++c) {
+          real p[3], q[3];
+#pragma unroll
+          for (int a = 0; a < D; ++a) p[a] = A.b.off[(int64_t)a * A.ccap + c];
+          const real d = canon_dist<D, real>(dS, t, p, q);
+          if (d <= A.R) {
+            if constexpr (std::is_same<P, PF64>::value) swd += A.R - d; else sws.add(A.R - d);
+          }
+        }
+      }
+  real sw;
+  if constexpr (std::is_same<P, PF64>::value) sw = swd; else sw = sws.value();
+  A.sw[(int64_t)k * A.mcap + m] = sw;
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, D, P> A) {
+  using real = typename P::real;
+  const uint32_t Pn = *A.d_P;
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (j >= Pn) return;
+  const uint32_t G = A.b.cell[j];
+  const int b = find_instance(A.inst_base, A.n_inst, G);
+  const InstK I = A.inst[b];
+  int Gc[3];
+  decode_cell<D>(I, G, Gc);
+  real p[3] = {0, 0, 0};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    p[a] = A.b.off[(int64_t)a * A.ccap + j];
+    real base = p[a] - (real)A.L.cd[k][a];
+    lo[a] = (int)floor(base - A.R - A.tiny) - 1;
+    hi[a] = (int)floor(base + A.R + A.tiny);
+  }
+  double acc = 0;
+  CSum sa, sb;
+#pragma unroll 1
+  for (int sz = lo[2]; sz <= hi[2]; ++sz)
+#pragma unroll 1
+    for (int sy = lo[1]; sy <= hi[1]; ++sy)
+#pragma unroll 1
+      for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+        uint32_t Sg;
+        if (!cell_at<D>(I, Gc[0] + sx, Gc[1] + sy, Gc[2] + sz, &Sg)) continue;
+        const int dS[3] = {sx, sy, sz};
+        const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
+        for (uint32_t m = m0; m < m1; ++m) {
+          real t[3], q[3];
+#pragma unroll
+          for (int a = 0; a < D; ++a) t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
+          const real d = canon_dist<D, real>(dS, t, p, q);
+          if (d <= A.R) {
+            const real s = A.sw[(int64_t)k * A.mcap + m];
+            if (s > (real)0) {
+              const real wgt = (A.R - d) / s;
+              if constexpr (std::is_same<P, PF64>::value) {
+                acc += wgt * A.a.f64[(int64_t)k * A.mcap + m];
+              } else {
+                sa.add_prod(wgt, A.a.rho[m]);
+                sb.add_prod(wgt, A.a.dev[(int64_t)k * A.mcap + m]);
+              }
+            }
+          }
+        }
+      }
+  bool empty;
+  if constexpr (std::is_same<P, PF64>::value) {
+    A.cpf64[(int64_t)k * A.ccap + j] = acc;
+    empty = acc < (double)A.eps;
+  } else {
+    // F = W_k * A + B in double-float
+    DF Ad = df_norm(sa.hi, sa.lo);
+    DF Bd = df_norm(sb.hi, sb.lo);
+    DF Fv = df_add(df_mul(DF{A.L.wf[k], A.L.wlo[k]}, Ad), Bd);
+    A.cpfhi[(int64_t)k * A.ccap + j] = Fv.hi;
+    A.cpflo[(int64_t)k * A.ccap + j] = Fv.lo;
+    empty = Fv.hi < A.eps;
+  }
+  if (empty) atomicOr(A.emask + j, 1u << k);
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_emit(const __grid_constant__ Args<Q, D, P> A) {
+  using real = typename P::real;
+  const uint32_t Pn = *A.d_P;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < Pn; j += gridDim.x * blockDim.x) {
+    const uint32_t em = A.emask[j];
+    const uint32_t G = A.b.cell[j];
+    const int b = find_instance(A.inst_base, A.n_inst, G);
+    const InstK I = A.inst[b];
+    double swd[Q];
+    float swf[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) { swd[k] = 0; swf[k] = 0.f; }
+    if (em) {
+      int Gc[3];
+      decode_cell<D>(I, G, Gc);
+      real p[3] = {0, 0, 0};
+      int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        p[a] = A.b.off[(int64_t)a * A.ccap + j];
+        lo[a] = (int)floor(p[a] - A.R - A.tiny) - 1;
+        hi[a] = (int)floor(p[a] + A.R + A.tiny);
+      }
+      CSum sws[Q];
+#pragma unroll 1
+      for (int gz = lo[2]; gz <= hi[2]; ++gz)
+#pragma unroll 1
+        for (int gy = lo[1]; gy <= hi[1]; ++gy)
+#pragma unroll 1
+          for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+            uint32_t Hg;
+            if (!cell_at<D>(I, Gc[0] + gx, Gc[1] + gy, Gc[2] + gz, &Hg)) continue;
+            const int dS[3] = {gx, gy, gz};
+            const uint32_t c0 = A.b.start[Hg], c1 = A.b.start[Hg + 1];
+            for (uint32_t c = c0; c < c1; ++c) {
+              const uint32_t both = A.emask[c] & em;
+              if (!both) continue;
+              real t[3], q[3];
+#pragma unroll
+              for (int a = 0; a < D; ++a) t[a] = A.b.off[(int64_t)a * A.ccap + c];
+              const real d = canon_dist<D, real>(dS, t, p, q);
+              if (d <= A.R) {
+                const real w = A.R - d;
+#pragma unroll
+                for (int k = 0; k < Q; ++k) {
+                  if ((both >> k) & 1u) {
+                    if constexpr (std::is_same<P, PF64>::value) swd[k] += w; else sws[k].add(w);
+                  }
+                }
+              }
+            }
+          }
+      if constexpr (!std::is_same<P, PF64>::value) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) swf[k] = sws[k].value();
+      }
+    }
+    if constexpr (std::is_same<P, PF64>::value) {
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        double v = A.cpf64[(int64_t)k * A.ccap + j];
+        if (((em >> k) & 1u) && swd[k] > 0.0) v = ((double)A.R / swd[k]) * (I.rho_rest * A.L.w[k]);
+        A.b.f64[(int64_t)k * A.ccap + j] = v;
+      }
+    } else {
+      DF Fk[Q];
+      DF rho = {0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        if (((em >> k) & 1u) && swf[k] > 0.f) {
+          const float s = (A.R / swf[k]) * (float)I.rho_rest;
+          Fk[k] = df_mul(DF{A.L.wf[k], A.L.wlo[k]}, DF{s, 0.f});
+        } else {
+          Fk[k] = DF{A.cpfhi[(int64_t)k * A.ccap + j], A.cpflo[(int64_t)k * A.ccap + j]};
+        }
+        rho = df_add(rho, Fk[k]);
+      }
+      A.b.rho[j] = df_float(rho);
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        DF dv = df_add(Fk[k], df_neg(df_mul(DF{A.L.wf[k], A.L.wlo[k]}, rho)));
+        A.b.dev[(int64_t)k * A.ccap + j] = df_float(dv);
+      }
+    }
+  }
+}
+
+// ---- import / export ------------------------------------------------------------------------
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_import_keys(const __grid_constant__ Args<Q, D, P> A, const int32_t* __restrict__ inst_of,
+                                                     const double* __restrict__ pos, int64_t m, double cell,
+                                                     uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                     typename P::real* __restrict__ toff) {
+  using real = typename P::real;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const int b = inst_of[i];
+    uint32_t key = 0xffffffffu;
+    if (b >= 0 && b < A.n_inst) {
+      const InstK I = A.inst[b];
+      int c[3] = {0, 0, 0};
+      bool ok = true;
+#pragma unroll
+      for (int a = 0; a < D; ++a) {
+        const double s = pos[i * D + a] / cell;
+        const double fl = floor(s);
+        real o = (real)(s - fl);
+        const real one_below = std::is_same<real, float>::value ? (real)0.99999994f : (real)0.99999999999999989;
+        if (o > one_below) o = one_below;
+        toff[(int64_t)a * m + i] = o;
+        long long x = (long long)fl - I.origin[a];
+        const long long n = I.dims[a];
+        if (I.periodic) x = ((x % n) + n) % n; else ok &= (x >= 0 && x < n);
+        c[a] = (int)x;
+      }
+      uint32_t g;
+      if (ok && cell_at<D>(I, c[0], c[1], c[2], &g)) key = g;
+    }
+    if (key == 0xffffffffu) atomicOr(A.status, ST_BAD_INPUT);
+    keys[i] = key;
+    vals[i] = (uint32_t)i;
+  }
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_import_gather(const __grid_constant__ Args<Q, D, P> A, const double* __restrict__ fin, int64_t m,
+                                                       const uint32_t* __restrict__ keys,
+                                                       const uint32_t* __restrict__ vals,
+                                                       const typename P::real* __restrict__ toff) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = vals[j];
+    A.a.cell[j] = keys[j];
+#pragma unroll
+    for (int a = 0; a < D; ++a) A.a.off[(int64_t)a * A.mcap + j] = toff[(int64_t)a * m + i];
+    if constexpr (std::is_same<P, PF64>::value) {
+#pragma unroll
+      for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + j] = fin[(int64_t)i * Q + k];
+    } else {
+      double rho = 0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) rho += fin[(int64_t)i * Q + k];
+      A.a.rho[j] = (float)rho;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + j] = (float)(fin[(int64_t)i * Q + k] - rho * A.L.w[k]);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.a.count = (uint32_t)m;
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_export(const __grid_constant__ Args<Q, D, P> A, double cell, int32_t* __restrict__ inst_out,
+                                                double* __restrict__ pos, double* __restrict__ fout) {
+  const uint32_t M = *A.a.count;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
+    const uint32_t g = A.a.cell[j];
+    const int b = find_instance(A.inst_base, A.n_inst, g);
+    const InstK I = A.inst[b];
+    int c[3];
+    decode_cell<D>(I, g, c);
+    if (inst_out) inst_out[j] = b;
+    if (pos) {
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+        pos[(int64_t)j * D + a] = ((double)(I.origin[a] + c[a]) + (double)A.a.off[(int64_t)a * A.mcap + j]) * cell;
+    }
+    if (fout) {
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        double v;
+        if constexpr (std::is_same<P, PF64>::value) v = A.a.f64[(int64_t)k * A.mcap + j];
+        else v = (double)A.a.rho[j] * A.L.w[k] + (double)A.a.dev[(int64_t)k * A.mcap + j];
+        fout[(int64_t)j * Q + k] = v;
+      }
+    }
+  }
+}
+
+// Per-instance FP64 mass and momentum, one block per instance, fixed reduction order.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_conservation(const __grid_constant__ Args<Q, D, P> A, double* __restrict__ out) {
+  const int b = blockIdx.x;
+  const InstK I = A.inst[b];
+  const uint32_t m0 = A.a.start[I.base];
+  const uint32_t m1 = A.a.start[A.inst_base[b + 1]];
+  double acc[1 + D];
+#pragma unroll
+  for (int i = 0; i <= D; ++i) acc[i] = 0;
+  for (uint32_t m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      double f;
+      if constexpr (std::is_same<P, PF64>::value) f = A.a.f64[(int64_t)k * A.mcap + m];
+      else f = (double)A.a.rho[m] * A.L.w[k] + (double)A.a.dev[(int64_t)k * A.mcap + m];
+      acc[0] += f;
+#pragma unroll
+      for (int a = 0; a < D; ++a) acc[1 + a] += f * A.L.c[k][a];
+    }
+  }
+  __shared__ double red[256];
+#pragma unroll 1
+  for (int i = 0; i <= D; ++i) {
+    red[threadIdx.x] = acc[i];
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[(int64_t)b * (1 + D) + i] = red[0];
+    __syncthreads();
+  }
+}
+
+// ---- host side ------------------------------------------------------------------------------------
+
+struct SimBase {
+  virtual ~SimBase() = default;
+  virtual int set_state(const int32_t*, const double*, const double*, int64_t, cudaStream_t) = 0;
+  virtual int step(int, cudaStream_t) = 0;
+  virtual int step_partial(int, cudaStream_t) = 0;
+  virtual int profile_step(float*, cudaStream_t) = 0;
+  virtual int count(int64_t*, cudaStream_t) = 0;
+  virtual int get_state(int32_t*, double*, double*, cudaStream_t) = 0;
+  virtual int status(uint32_t*, int, cudaStream_t) = 0;
+  virtual int conservation(double*, cudaStream_t) = 0;
+  virtual int trace(int, void*, int64_t, int64_t*, cudaStream_t) = 0;
+  virtual int64_t device_bytes() const = 0;
+  int use_graphs = 1;
+};
+
+template <int Q, int D, class P>
+struct SimImpl : SimBase {
+  using real = typename P::real;
+  dbm_sim_desc desc{};
+  std::vector<InstK> inst_h;
+  uint32_t ncells = 0;
+  int key_bits = 1;
+  int64_t mcap = 0, ccap = 0;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  Args<Q, D, P> args{};  // args for the current direction (a = current state)
+  StateP<P> st[2];
+  int cur = 0;
+  // sort buffers
+  uint32_t *k_in = nullptr, *v_in = nullptr, *k_alt = nullptr, *v_alt = nullptr;
+  bool sorted_in_alt = false;
+  void* sort_tmp = nullptr;
+  void* compact_tmp = nullptr;
+  cudaStream_t own = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  unsigned long long graph_kernels = 0;
+  int trace_on = 0;
+
+  ~SimImpl() override {
+    for (auto& g : graph)
+      if (g) cudaGraphExecDestroy(g);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (own) cudaStreamDestroy(own);
+    for (void* p : allocs) cudaFree(p);
+  }
+
+  template <class T>
+  int alloc(T** p, int64_t n) {
+    size_t b = (size_t)std::max<int64_t>(n, 1) * sizeof(T);
+    void* q = nullptr;
+    DBM_CUDA(cudaMalloc(&q, b));
+    allocs.push_back(q);
+    bytes += (int64_t)b;
+    *p = (T*)q;
+    return DBM_OK;
+  }
+
+  int init(const dbm_sim_desc& d, const dbm_instance_desc* in, int n) {
+    desc = d;
+    const LatHost& LH = *lat_host(d.lattice);
+    const double R = d.r_res / d.cell;
+    double cmax = 0;
+    for (int k = 0; k < Q; ++k) {
+      double s = 0;
+      for (int a = 0; a < D; ++a) s += LH.c[k][a] * LH.c[k][a];
+      cmax = std::max(cmax, std::sqrt(s) * d.dx / d.cell);
+    }
+    const int need = 2 * (int)std::ceil(R + cmax) + 4;  // periodic boxes must exceed every window
+    uint64_t total = 0;
+    inst_h.resize(n);
+    for (int i = 0; i < n; ++i) {
+      InstK& I = inst_h[i];
+      I.base = (uint32_t)total;
+      uint64_t sz = 1;
+      for (int a = 0; a < 3; ++a) {
+        I.dims[a] = a < D ? in[i].dims[a] : 1;
+        I.origin[a] = a < D ? in[i].origin[a] : 0;
+        if (I.dims[a] < 1) { set_last_error("instance %d: dims must be >= 1", i); return DBM_ERR_INVALID; }
+        if (a < D && in[i].periodic && I.dims[a] < need) {
+          set_last_error("instance %d: periodic box needs >= %d cells per axis (got %d)", i, need, I.dims[a]);
+          return DBM_ERR_INVALID;
+        }
+        sz *= (uint64_t)I.dims[a];
+      }
+      I.periodic = in[i].periodic ? 1 : 0;
+      if (!(in[i].tau > 0.5)) { set_last_error("instance %d: tau must be > 1/2", i); return DBM_ERR_INVALID; }
+      I.tau = in[i].tau;
+      I.rho_rest = in[i].rho_rest;
+      total += sz;
+    }
+    if (total + 1 >= 0xffffffffull) { set_last_error("too many cells (%llu)", (unsigned long long)total); return DBM_ERR_CAPACITY; }
+    ncells = (uint32_t)total;
+    key_bits = 1;
+    while (((uint64_t)1 << key_bits) <= (uint64_t)ncells) ++key_bits;
+    ccap = ncells;
+    mcap = std::max<int64_t>(d.moment_capacity, ncells);
+    if (mcap >= 0x7fffffffLL) { set_last_error("moment capacity too large"); return DBM_ERR_CAPACITY; }
+
+    InstK* dinst;
+    uint32_t* dbase;
+    DBM_TRY(alloc(&dinst, n));
+    DBM_TRY(alloc(&dbase, n + 1));
+    std::vector<uint32_t> hb(n + 1);
+    for (int i = 0; i < n; ++i) hb[i] = inst_h[i].base;
+    hb[n] = ncells;
+    DBM_CUDA(cudaMemcpy(dinst, inst_h.data(), sizeof(InstK) * n, cudaMemcpyHostToDevice));
+    DBM_CUDA(cudaMemcpy(dbase, hb.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice));
+
+    for (int s = 0; s < 2; ++s) {
+      StateP<P>& S = st[s];
+      const int64_t cap = std::max(mcap, ccap);
+      DBM_TRY(alloc(&S.cell, cap));
+      DBM_TRY(alloc(&S.off, (int64_t)D * cap));
+      if constexpr (std::is_same<P, PF64>::value) {
+        DBM_TRY(alloc(&S.f64, (int64_t)Q * cap));
+      } else {
+        DBM_TRY(alloc(&S.rho, cap));
+        DBM_TRY(alloc(&S.dev, (int64_t)Q * cap));
+      }
+      DBM_TRY(alloc(&S.start, (int64_t)ncells + 1));
+      DBM_TRY(alloc(&S.count, 1));
+      DBM_CUDA(cudaMemset(S.count, 0, 4));
+      DBM_CUDA(cudaMemset(S.start, 0, ((size_t)ncells + 1) * 4));
+    }
+    // both state buffers share one capacity so they can swap roles
+    mcap = ccap = std::max(mcap, ccap);
+
+    Args<Q, D, P>& A = args;
+    A.L = make_latk<Q, D>(LH, d.dx, d.cell);
+    A.inst = dinst;
+    A.inst_base = dbase;
+    A.n_inst = n;
+    A.ncells = ncells;
+    A.R = (real)R;
+    A.tiny = (real)1e-4;
+    A.kappa_hard = d.kappa_hard;
+    A.eps = (real)d.eps;
+    A.mcap = mcap;
+    A.ccap = ccap;
+    DBM_TRY(alloc(&A.occ, ncells));
+    DBM_TRY(alloc(&A.tcnt, ncells));
+    DBM_TRY(alloc(&A.cen, (int64_t)D * ncells));
+    DBM_TRY(alloc(&A.mask, ncells));
+    DBM_TRY(alloc(&A.fkey, ncells));
+    DBM_TRY(alloc(&A.foff, (int64_t)D * ncells));
+    const int64_t sort_cap = std::max<int64_t>(ncells, mcap);  // set_state sorts up to mcap moments
+    DBM_TRY(alloc(&k_in, sort_cap));
+    DBM_TRY(alloc(&v_in, sort_cap));
+    DBM_TRY(alloc(&k_alt, sort_cap));
+    DBM_TRY(alloc(&v_alt, sort_cap));
+    char* tmp;
+    DBM_TRY(alloc(&tmp, (int64_t)radix_tmp_bytes(sort_cap)));
+    sort_tmp = tmp;
+    DBM_TRY(alloc(&tmp, (int64_t)compact_tmp_bytes(ncells)));
+    compact_tmp = tmp;
+    DBM_TRY(alloc(&A.sw, (int64_t)Q * mcap));
+    if constexpr (std::is_same<P, PF64>::value) {
+      DBM_TRY(alloc(&A.cpf64, (int64_t)Q * ccap));
+    } else {
+      DBM_TRY(alloc(&A.cpfhi, (int64_t)Q * ccap));
+      DBM_TRY(alloc(&A.cpflo, (int64_t)Q * ccap));
+    }
+    DBM_TRY(alloc(&A.emask, ccap));
+    DBM_TRY(alloc(&A.status, 1));
+    DBM_TRY(alloc(&A.d_P, 1));
+    DBM_CUDA(cudaMemset(A.status, 0, 4));
+    DBM_CUDA(cudaMemset(A.d_P, 0, 4));
+    DBM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+    DBM_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+    DBM_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+    return DBM_OK;
+  }
+
+  void bind() {
+    args.a = st[cur];
+    args.b = st[cur ^ 1];
+    args.write_trace = trace_on;
+  }
+
+  int import_sorted_states(int64_t m, cudaStream_t s, const int32_t* inst_of, const double* pos, const double* fin) {
+    bind();
+    real* toff;
+    DBM_TRY(alloc(&toff, (int64_t)D * std::max<int64_t>(m, 1)));  // freed with the handle (rare call)
+    const unsigned grid = std::min<unsigned>(div_up(std::max<int64_t>(m, 1), 256), (unsigned)sm_count() * 8);
+    k_import_keys<Q, D, P><<<grid, 256, 0, s>>>(args, inst_of, pos, m, desc.cell, k_in, v_in, toff);
+    DBM_LAUNCH_CHECK();
+    bool alt = false;
+    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, m, nullptr, 32, sort_tmp, s, &alt));
+    const uint32_t* ks = alt ? k_alt : k_in;
+    const uint32_t* vs = alt ? v_alt : v_in;
+    k_import_gather<Q, D, P><<<grid, 256, 0, s>>>(args, fin, m, ks, vs, toff);
+    DBM_LAUNCH_CHECK();
+    // count of valid keys = m (invalid ones sort last with key 0xffffffff and raise ST_BAD_INPUT)
+    DBM_CUDA(cudaMemcpyAsync(args.d_P, args.a.count, 4, cudaMemcpyDeviceToDevice, s));
+    k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, s>>>(
+        ks, args.d_P, ncells, args.a.start);
+    DBM_LAUNCH_CHECK();
+    // release the temporary offsets right away
+    DBM_CUDA(cudaStreamSynchronize(s));
+    cudaFree(toff);
+    allocs.pop_back();
+    bytes -= (int64_t)((size_t)D * std::max<int64_t>(m, 1) * sizeof(real));
+    return DBM_OK;
+  }
+
+  int set_state(const int32_t* inst_of, const double* pos, const double* fin, int64_t m, cudaStream_t s) override {
+    if (m < 0 || m > mcap) { set_last_error("set_state: %lld moments exceed capacity %lld", (long long)m, (long long)mcap); return DBM_ERR_CAPACITY; }
+    if (m > 0 && (!inst_of || !pos || !fin)) { set_last_error("set_state: null input"); return DBM_ERR_INVALID; }
+    cur = 0;
+    return import_sorted_states(m, s, inst_of, pos, fin);
+  }
+
+  // Launch the stages of one step (a = st[cur] -> b = st[cur^1]) on stream s, up to `upto`.
+  cudaEvent_t* stage_ev = nullptr;  // when set, an event is recorded after each stage
+  void mark(int i, cudaStream_t s) {
+    if (stage_ev) cudaEventRecord(stage_ev[i], s);
+  }
+
+  int launch_step(cudaStream_t s, int upto) {
+    bind();
+    Args<Q, D, P>& A = args;
+    mark(0, s);
+    const unsigned gm = std::min<unsigned>(div_up(mcap, 256), (unsigned)sm_count() * 16);
+    k_collide<Q, D, P><<<gm, 256, 0, s>>>(A);
+    DBM_LAUNCH_CHECK();
+    mark(1, s);
+    if (upto <= 1) return DBM_OK;
+    k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
+    DBM_LAUNCH_CHECK();
+    mark(2, s);
+    if (upto <= 2) return DBM_OK;
+    DBM_TRY(compact_flags_u32(A.occ, A.fkey, k_in, v_in, ncells, A.d_P, compact_tmp, s));
+    bool alt = false;
+    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, ncells, A.d_P, key_bits, sort_tmp, s, &alt));
+    sorted_in_alt = alt;
+    A.skeys = alt ? k_alt : k_in;
+    A.svals = alt ? v_alt : v_in;
+    const unsigned gc = std::min<unsigned>(div_up(ccap, 256), (unsigned)sm_count() * 16);
+    k_finalize<Q, D, P><<<gc, 256, 0, s>>>(A);
+    DBM_LAUNCH_CHECK();
+    k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, s>>>(
+        A.skeys, A.d_P, ncells, A.b.start);
+    DBM_LAUNCH_CHECK();
+    mark(3, s);
+    if (upto <= 3) return DBM_OK;
+    k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
+    DBM_LAUNCH_CHECK();
+    mark(4, s);
+    if (upto <= 4) return DBM_OK;
+    DBM_CUDA(cudaMemsetAsync(A.emask, 0, (size_t)ccap * 4, s));
+    k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
+    DBM_LAUNCH_CHECK();
+    mark(5, s);
+    if (upto <= 5) return DBM_OK;
+    k_emit<Q, D, P><<<gc, 256, 0, s>>>(A);
+    DBM_LAUNCH_CHECK();
+    mark(6, s);
+    return DBM_OK;
+  }
+
+  int step(int n, cudaStream_t s) override {
+    if (n <= 0) return DBM_OK;
+    DBM_CUDA(cudaEventRecord(ev_in, s));
+    DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
+    for (int i = 0; i < n; ++i) {
+      if (use_graphs && !trace_on) {
+        if (!graph[cur]) {
+          const unsigned long long before = g_launches;
+          cudaGraph_t gr;
+          DBM_CUDA(cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal));
+          int rc = launch_step(own, 99);
+          cudaError_t e = cudaStreamEndCapture(own, &gr);
+          if (rc != DBM_OK) return rc;
+          if (e != cudaSuccess) { set_last_error("graph capture failed: %s", cudaGetErrorString(e)); return DBM_ERR_CUDA; }
+          graph_kernels = g_launches - before;
+          g_launches = before;
+          DBM_CUDA(cudaGraphInstantiate(&graph[cur], gr, 0));
+          cudaGraphDestroy(gr);
+        }
+        DBM_CUDA(cudaGraphLaunch(graph[cur], own));
+        count_launch(graph_kernels);
+      } else {
+        DBM_TRY(launch_step(own, 99));
+      }
+      cur ^= 1;
+    }
+    bind();
+    DBM_CUDA(cudaEventRecord(ev_out, own));
+    DBM_CUDA(cudaStreamWaitEvent(s, ev_out, 0));
+    return DBM_OK;
+  }
+
+  // One full step launched stage by stage (no graph) with an event after each stage; stage_ms
+  // receives the 6 stage durations (collide, thin+refine, compaction+sort+finalize, weights,
+  // gather, emit) measured on the stream the kernels run on.
+  int profile_step(float* stage_ms, cudaStream_t s) override {
+    cudaEvent_t ev[7];
+    for (auto& e : ev) DBM_CUDA(cudaEventCreate(&e));
+    DBM_CUDA(cudaEventRecord(ev_in, s));
+    DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
+    stage_ev = ev;
+    int rc = launch_step(own, 99);
+    stage_ev = nullptr;
+    if (rc == DBM_OK) {
+      cur ^= 1;
+      bind();
+      DBM_CUDA(cudaEventRecord(ev_out, own));
+      DBM_CUDA(cudaStreamWaitEvent(s, ev_out, 0));
+      DBM_CUDA(cudaEventSynchronize(ev[6]));
+      for (int i = 0; i < 6; ++i) cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]);
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+  }
+
+  int step_partial(int upto, cudaStream_t s) override {
+    trace_on = 1;
+    DBM_CUDA(cudaEventRecord(ev_in, s));
+    DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
+    int rc = launch_step(own, upto);
+    DBM_CUDA(cudaEventRecord(ev_out, own));
+    DBM_CUDA(cudaStreamWaitEvent(s, ev_out, 0));
+    if (rc != DBM_OK) return rc;
+    if (upto >= 6) { cur ^= 1; }
+    bind();
+    return DBM_OK;
+  }
+
+  int count(int64_t* m, cudaStream_t s) override {
+    uint32_t h = 0;
+    DBM_CUDA(cudaMemcpyAsync(&h, st[cur].count, 4, cudaMemcpyDeviceToHost, s));
+    DBM_CUDA(cudaStreamSynchronize(s));
+    *m = h;
+    return DBM_OK;
+  }
+
+  int get_state(int32_t* inst_out, double* pos, double* fout, cudaStream_t s) override {
+    bind();
+    const unsigned grid = std::min<unsigned>(div_up(mcap, 256), (unsigned)sm_count() * 8);
+    k_export<Q, D, P><<<grid, 256, 0, s>>>(args, desc.cell, inst_out, pos, fout);
+    DBM_LAUNCH_CHECK();
+    return DBM_OK;
+  }
+
+  int status(uint32_t* flags, int clear, cudaStream_t s) override {
+    uint32_t h = 0;
+    DBM_CUDA(cudaMemcpyAsync(&h, args.status, 4, cudaMemcpyDeviceToHost, s));
+    if (clear) DBM_CUDA(cudaMemsetAsync(args.status, 0, 4, s));
+    DBM_CUDA(cudaStreamSynchronize(s));
+    *flags = h;
+    return DBM_OK;
+  }
+
+  int conservation(double* out, cudaStream_t s) override {
+    bind();
+    k_conservation<Q, D, P><<<args.n_inst, 256, 0, s>>>(args, out);
+    DBM_LAUNCH_CHECK();
+    return DBM_OK;
+  }
+
+  int trace(int what, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) override {
+    const void* src = nullptr;
+    int64_t sz = 0;
+    const Args<Q, D, P>& A = args;
+    switch (what) {
+      case DBM_TRACE_OCC: src = A.occ; sz = (int64_t)ncells * 4; break;
+      case DBM_TRACE_THIN_CNT: src = A.tcnt; sz = (int64_t)ncells * 4; break;
+      case DBM_TRACE_CENTROID: src = A.cen; sz = (int64_t)D * ncells * sizeof(real); break;
+      case DBM_TRACE_MASK: src = A.mask; sz = (int64_t)ncells * 4; break;
+      case DBM_TRACE_FINAL_CELL: src = A.fkey; sz = (int64_t)ncells * 4; break;
+      case DBM_TRACE_FINAL_OFF: src = A.foff; sz = (int64_t)D * ncells * sizeof(real); break;
+      case DBM_TRACE_SW: src = A.sw; sz = (int64_t)Q * mcap * sizeof(real); break;
+      case DBM_TRACE_EMPTY: src = A.emask; sz = ccap * 4; break;
+      case DBM_TRACE_FSTAR:
+        if constexpr (std::is_same<P, PF64>::value) { src = A.a.f64; sz = (int64_t)Q * mcap * 8; }
+        else { src = A.a.dev; sz = (int64_t)Q * mcap * 4; }
+        break;
+      case DBM_TRACE_CPF:
+        if constexpr (std::is_same<P, PF64>::value) { src = A.cpf64; sz = (int64_t)Q * ccap * 8; }
+        else {
+          sz = (int64_t)2 * Q * ccap * 4;
+          if (needed) *needed = sz;
+          if (dst) {
+            if (nbytes < sz) { set_last_error("trace: destination too small"); return DBM_ERR_INVALID; }
+            DBM_CUDA(cudaMemcpyAsync(dst, A.cpfhi, (size_t)Q * ccap * 4, cudaMemcpyDeviceToDevice, s));
+            DBM_CUDA(cudaMemcpyAsync((char*)dst + (size_t)Q * ccap * 4, A.cpflo, (size_t)Q * ccap * 4,
+                                     cudaMemcpyDeviceToDevice, s));
+          }
+          return DBM_OK;
+        }
+        break;
+      case DBM_TRACE_SORTED: {
+        sz = (int64_t)2 * ncells * 4;
+        if (needed) *needed = sz;
+        if (dst) {
+          if (nbytes < sz) { set_last_error("trace: destination too small"); return DBM_ERR_INVALID; }
+          const uint32_t* ks = sorted_in_alt ? k_alt : k_in;
+          const uint32_t* vs = sorted_in_alt ? v_alt : v_in;
+          DBM_CUDA(cudaMemcpyAsync(dst, ks, (size_t)ncells * 4, cudaMemcpyDeviceToDevice, s));
+          DBM_CUDA(cudaMemcpyAsync((char*)dst + (size_t)ncells * 4, vs, (size_t)ncells * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        return DBM_OK;
+      }
+      case DBM_TRACE_COUNTS: {
+        sz = 8;
+        if (needed) *needed = sz;
+        if (dst) {
+          if (nbytes < sz) { set_last_error("trace: destination too small"); return DBM_ERR_INVALID; }
+          DBM_CUDA(cudaMemcpyAsync(dst, A.a.count, 4, cudaMemcpyDeviceToDevice, s));
+          DBM_CUDA(cudaMemcpyAsync((char*)dst + 4, A.d_P, 4, cudaMemcpyDeviceToDevice, s));
+        }
+        return DBM_OK;
+      }
+      default: set_last_error("trace: unknown buffer %d", what); return DBM_ERR_INVALID;
+    }
+    if (needed) *needed = sz;
+    if (dst) {
+      if (nbytes < sz) { set_last_error("trace: destination too small"); return DBM_ERR_INVALID; }
+      DBM_CUDA(cudaMemcpyAsync(dst, src, (size_t)sz, cudaMemcpyDeviceToDevice, s));
+    }
+    return DBM_OK;
+  }
+
+  int64_t device_bytes() const override { return bytes; }
+};
+
+}  // namespace dbm
+
+using namespace dbm;
+
+struct dbm_sim {
+  SimBase* impl;
+};
+
+template <class P>
+static int make_impl(const dbm_sim_desc& d, const dbm_instance_desc* in, int n, SimBase** out) {
+  return dispatch_lattice(d.lattice, [&](auto tag) -> int {
+    using LT = decltype(tag);
+    auto* s = new SimImpl<LT::Q, LT::D, P>();
+    int rc = s->init(d, in, n);
+    if (rc != DBM_OK) { delete s; return rc; }
+    *out = s;
+    return DBM_OK;
+  });
+}
+
+extern "C" {
+
+int dbm_sim_create(const dbm_sim_desc* desc, const dbm_instance_desc* inst, int32_t n_inst, dbm_sim** out) {
+  if (!desc || !inst || n_inst < 1 || !out) { set_last_error("dbm_sim_create: bad arguments"); return DBM_ERR_INVALID; }
+  if (!(desc->dx > 0) || !(desc->r_res > 0) || !(desc->cell > 0) || desc->moment_capacity < 0) {
+    set_last_error("dbm_sim_create: dx, r_res and cell must be > 0");
+    return DBM_ERR_INVALID;
+  }
+  if (desc->precision != DBM_FP64 && desc->precision != DBM_FP32DEV) {
+    set_last_error("dbm_sim_create: unknown precision %d", desc->precision);
+    return DBM_ERR_INVALID;
+  }
+  SimBase* impl = nullptr;
+  int rc = desc->precision == DBM_FP64 ? make_impl<PF64>(*desc, inst, n_inst, &impl)
+                                       : make_impl<PF32>(*desc, inst, n_inst, &impl);
+  if (rc != DBM_OK) return rc;
+  *out = new dbm_sim{impl};
+  return DBM_OK;
+}
+
+int dbm_sim_destroy(dbm_sim* s) {
+  if (!s) return DBM_OK;
+  delete s->impl;
+  delete s;
+  return DBM_OK;
+}
+
+#define SIM_CHECK(s)                                           \
+  if (!(s) || !(s)->impl) {                                    \
+    set_last_error("null simulator handle");                   \
+    return DBM_ERR_INVALID;                                    \
+  }
+
+int dbm_sim_set_state(dbm_sim* s, const int32_t* inst, const double* pos, const double* f, int64_t m, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->set_state(inst, pos, f, m, (cudaStream_t)stream);
+}
+int dbm_sim_step(dbm_sim* s, int32_t steps, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->step(steps, (cudaStream_t)stream);
+}
+int dbm_sim_step_partial(dbm_sim* s, int32_t stage, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->step_partial(stage, (cudaStream_t)stream);
+}
+int dbm_sim_profile_step(dbm_sim* s, float* stage_ms, void* stream) {
+  SIM_CHECK(s);
+  if (!stage_ms) return DBM_ERR_INVALID;
+  return s->impl->profile_step(stage_ms, (cudaStream_t)stream);
+}
+int dbm_sim_count(dbm_sim* s, int64_t* m, void* stream) {
+  SIM_CHECK(s);
+  if (!m) return DBM_ERR_INVALID;
+  return s->impl->count(m, (cudaStream_t)stream);
+}
+int dbm_sim_get_state(dbm_sim* s, int32_t* inst, double* pos, double* f, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->get_state(inst, pos, f, (cudaStream_t)stream);
+}
+int dbm_sim_status(dbm_sim* s, uint32_t* flags, int32_t clear, void* stream) {
+  SIM_CHECK(s);
+  if (!flags) return DBM_ERR_INVALID;
+  return s->impl->status(flags, clear, (cudaStream_t)stream);
+}
+int dbm_sim_conservation(dbm_sim* s, double* out, void* stream) {
+  SIM_CHECK(s);
+  if (!out) return DBM_ERR_INVALID;
+  return s->impl->conservation(out, (cudaStream_t)stream);
+}
+int dbm_sim_use_graphs(dbm_sim* s, int32_t on) {
+  SIM_CHECK(s);
+  s->impl->use_graphs = on ? 1 : 0;
+  return DBM_OK;
+}
+int dbm_sim_trace(dbm_sim* s, int32_t what, void* dst, int64_t bytes, int64_t* needed, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->trace(what, dst, bytes, needed, (cudaStream_t)stream);
+}
+int64_t dbm_sim_device_bytes(dbm_sim* s) {
+  if (!s || !s->impl) return -1;
+  return s->impl->device_bytes();
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+// The fused DiReBM step on a dense cell grid: device-side data structures and helpers.
+//
+// Geometry: a batch of instances, each a box of dims[0] x dims[1] (x dims[2]) cells of size
+// `cell` (the thinning cell).  Cells of all instances are numbered globally, instance by
+// instance, row-major (x fastest) inside each.  A moment is (global cell, offset in [0,1)^D in
+// cell units) and the moments are kept sorted by global cell, with start[c] .. start[c+1] the
+// moments of cell c -- the "hash grid built from sorted cell ranges", exact (no aliasing) because
+// the grid is dense.  Components are never materialised: the component of moment m in direction
+// k sits at S + off + cd_k (cd_k = c_k*dx/cell) and every kernel recomputes it with the same
+// round-to-nearest operations, so each (m, k) makes the same integer decisions everywhere.
+#pragma once
+
+#include <type_traits>
+
+#include "lattice.cuh"
+
+namespace dbm {
+
+struct InstK {
+  uint32_t base;     // first global cell
+  int32_t dims[3];
+  int32_t origin[3];
+  int32_t periodic;
+  double tau;
+  double rho_rest;
+};
+
+struct PF64 {
+  using real = double;
+  static constexpr int id = DBM_FP64;
+};
+struct PF32 {
+  using real = float;
+  static constexpr int id = DBM_FP32DEV;
+};
+
+template <class P>
+struct StateP {
+  using real = typename P::real;
+  uint32_t* cell = nullptr;   // [cap]
+  real* off = nullptr;        // [D][cap]
+  double* f64 = nullptr;      // FP64: [Q][cap]
+  float* rho = nullptr;       // FP32DEV: [cap]
+  float* dev = nullptr;       // FP32DEV: [Q][cap]
+  uint32_t* start = nullptr;  // [ncells + 1]
+  uint32_t* count = nullptr;  // device scalar
+};
+
+template <int Q, int D, class P>
+struct Args {
+  using real = typename P::real;
+  LatK<Q, D> L;
+  const InstK* inst;
+  const uint32_t* inst_base;  // [n_inst + 1]
+  int n_inst;
+  uint32_t ncells;
+  real R;          // r_res / cell
+  real tiny;       // window safety margin (cell units)
+  int kappa_hard;
+  real eps;
+  int64_t mcap;    // moment buffer capacity
+  int64_t ccap;    // control-point buffer capacity (= ncells)
+  StateP<P> a;     // input moments (collided in place)
+  StateP<P> b;     // output moments (= sorted control points)
+  // scratch, per cell
+  uint32_t* occ;
+  uint32_t* tcnt;
+  real* cen;       // [D][ncells]
+  uint32_t* mask;
+  uint32_t* fkey;
+  real* foff;      // [D][ncells]
+  // sort (keys_in/vals_in before, skeys/svals = the sorted result)
+  uint32_t* skeys;
+  uint32_t* svals;
+  // resampling
+  real* sw;        // [Q][mcap]
+  double* cpf64;   // FP64: [Q][ccap]
+  float* cpfhi;    // FP32DEV: [Q][ccap]
+  float* cpflo;    // FP32DEV: [Q][ccap]
+  uint32_t* emask; // [ccap]
+  uint32_t* status;
+  uint32_t* d_P;
+  int write_trace;
+};
+
+// ---- geometry helpers ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int find_instance(const uint32_t* __restrict__ base, int n, uint32_t g) {
+  int lo = 0, hi = n;  // invariant: base[lo] <= g < base[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(base + mid) <= g) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+template <int D>
+__device__ __forceinline__ void decode_cell(const InstK& I, uint32_t g, int (&c)[3]) {
+  uint32_t local = g - I.base;
+  c[0] = (int)(local % (uint32_t)I.dims[0]);
+  local /= (uint32_t)I.dims[0];
+  if (D == 3) {
+    c[1] = (int)(local % (uint32_t)I.dims[1]);
+    c[2] = (int)(local / (uint32_t)I.dims[1]);
+  } else {
+    c[1] = (int)local;
+    c[2] = 0;
+  }
+}
+
+// Global cell of unwrapped integer coordinates, or false if a bounded box has no such cell.
+// Offsets are at most a few cells, far below the minimum box size, so one wrap suffices.
+template <int D>
+__device__ __forceinline__ bool cell_at(const InstK& I, int x, int y, int z, uint32_t* g) {
+  const int nx = I.dims[0], ny = I.dims[1], nz = I.dims[2];
+  if (I.periodic) {
+    x = x < 0 ? x + nx : (x >= nx ? x - nx : x);
+    y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+    if (D == 3) z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
+  } else {
+    if (x < 0 || x >= nx || y < 0 || y >= ny) return false;
+    if (D == 3 && (z < 0 || z >= nz)) return false;
+  }
+  uint32_t lin = (uint32_t)x + (uint32_t)nx * ((uint32_t)y + (D == 3 ? (uint32_t)ny * (uint32_t)z : 0u));
+  *g = I.base + lin;
+  return true;
+}
+
+// e = (float(dS) + t) - p and |e| with round-to-nearest steps in a fixed order (the oracle's
+// canonical displacement; see oracle/grid_step.py).
+template <int D, class T>
+__device__ __forceinline__ T canon_dist(const int (&dS)[3], const T (&t)[3], const T (&p)[3], T (&q)[3]) {
+  T s = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    q[a] = rn_add((T)dS[a], t[a]);
+    T e = rn_sub(q[a], p[a]);
+    T e2 = rn_mul(e, e);
+    s = a == 0 ? e2 : rn_add(s, e2);
+  }
+  return rn_sqrt(s);
+}
+
+template <class P>
+__device__ __forceinline__ typename P::real floor_r(typename P::real x) { return floor(x); }
+
+}  // namespace dbm

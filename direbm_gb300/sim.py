@@ -1,0 +1,219 @@
+"""Batched DiReBM simulation on one GPU (host side of the fused CUDA step).
+
+``Simulation`` owns a ``dbm_sim`` handle (include/direbm_gb300.h): a batch of independent
+instances -- each a box of cells, periodic or bounded, with its own tau and rest density --
+advanced together by the fused step kernels.  It is the engine behind the drop-in
+``direbm_gb300.warp.GpuSimulator`` (the reference's direbm/warp/simulator.py:25-77) and behind
+the batched-ensemble benchmark.
+
+Parameters follow the reference's names (dx, kappa_hard, rho_rest, tau) plus the
+generalisations the benchmark configurations need: ``r_res`` (resampling radius; reference: dx),
+``cell`` (thinning cell; reference: dx/alpha), ``lattice`` and ``precision``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .lattices import get as get_lattice
+
+
+@dataclass
+class Instance:
+    """One independent simulation box: ``dims`` cells per axis, world origin ``origin`` (cells)."""
+
+    dims: tuple
+    origin: tuple = (0, 0, 0)
+    periodic: bool = True
+    tau: float = 0.6
+    rho_rest: float = 1.0
+
+
+_PREC = {"fp64": _lib.FP64, "fp32dev": _lib.FP32DEV, "fp32": _lib.FP32DEV}
+
+
+def _require_cuda(device=None) -> torch.device:
+    if not torch.cuda.is_available():
+        raise _lib.DbmError("a CUDA device is required (the DiReBM kernels have no CPU path)")
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    if dev.type != "cuda":
+        raise _lib.DbmError(f"device {dev} is not a CUDA device")
+    return dev
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Simulation:
+    def __init__(
+        self,
+        instances,
+        *,
+        lattice="D2Q9",
+        precision="fp32dev",
+        dx: float = 1.0,
+        r_res: float | None = None,
+        cell: float | None = None,
+        alpha: float = 4.0,
+        kappa_hard: int = 4,
+        eps: float = 1e-6,
+        moment_capacity: int = 0,
+        graphs: bool = True,
+        device=None,
+    ):
+        self.device = _require_cuda(device)
+        self.lib = _lib.load()
+        self.lattice = get_lattice(lattice)
+        if precision not in _PREC:
+            raise ValueError(f"precision must be one of {sorted(_PREC)}")
+        self.precision = "fp64" if _PREC[precision] == _lib.FP64 else "fp32dev"
+        self.dx = float(dx)
+        self.r_res = float(dx if r_res is None else r_res)
+        self.cell = float(dx / alpha if cell is None else cell)
+        self.kappa_hard = int(kappa_hard)
+        self.eps = float(eps)
+        self.instances = [inst if isinstance(inst, Instance) else Instance(**inst) for inst in instances]
+        D = self.lattice.D
+        desc = _lib.SimDesc(
+            lattice=self.lattice.id, precision=_PREC[precision], dx=self.dx, r_res=self.r_res,
+            cell=self.cell, kappa_hard=self.kappa_hard, eps=self.eps, moment_capacity=int(moment_capacity),
+        )
+        arr = (_lib.InstanceDesc * len(self.instances))()
+        for i, inst in enumerate(self.instances):
+            dims = tuple(int(v) for v in inst.dims)
+            if len(dims) != D:
+                raise ValueError(f"instance {i}: dims must have {D} entries")
+            org = tuple(int(v) for v in inst.origin)[:D] + (0,) * (3 - D)
+            arr[i].dims[:] = list(dims) + [1] * (3 - D)
+            arr[i].origin[:] = list(org[:3])
+            arr[i].periodic = 1 if inst.periodic else 0
+            arr[i].tau = float(inst.tau)
+            arr[i].rho_rest = float(inst.rho_rest)
+        self.ncells = int(sum(int(np.prod(inst.dims)) for inst in self.instances))
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_create(ctypes.byref(desc), arr, len(self.instances), ctypes.byref(h)),
+                       "dbm_sim_create")
+        self._h = h
+        self.lib.dbm_sim_use_graphs(self._h, 1 if graphs else 0)
+        self.iteration = 0
+
+    # ---- lifecycle ------------------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.dbm_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.lib.dbm_sim_device_bytes(self._h))
+
+    # ---- state ----------------------------------------------------------------------------------
+    def set_state(self, inst, pos, f):
+        """Load moments: instance index (M,), world positions (M, D), distributions (M, Q)."""
+        dev = self.device
+        pos = torch.as_tensor(pos, dtype=torch.float64, device=dev).contiguous()
+        f = torch.as_tensor(f, dtype=torch.float64, device=dev).contiguous()
+        M = int(pos.shape[0])
+        if inst is None:
+            inst = torch.zeros(M, dtype=torch.int32, device=dev)
+        inst = torch.as_tensor(inst, dtype=torch.int32, device=dev).contiguous()
+        if pos.shape != (M, self.lattice.D) or f.shape != (M, self.lattice.Q) or inst.shape != (M,):
+            raise ValueError("set_state: expected inst (M,), pos (M, D), f (M, Q)")
+        with torch.cuda.device(dev):
+            _lib.check(self.lib.dbm_sim_set_state(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), M, _stream()),
+                       "dbm_sim_set_state")
+            st = self.status(clear=True)
+        if st & _lib.ST_BAD_INPUT:
+            raise _lib.DbmError("set_state: a moment lies outside its instance box")
+        self.iteration = 0
+
+    def step(self, n: int = 1):
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_step(self._h, int(n), _stream()), "dbm_sim_step")
+        self.iteration += int(n)
+
+    def step_partial(self, stage: int):
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_step_partial(self._h, int(stage), _stream()), "dbm_sim_step_partial")
+        if stage >= 6:
+            self.iteration += 1
+
+    STAGES = ("collide", "thin_refine", "sort", "weights", "gather", "emit")
+
+    def profile_step(self) -> dict:
+        """Advance one step stage by stage and return {stage: milliseconds} (CUDA events)."""
+        ms = (ctypes.c_float * 6)()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_profile_step(self._h, ms, _stream()), "dbm_sim_profile_step")
+        self.iteration += 1
+        return dict(zip(self.STAGES, [float(v) for v in ms]))
+
+    def count(self) -> int:
+        m = ctypes.c_int64()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_count(self._h, ctypes.byref(m), _stream()), "dbm_sim_count")
+        return int(m.value)
+
+    def state(self):
+        """(instance (M,) int32, positions (M, D) fp64, f (M, Q) fp64) as CUDA tensors."""
+        M = self.count()
+        dev = self.device
+        inst = torch.empty(M, dtype=torch.int32, device=dev)
+        pos = torch.empty((M, self.lattice.D), dtype=torch.float64, device=dev)
+        f = torch.empty((M, self.lattice.Q), dtype=torch.float64, device=dev)
+        if M:
+            with torch.cuda.device(dev):
+                _lib.check(self.lib.dbm_sim_get_state(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), _stream()),
+                           "dbm_sim_get_state")
+        return inst, pos, f
+
+    def state_numpy(self):
+        inst, pos, f = self.state()
+        return inst.cpu().numpy(), pos.cpu().numpy(), f.cpu().numpy()
+
+    def status(self, clear: bool = False) -> int:
+        v = ctypes.c_uint32()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_status(self._h, ctypes.byref(v), 1 if clear else 0, _stream()), "dbm_sim_status")
+        return int(v.value)
+
+    def check_status(self):
+        st = self.status(clear=False)
+        if st:
+            names = [n for n, b in (("out_of_box", 1), ("capacity", 2), ("nonfinite", 4), ("bad_input", 8)) if st & b]
+            raise _lib.DbmError(f"device status: {', '.join(names)}")
+
+    def conservation(self) -> torch.Tensor:
+        """Per-instance FP64 (mass, momentum...) of the current state, shape (n_inst, 1 + D)."""
+        out = torch.empty((len(self.instances), 1 + self.lattice.D), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_conservation(self._h, out.data_ptr(), _stream()), "dbm_sim_conservation")
+        return out
+
+    def trace(self, name: str) -> torch.Tensor:
+        """Copy an internal buffer (see include/direbm_gb300.h DBM_TRACE_*) into a uint8 tensor."""
+        what = _lib.TRACE[name]
+        need = ctypes.c_int64()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_trace(self._h, what, None, 0, ctypes.byref(need), _stream()), "dbm_sim_trace")
+            buf = torch.empty(int(need.value), dtype=torch.uint8, device=self.device)
+            _lib.check(self.lib.dbm_sim_trace(self._h, what, buf.data_ptr(), buf.numel(), ctypes.byref(need), _stream()),
+                       "dbm_sim_trace")
+        return buf

@@ -1,0 +1,156 @@
+"""GpuSimulator with the reference's interface (direbm/warp/simulator.py:25-77).
+
+``GpuSimulator(pos_m, f_m, tau, *, dx, alpha, kappa_hard, rho_rest, device)`` with ``step()``,
+``moments() -> (positions (N, 2) FP32, f (N, Q) FP32)``, ``pos_m`` / ``f_m`` (``.shape[0]`` is the
+moment count) and ``iteration``.  The engine is the fused batched step (direbm_gb300.sim) with a
+single instance.
+
+The reference domain is unbounded.  The fused step works on a dense cell grid, so an unbounded
+run is kept in a bounded box that is re-planned as the material spreads: moments move by at most
+max|c|*dx per step (every new moment is a weighted mean of component positions), so a box with a
+margin of (replan_every + 1) steps of growth cannot be left before the next planning point; at
+that point the box is re-centred on the current bounding box if needed.  A device status bit
+(out_of_box) guards the invariant and raises if it is ever broken.
+
+Extra keyword arguments (not in the reference): ``lattice``, ``r_res`` (default dx), ``cell``
+(default dx/alpha), ``precision`` ("fp32dev" or "fp64"), ``box`` ((lo, hi) world corners of a fixed
+box), ``periodic`` (with ``box``), ``graphs``.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from ..lattices import D2Q7, equilibrium, get
+from ..sim import Instance, Simulation
+from ._arrays import DeviceArray
+
+DX = 1.0
+ALPHA = 4.0
+KAPPA_HARD = 4
+
+
+class GpuSimulator:
+    def __init__(
+        self,
+        pos_m,
+        f_m,
+        tau,
+        *,
+        dx=DX,
+        alpha=ALPHA,
+        kappa_hard=KAPPA_HARD,
+        rho_rest=1.0,
+        device=None,
+        lattice=D2Q7,
+        r_res=None,
+        cell=None,
+        precision="fp32dev",
+        box=None,
+        periodic=False,
+        replan_every=8,
+        graphs=True,
+    ):
+        self.lattice = get(lattice)
+        self.tau = float(tau)
+        self.dx = float(dx)
+        self.cell = float(dx / alpha if cell is None else cell)
+        self.r_res = float(dx if r_res is None else r_res)
+        self.kappa_hard = int(kappa_hard)
+        self.rho_rest = float(rho_rest)
+        self.precision = precision
+        self.device = device
+        self.graphs = graphs
+        self.replan_every = max(1, int(replan_every))
+        self.f_rest = equilibrium(np.float64(self.rho_rest), np.zeros(self.lattice.D), self.lattice)
+        self.fixed_box = box is not None
+        self.periodic = bool(periodic) and self.fixed_box
+        self.iteration = 0
+        self._since_plan = 0
+        self._sim = None
+        self._box = None
+        pos = np.asarray(pos_m, dtype=np.float64).reshape(-1, self.lattice.D)
+        f = np.asarray(f_m, dtype=np.float64).reshape(-1, self.lattice.Q)
+        if self.fixed_box:
+            lo = np.floor(np.asarray(box[0], dtype=np.float64) / self.cell).astype(int)
+            hi = np.ceil(np.asarray(box[1], dtype=np.float64) / self.cell).astype(int)
+            self._make(lo, hi, len(pos))
+        else:
+            self._plan(pos, len(pos))
+        self._sim.set_state(None, pos, f)
+
+    # ---- box planning ---------------------------------------------------------------------------
+    def _growth(self) -> float:
+        cmax = float(np.linalg.norm(self.lattice.C, axis=1).max()) * self.dx
+        return (self.replan_every + 1) * cmax + self.r_res + 2 * self.cell
+
+    def _make(self, lo, hi, m):
+        dims = tuple(int(v) for v in (hi - lo))
+        inst = Instance(dims=dims, origin=tuple(int(v) for v in lo), periodic=self.periodic, tau=self.tau,
+                        rho_rest=self.rho_rest)
+        cap = max(int(m), int(np.prod(dims)))
+        if self._sim is not None:
+            self._sim.close()
+        self._sim = Simulation([inst], lattice=self.lattice, precision=self.precision, dx=self.dx, r_res=self.r_res,
+                               cell=self.cell, kappa_hard=self.kappa_hard, moment_capacity=cap, graphs=self.graphs,
+                               device=self.device)
+        self._box = (np.asarray(lo), np.asarray(hi))
+
+    def _plan(self, pos, m):
+        if len(pos) == 0:
+            lo = np.zeros(self.lattice.D)
+            hi = np.zeros(self.lattice.D)
+        else:
+            lo, hi = pos.min(axis=0), pos.max(axis=0)
+        g = self._growth()
+        span = max(float((hi - lo).max()), 1.0)
+        margin = g + 0.25 * span  # slack so that steady growth does not re-plan every time
+        blo = np.floor((lo - margin) / self.cell).astype(int)
+        bhi = np.ceil((hi + margin) / self.cell).astype(int)
+        self._make(blo, bhi, m)
+
+    def _maybe_replan(self):
+        if self.fixed_box or self._since_plan < self.replan_every:
+            return
+        self._since_plan = 0
+        _, pos, f = self._sim.state_numpy()
+        if len(pos) == 0:
+            return
+        g = self._growth()
+        lo_c = np.floor((pos.min(axis=0) - g) / self.cell)
+        hi_c = np.ceil((pos.max(axis=0) + g) / self.cell)
+        blo, bhi = self._box
+        if np.all(lo_c >= blo) and np.all(hi_c <= bhi):
+            return
+        self._plan(pos, len(pos))
+        self._sim.set_state(None, pos, f)
+
+    # ---- reference API -----------------------------------------------------------------------------
+    def step(self):
+        self._maybe_replan()
+        self._sim.step(1)
+        self._sim.check_status()
+        self.iteration += 1
+        self._since_plan += 1
+
+    def moments(self):
+        """(positions (N, D) FP32, f (N, Q) FP32) as numpy."""
+        _, pos, f = self._sim.state_numpy()
+        return pos.astype(np.float32), f.astype(np.float32)
+
+    @property
+    def pos_m(self):
+        _, pos, _ = self._sim.state()
+        return DeviceArray(pos.float())
+
+    @property
+    def f_m(self):
+        _, _, f = self._sim.state()
+        return DeviceArray(f.float())
+
+    @property
+    def simulation(self) -> Simulation:
+        return self._sim
+
+
+__all__ = ["GpuSimulator"]

@@ -1,0 +1,172 @@
+/*
+ * direbm_gb300.h -- C ABI of the GB300 (sm_103a) DiReBM library, libdirebm_gb300.so.
+ *
+ * Every entry point takes plain pointers and sizes, an explicit CUDA stream (cudaStream_t passed
+ * as void*; NULL means the legacy default stream) and returns an int status (DBM_OK = 0).  No
+ * exception crosses the ABI; dbm_last_error() returns a message for the last failure on the
+ * calling process.  Pointers named d_* are device pointers owned by the caller; the simulator
+ * handle owns its own state and scratch buffers (allocated at dbm_sim_create).
+ *
+ * Reference interfaces replaced (berfandil/DiReBM, Python + NVIDIA Warp):
+ *   direbm/warp/physics.py     collide, equilibrium, default_device
+ *   direbm/warp/propagation.py disperse, create_control_points, refine_control_points, resample
+ *   direbm/warp/simulator.py   GpuSimulator (__init__, step, moments)
+ *   direbm/warp/lbm.py         GpuHexLBM (__init__, set_pulse, step, macroscopic)
+ *   Warp library primitives    wp.utils.radix_sort_pairs / runlength_encode / array_scan
+ */
+#ifndef DIREBM_GB300_H
+#define DIREBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------- */
+#define DBM_OK 0
+#define DBM_ERR_INVALID 1   /* bad argument (message in dbm_last_error) */
+#define DBM_ERR_CUDA 2      /* a CUDA runtime call failed */
+#define DBM_ERR_CAPACITY 3  /* a capacity would be exceeded */
+#define DBM_ERR_STATE 4     /* device status word reports a fault (see dbm_sim_status) */
+
+/* ---- enums -------------------------------------------------------------------------------- */
+#define DBM_D2Q7 0   /* reference lattice: direbm/constants.py:15-36 */
+#define DBM_D2Q9 1   /* standard square set (new; the reference has none) */
+#define DBM_D3Q13 2  /* reference icosahedral set: direbm/lattices.py:44-61 */
+#define DBM_D3Q19 3  /* standard cubic set (new) */
+
+#define DBM_FP64 0      /* f and offsets in FP64 */
+#define DBM_FP32DEV 1   /* f stored as FP32 rho + FP32 deviation from rho*W; FP32 offsets */
+
+/* ---- library ------------------------------------------------------------------------------ */
+const char* dbm_last_error(void);
+int dbm_version(void);
+/* Number of kernels this library has launched in this process (graph replays count their
+ * kernel nodes). */
+unsigned long long dbm_launch_count(void);
+/* Replaces direbm/warp/physics.py:21-22 default_device(): returns the CUDA device count. */
+int dbm_device_count(int* count);
+
+/* ---- BGK physics on explicit arrays --------------------------------------------------------
+ * Replaces direbm/warp/physics.py:78-97 collide(f_np, tau) / equilibrium(rho_np, u_np), whose
+ * Warp kernels are _collide / _equilibrium (physics.py:45-75).  Layout is the reference's: f is
+ * row-major (n, Q), u is (n, D).  In place for collide. */
+int dbm_collide_f32(float* d_f, int64_t n, int lattice, float tau, void* stream);
+int dbm_collide_f64(double* d_f, int64_t n, int lattice, double tau, void* stream);
+int dbm_equilibrium_f32(const float* d_rho, const float* d_u, int64_t n, int lattice, float* d_out, void* stream);
+int dbm_equilibrium_f64(const double* d_rho, const double* d_u, int64_t n, int lattice, double* d_out, void* stream);
+
+/* ---- device radix sort ------------------------------------------------------------------------
+ * Replaces wp.utils.radix_sort_pairs (called at direbm/warp/propagation.py:138): stable
+ * ascending LSD sort of (key, value) pairs over the low `key_bits` bits.  Sorts d_keys/d_vals in
+ * place, using d_tmp (size from dbm_radix_sort_tmp_bytes) as scratch. */
+int64_t dbm_radix_sort_tmp_bytes(int64_t n, int key_bytes);
+int dbm_radix_sort_pairs_u32(uint32_t* d_keys, uint32_t* d_vals, int64_t n, int key_bits, void* d_tmp, void* stream);
+int dbm_radix_sort_pairs_u64(uint64_t* d_keys, uint32_t* d_vals, int64_t n, int key_bits, void* d_tmp, void* stream);
+
+/* ---- stage functions on explicit component arrays (FP32, 2D D2Q7 layout of the reference) ---
+ * disperse: direbm/warp/propagation.py:21-36,115-127.  pos_m (M,2), f_m (M,Q) -> pos_c (Q*M,2),
+ * val_c (Q*M), dir_c (Q*M), component index Q*i + k. */
+int dbm_disperse_f32(const float* d_pos_m, const float* d_f_m, int64_t m, int lattice, float dx,
+                     float* d_pos_c, float* d_val_c, int32_t* d_dir_c, void* stream);
+/* create_control_points: direbm/warp/propagation.py:39-68,130-153.  Cell key (floor(x/cs),
+ * floor(y/cs)), stable radix sort, run-length encode, exclusive scan, sequential FP32 centroid
+ * per run in sorted order.  d_cp_pos needs room for nc points; *p_out receives P (this call
+ * synchronises the stream, as the reference's run_count.numpy() did). */
+int dbm_create_control_points_f32(const float* d_pos_c, int64_t nc, float cs, float* d_cp_pos,
+                                  int64_t* p_out, void* stream);
+/* refine_control_points: direbm/warp/propagation.py:77-112,249-275. */
+int dbm_refine_control_points_f32(const float* d_cp_pos, int64_t p, const float* d_pos_c, const float* d_val_c,
+                                  const int32_t* d_dir_c, int64_t nc, float dx, int kappa_hard,
+                                  float* d_new_pos, void* stream);
+/* resample: direbm/warp/propagation.py:156-246 (scatter + gap fill + emit), as a deterministic
+ * two-pass gather instead of float atomics.  out_f is (P, Q). */
+int dbm_resample_f32(const float* d_pos_c, const float* d_val_c, const int32_t* d_dir_c, int64_t nc,
+                     const float* d_cp_pos, int64_t p, float dx, const float* d_f_rest, int lattice,
+                     float eps, float* d_out_pos, float* d_out_f, void* stream);
+
+/* ---- hexagonal D2Q7 lattice Boltzmann ------------------------------------------------------
+ * Replaces direbm/warp/lbm.py:24-105 (_lbm_collide + _lbm_stream, GpuHexLBM.step) with one
+ * fused push collide-stream kernel over structure-of-arrays storage, batched over independent
+ * runs.  Storage of run r, direction k, node (j, i) is at index ((r*7 + k)*nj + j)*ni + i.
+ *   FP64:    d_src/d_dst are double, holding f.
+ *   FP32DEV: d_src/d_dst are float, holding f - W_k*rho0 (deviation from the rest state).
+ * d_tau has one entry per run (double). */
+int dbm_lbm_step(int precision, const void* d_src, void* d_dst, int32_t ni, int32_t nj, int32_t runs,
+                 const double* d_tau, double rho0, int32_t steps, void* d_tmp, void* stream);
+
+/* ---- the fused DiReBM simulator -----------------------------------------------------------
+ * Replaces direbm/warp/simulator.py:25-77 (GpuSimulator) and the pipeline it drives.  A handle
+ * holds a batch of independent instances, each a box of `dims` cells of size `cell` (periodic or
+ * not); moments live as (cell, offset) sorted by cell; each step runs collide, thinning + refine,
+ * a radix sort of the control points, the two-pass resampling gather and the gap fill, with no
+ * host synchronisation. */
+typedef struct dbm_sim dbm_sim;
+
+typedef struct {
+  int32_t lattice;     /* DBM_D2Q7 ... */
+  int32_t precision;   /* DBM_FP64 / DBM_FP32DEV */
+  double dx;           /* dispersion distance (reference: dx) */
+  double r_res;        /* resampling / refine radius (reference: dx) */
+  double cell;         /* thinning cell (reference: dx / alpha) */
+  int32_t kappa_hard;  /* reference: kappa_hard (constants.py:43) */
+  double eps;          /* gap-fill emptiness threshold (reference GPU path: 1e-6) */
+  int64_t moment_capacity; /* >= initial moment count; raised to the cell count if smaller */
+} dbm_sim_desc;
+
+typedef struct {
+  int32_t dims[3];     /* cells per axis (unused axes = 1) */
+  int32_t origin[3];   /* world cell index of local cell 0 */
+  int32_t periodic;    /* 1 = periodic box, 0 = bounded box (leaving it sets a status bit) */
+  double tau;          /* BGK relaxation time of this instance */
+  double rho_rest;     /* gap-fill rest density (reference: rho_rest) */
+} dbm_instance_desc;
+
+int dbm_sim_create(const dbm_sim_desc* desc, const dbm_instance_desc* inst, int32_t n_inst, dbm_sim** out);
+int dbm_sim_destroy(dbm_sim* sim);
+/* Load moments: d_inst (m) instance of each moment, d_pos (m, D) world positions, d_f (m, Q). */
+int dbm_sim_set_state(dbm_sim* sim, const int32_t* d_inst, const double* d_pos, const double* d_f, int64_t m,
+                      void* stream);
+/* Advance `steps` steps (replays a captured CUDA graph when graphs are enabled). */
+int dbm_sim_step(dbm_sim* sim, int32_t steps, void* stream);
+/* Synchronises `stream` and returns the current moment count. */
+int dbm_sim_count(dbm_sim* sim, int64_t* m, void* stream);
+/* Export the state (outputs sized by dbm_sim_count), world positions and f in FP64. */
+int dbm_sim_get_state(dbm_sim* sim, int32_t* d_inst, double* d_pos, double* d_f, void* stream);
+/* Synchronises and returns the device status word (ST_* bits); clears it when clear != 0. */
+int dbm_sim_status(dbm_sim* sim, uint32_t* flags, int32_t clear, void* stream);
+/* Per-instance FP64 totals: mass, then momentum per axis -> d_out (n_inst, 1 + D). */
+int dbm_sim_conservation(dbm_sim* sim, double* d_out, void* stream);
+/* Graph capture on/off for dbm_sim_step (default on). */
+int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
+/* Run one step but stop after `stage` (1 collide, 2 thin+refine, 3 sort, 4 weights, 5 gather,
+ * 6 emit) so intermediates can be exported with dbm_sim_trace. */
+int dbm_sim_step_partial(dbm_sim* sim, int32_t stage, void* stream);
+/* Run one full step stage by stage (no graph) with CUDA events recorded on the stream the kernels
+ * run on; stage_ms[6] receives the durations of: collide, thin+refine, compaction+sort+finalize,
+ * weights, gather, emit.  Synchronises. */
+int dbm_sim_profile_step(dbm_sim* sim, float* stage_ms, void* stream);
+/* Copy an internal buffer (DBM_TRACE_*) into d_dst (bytes given); *needed returns its size. */
+int dbm_sim_trace(dbm_sim* sim, int32_t what, void* d_dst, int64_t bytes, int64_t* needed, void* stream);
+/* Device memory held by the handle. */
+int64_t dbm_sim_device_bytes(dbm_sim* sim);
+
+#define DBM_TRACE_OCC 1        /* u32[ncells]   occupied flag per cell after thinning */
+#define DBM_TRACE_THIN_CNT 2   /* u32[ncells]   components per occupied cell */
+#define DBM_TRACE_CENTROID 3   /* real[D][ncells] centroid offset (rel. to the cell) */
+#define DBM_TRACE_MASK 4       /* u32[ncells]   refine direction mask */
+#define DBM_TRACE_FINAL_CELL 5 /* u32[ncells]   refined CP cell */
+#define DBM_TRACE_FINAL_OFF 6  /* real[D][ncells] refined CP offset */
+#define DBM_TRACE_SORTED 7     /* u32[2][P]     sorted (cell, origin cell) pairs */
+#define DBM_TRACE_SW 8         /* real[Q][Mcap] weight sums per component (FP32DEV: float) */
+#define DBM_TRACE_CPF 9        /* FP64: double[Q][cap]; FP32DEV: float[2][Q][cap] (hi, lo) */
+#define DBM_TRACE_EMPTY 10     /* u32[cap]      empty-direction mask per CP */
+#define DBM_TRACE_FSTAR 11     /* collided f of the input moments, layout of the state */
+#define DBM_TRACE_COUNTS 12    /* u32[2]: M (moments in), P (control points) */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIREBM_GB300_H */

@@ -1,0 +1,385 @@
+"""The DiReBM step on a dense cell grid (test oracle for the fused CUDA pipeline).
+
+This restates the reference GPU step (direbm/warp/simulator.py:50-73 -> collide, disperse,
+create_control_points, refine_control_points, resample in direbm/warp/propagation.py) in the data
+layout the CUDA pipeline uses, with the generalisations the benchmark configurations need:
+any velocity set, a resampling radius ``r_res`` separate from ``dx``, a thinning cell ``cell``
+separate from dx/alpha, periodic boxes, and a batch of independent instances.
+
+Representation (shared with the CUDA pipeline; everything in units of the thinning cell):
+  * a moment sits at integer cell coordinates S (inside its instance's box) plus an offset
+    ``off`` in [0, 1) per axis; world position = (origin + S + off) * cell;
+  * moments are kept sorted by global cell index (instance base + row-major cell index), stable;
+  * direction k disperses by cd_k = c_k * dx / cell; the component of moment m lands in cell
+    S + floor(off + cd_k)  (propagation.py:39-51 with the division folded into the cell units).
+
+Step, in order (each line cites the reference function it follows):
+  1. collide every moment, per-instance tau, no vacuum guard       (warp/physics.py:45-62)
+  2. thin: one control point (CP) per occupied cell, at the centroid of the components landing
+     there                                                         (propagation.py:130-153)
+  3. refine: kappa = number of distinct directions among components within r (inclusive); keep the
+     CP if kappa <= kappa_hard, else move it to sum(e^f q)/sum(e^f)  (propagation.py:77-112)
+  4. stable-sort the CPs by the cell of their refined position (the next step's moment order)
+  5. per component: sw = sum over CPs within r of (r - d); dropped if sw <= 0 (propagation.py:156-178)
+  6. per CP and direction: f = sum over components within r of (r - d)/sw * f   (propagation.py:179-186)
+  7. gap fill: directions with f < eps get (r / sum_{CPs within r, also empty}(r - d)) * f_rest;
+     emptiness is judged on the pre-fill values; emit one moment per CP      (propagation.py:189-218)
+
+The radius test and every floor use one canonical operation order (no fused multiply-add):
+    t = off + cd ;  q = float(S - F) + t ;  e = q - p ;  d = sqrt(sum e*e) ;  inside = d <= R
+evaluated in the working precision (float64, or float32 for the FP32 store), so integer
+decisions are bit-identical to the CUDA kernels.  Sums are in float64 here; the CUDA FP64 path
+agrees to ~1e-15 relative, the FP32 path to its stated tolerance.
+
+Parity pinning: stage 2 reduces to the reference tests' own numpy restatement of cell thinning
+(tests/test_warp_propagation.py:27-36) when all components of an unbounded domain are given, and
+stage 3 reproduces the ring fixtures of tests/test_warp_propagation.py:79-112; both are checked in
+tests/test_oracle_golden.py.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .lattices import Lattice
+from .physics import collide_unguarded
+
+
+@dataclass
+class Instance:
+    dims: tuple  # cells per axis
+    origin: tuple = None  # world cell of local cell 0 (integer per axis)
+    periodic: bool = True
+    tau: float = 0.6
+    rho_rest: float = 1.0
+
+
+@dataclass
+class GridSpec:
+    lattice: Lattice
+    dx: float
+    r_res: float
+    cell: float
+    kappa_hard: int
+    instances: list
+    eps: float = 1e-6
+    dtype: type = np.float64  # working precision of the decision arithmetic
+    base: np.ndarray = field(init=False)
+    ncells: int = field(init=False)
+
+    def __post_init__(self):
+        D = self.lattice.D
+        sizes = [int(np.prod(inst.dims)) for inst in self.instances]
+        for inst in self.instances:
+            assert len(inst.dims) == D
+            if inst.origin is None:
+                inst.origin = (0,) * D
+        self.base = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        self.ncells = int(self.base[-1])
+
+    @property
+    def D(self):
+        return self.lattice.D
+
+    @property
+    def Q(self):
+        return self.lattice.Q
+
+    @property
+    def cd(self):
+        return (self.lattice.C * self.dx / self.cell).astype(self.dtype)
+
+    @property
+    def R(self):
+        return self.dtype(self.r_res / self.cell)
+
+    def dims_arr(self):
+        return np.array([inst.dims for inst in self.instances], dtype=np.int64)
+
+    def periodic_arr(self):
+        return np.array([inst.periodic for inst in self.instances], dtype=bool)
+
+    def tau_arr(self):
+        return np.array([inst.tau for inst in self.instances], dtype=np.float64)
+
+    def f_rest(self):
+        W = self.lattice.W
+        return np.array([inst.rho_rest * W for inst in self.instances])
+
+
+# ---- cell indexing ----------------------------------------------------------------------------
+
+def decode(spec: GridSpec, g):
+    g = np.asarray(g, dtype=np.int64)
+    b = np.searchsorted(spec.base, g, side="right") - 1
+    local = g - spec.base[b]
+    dims = spec.dims_arr()[b]
+    coords = np.zeros((len(g), spec.D), dtype=np.int64)
+    rem = local
+    for a in range(spec.D):
+        coords[:, a] = rem % dims[:, a]
+        rem = rem // dims[:, a]
+    return b, coords
+
+
+def encode(spec: GridSpec, b, coords):
+    """Global cell of (unwrapped) coords; -1 where a non-periodic instance has no such cell."""
+    b = np.asarray(b, dtype=np.int64)
+    coords = np.asarray(coords, dtype=np.int64)
+    dims = spec.dims_arr()[b]
+    per = spec.periodic_arr()[b]
+    wrapped = np.where(per[:, None], np.mod(coords, dims), coords)
+    inside = np.all((wrapped >= 0) & (wrapped < dims), axis=1)
+    lin = np.zeros(len(b), dtype=np.int64)
+    stride = np.ones(len(b), dtype=np.int64)
+    for a in range(spec.D):
+        lin += wrapped[:, a] * stride
+        stride *= dims[:, a]
+    return np.where(inside, spec.base[b] + lin, -1)
+
+
+@dataclass
+class GridState:
+    cell: np.ndarray  # (M,) int64 global cell, sorted
+    off: np.ndarray  # (M, D) offsets in [0,1), working dtype
+    f: np.ndarray  # (M, Q) float64
+
+
+def from_world(spec: GridSpec, inst_idx, pos, f):
+    """World positions -> sorted grid state (s = x / cell in float64, floor, offset = s - floor,
+    offset rounded to the working precision and clamped below 1)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    inst_idx = np.asarray(inst_idx, dtype=np.int64)
+    s = pos / np.float64(spec.cell)
+    fl = np.floor(s)
+    off = (s - fl).astype(spec.dtype)
+    one_below = np.nextafter(spec.dtype(1.0), spec.dtype(0.0))
+    off = np.minimum(off, one_below)
+    origin = np.array([spec.instances[b].origin for b in inst_idx], dtype=np.int64).reshape(len(inst_idx), spec.D)
+    coords = fl.astype(np.int64) - origin
+    g = encode(spec, inst_idx, coords)
+    if np.any(g < 0):
+        raise ValueError("moment outside its instance box")
+    order = np.argsort(g, kind="stable")
+    return GridState(cell=g[order], off=off[order], f=np.asarray(f, dtype=np.float64)[order])
+
+
+def to_world(spec: GridSpec, st: GridState):
+    b, coords = decode(spec, st.cell)
+    origin = np.array([spec.instances[i].origin for i in b], dtype=np.int64).reshape(len(b), spec.D)
+    x = ((origin + coords).astype(np.float64) + st.off.astype(np.float64)) * np.float64(spec.cell)
+    return b, x, st.f
+
+
+# ---- canonical distance ------------------------------------------------------------------------
+
+def disp(spec: GridSpec, dS, t, p):
+    """e = (float(dS) + t) - p in the working precision."""
+    dt = spec.dtype
+    return ((dS.astype(dt) + t.astype(dt)).astype(dt) - p.astype(dt)).astype(dt)
+
+
+def norm(spec: GridSpec, e):
+    dt = spec.dtype
+    s = (e[:, 0] * e[:, 0]).astype(dt)
+    for a in range(1, e.shape[1]):
+        s = (s + (e[:, a] * e[:, a]).astype(dt)).astype(dt)
+    return np.sqrt(s).astype(dt)
+
+
+def _offsets(D, lo, hi):
+    rng = np.arange(lo, hi + 1)
+    grids = np.meshgrid(*([rng] * D), indexing="ij")
+    return np.stack([gr.ravel() for gr in grids], axis=1)
+
+
+def components(spec: GridSpec, st: GridState):
+    """All (m, k) components: moment index, direction, source coords, t = off + cd (working dtype)."""
+    M, Q = len(st.cell), spec.Q
+    b, S = decode(spec, st.cell)
+    m = np.repeat(np.arange(M), Q)
+    k = np.tile(np.arange(Q), M)
+    t = (st.off[m].astype(spec.dtype) + spec.cd[k]).astype(spec.dtype)
+    return m, k, b[m], S[m], t
+
+
+# ---- the stages --------------------------------------------------------------------------------
+
+def collide_state(spec: GridSpec, st: GridState):
+    b, _ = decode(spec, st.cell)
+    return collide_unguarded(st.f, spec.tau_arr()[b], spec.lattice)
+
+
+def thin(spec: GridSpec, st: GridState):
+    """Stage 2.  Returns (occupied global cells sorted, count per CP, centroid rel (P,D),
+    component landing cell per (m,k) (or -1 outside a non-periodic box))."""
+    m, k, b, S, t = components(spec, st)
+    fl = np.floor(t).astype(np.int64)
+    C = encode(spec, b, S + fl)
+    rel = ((-fl).astype(spec.dtype) + t).astype(spec.dtype)
+    ok = C >= 0
+    cells, inv = np.unique(C[ok], return_inverse=True)
+    cnt = np.bincount(inv, minlength=len(cells))
+    sums = np.zeros((len(cells), spec.D))
+    np.add.at(sums, inv, rel[ok].astype(np.float64))
+    cen = (sums / cnt[:, None]).astype(spec.dtype)
+    return cells, cnt, cen, C
+
+
+def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
+    """(component, CP) pairs within R.  CPs are (global cell, offset), any number per cell.
+    Returns comp index into the (m,k) list, CP index, d, and q = float(S - G) + t (rel to CP cell)."""
+    if comps is None:
+        comps = components(spec, st)
+    m, k, b, S, t = comps
+    fl = np.floor(t).astype(np.int64)
+    order = np.argsort(cp_cell, kind="stable")
+    cs = cp_cell[order]
+    Rc = int(np.ceil(float(spec.R)))
+    ci_all, pj_all, d_all, q_all = [], [], [], []
+    for o in _offsets(spec.D, -Rc - 1, Rc + 1):
+        G = encode(spec, b, S + fl + o)
+        lo = np.searchsorted(cs, G, side="left")
+        hi = np.searchsorted(cs, G, side="right")
+        cnt = np.where(G >= 0, hi - lo, 0)
+        if cnt.sum() == 0:
+            continue
+        ci = np.repeat(np.arange(len(m)), cnt)
+        within = np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+        pj = order[np.repeat(lo, cnt) + within]
+        dS = -(fl[ci] + o)
+        q = (dS.astype(spec.dtype) + t[ci]).astype(spec.dtype)
+        e = (q - cp_off[pj].astype(spec.dtype)).astype(spec.dtype)
+        d = norm(spec, e)
+        keep = d <= spec.R
+        ci_all.append(ci[keep])
+        pj_all.append(pj[keep])
+        d_all.append(d[keep])
+        q_all.append(q[keep])
+    if not ci_all:
+        z = np.zeros(0, np.int64)
+        return z, z, np.zeros(0, spec.dtype), np.zeros((0, spec.D), spec.dtype)
+    return np.concatenate(ci_all), np.concatenate(pj_all), np.concatenate(d_all), np.concatenate(q_all)
+
+
+def refine(spec: GridSpec, st: GridState, fstar, cells, cen):
+    """Stage 3.  Returns (mask, kappa, final global cell, final offset) per CP (thinning order)."""
+    comps = components(spec, st)
+    m, k, b, S, t = comps
+    ci, pj, d, q = _pairs_comp_cp(spec, st, cells, cen, comps)
+    P = len(cells)
+    mask = np.zeros(P, dtype=np.int64)
+    np.bitwise_or.at(mask, pj, np.left_shift(1, k[ci]))
+    kappa = np.array([bin(int(x)).count("1") for x in mask], dtype=np.int64)
+    w = np.exp(fstar[m[ci], k[ci]])
+    sw = np.zeros(P)
+    sx = np.zeros((P, spec.D))
+    np.add.at(sw, pj, w)
+    np.add.at(sx, pj, w[:, None] * q.astype(np.float64))
+    move = kappa > spec.kappa_hard
+    npos = cen.astype(spec.dtype).copy()
+    npos[move] = (sx[move] / sw[move, None]).astype(spec.dtype)
+    shift = np.floor(npos).astype(np.int64)
+    off = (npos - shift.astype(spec.dtype)).astype(spec.dtype)
+    over = off >= spec.dtype(1.0)
+    off[over] = 0
+    shift[over] += 1
+    bcp, F = decode(spec, cells)
+    G = encode(spec, bcp, F + shift)
+    return mask, kappa, G, off
+
+
+def sort_cps(G):
+    """Stage 4: stable ascending sort by final cell (ties keep thinning order)."""
+    return np.argsort(G, kind="stable")
+
+
+def weights(spec: GridSpec, st: GridState, cp_cell, cp_off, comps=None):
+    """Stage 5.  sw per component (m,k) plus the pair list (ci, pj, d)."""
+    if comps is None:
+        comps = components(spec, st)
+    m = comps[0]
+    ci, pj, d, _ = _pairs_comp_cp(spec, st, cp_cell, cp_off, comps)
+    wv = (spec.R - d).astype(np.float64)
+    sw = np.zeros(len(m))
+    np.add.at(sw, ci, wv)
+    return sw, ci, pj, wv
+
+
+def gather(spec: GridSpec, st: GridState, fstar, cp_cell, cp_off):
+    """Stages 5+6.  Returns cp_f (P,Q) before gap fill and sw per component."""
+    comps = components(spec, st)
+    m, k = comps[0], comps[1]
+    sw, ci, pj, wv = weights(spec, st, cp_cell, cp_off, comps)
+    live = sw[ci] > 0.0
+    P = len(cp_cell)
+    cp_f = np.zeros((P, spec.Q))
+    np.add.at(cp_f, (pj[live], k[ci[live]]), (wv[live] / sw[ci[live]]) * fstar[m[ci[live]], k[ci[live]]])
+    return cp_f, sw.reshape(-1, spec.Q)
+
+
+def gapfill(spec: GridSpec, cp_cell, cp_off, cp_f):
+    """Stage 7 (CP-CP distance from each CP's own perspective)."""
+    P = len(cp_cell)
+    empty = cp_f < spec.eps
+    b, F = decode(spec, cp_cell)
+    order = np.argsort(cp_cell, kind="stable")
+    cs = cp_cell[order]
+    Rc = int(np.ceil(float(spec.R)))
+    a_all, c_all, w_all = [], [], []
+    for o in _offsets(spec.D, -Rc - 1, Rc + 1):
+        G = encode(spec, b, F + o)
+        lo = np.searchsorted(cs, G, side="left")
+        hi = np.searchsorted(cs, G, side="right")
+        cnt = np.where(G >= 0, hi - lo, 0)
+        if cnt.sum() == 0:
+            continue
+        ai = np.repeat(np.arange(P), cnt)
+        within = np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+        cj = order[np.repeat(lo, cnt) + within]
+        e = disp(spec, np.broadcast_to(o, (len(ai), spec.D)), cp_off[cj], cp_off[ai])
+        d = norm(spec, e)
+        keep = d <= spec.R
+        a_all.append(ai[keep])
+        c_all.append(cj[keep])
+        w_all.append((spec.R - d[keep]).astype(np.float64))
+    ai = np.concatenate(a_all)
+    cj = np.concatenate(c_all)
+    ww = np.concatenate(w_all)
+    out = cp_f.copy()
+    f_rest = spec.f_rest()[b]
+    for i in range(spec.Q):
+        sel = empty[cj, i]
+        s = np.zeros(P)
+        np.add.at(s, ai[sel], ww[sel])
+        fill = empty[:, i] & (s > 0.0)
+        out[fill, i] = (float(spec.R) / s[fill]) * f_rest[fill, i]
+    return out, empty
+
+
+def step(spec: GridSpec, st: GridState, trace: dict | None = None) -> GridState:
+    fstar = collide_state(spec, st)
+    cells, cnt, cen, comp_cell = thin(spec, st)
+    mask, kappa, G, off = refine(spec, st, fstar, cells, cen)
+    keep = G >= 0
+    order = sort_cps(np.where(keep, G, np.iinfo(np.int64).max))
+    order = order[keep[order]]
+    cp_cell = G[order]
+    cp_off = off[order]
+    cp_f, sw = gather(spec, st, fstar, cp_cell, cp_off)
+    f_new, empty = gapfill(spec, cp_cell, cp_off, cp_f)
+    if trace is not None:
+        trace.update(
+            fstar=fstar, thin_cells=cells, thin_count=cnt, centroid=cen, comp_cell=comp_cell,
+            mask=mask, kappa=kappa, final_cell=G, final_off=off, order=order, sw=sw,
+            cp_f=cp_f, empty=empty,
+        )
+    return GridState(cell=cp_cell, off=cp_off, f=f_new)
+
+
+def run(spec: GridSpec, st: GridState, steps: int) -> GridState:
+    for _ in range(steps):
+        st = step(spec, st)
+    return st

@@ -1,0 +1,146 @@
+"""Generate golden vectors from the reference's own CPU code (berfandil/DiReBM).
+
+Run in a container where the reference checkout is available:
+
+    python tests/golden/make_golden.py /path/to/DiReBM
+
+It imports the reference's numpy package (``direbm``, ``direbm.lbm``, ``direbm.fields``,
+``direbm.reference``) -- which needs no Warp -- and, for the two numpy helpers that live in the
+reference's Warp test module (``_cell_thin_ref`` and ``_ring`` of tests/test_warp_propagation.py),
+extracts just those function definitions with ``ast`` (the module itself imports Warp).  The
+outputs are small ``.npz`` files next to this script; the tests load only those files, so the
+reference checkout is not needed where the tests run.
+"""
+
+from __future__ import annotations
+
+import ast
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+
+
+def _load_test_helpers(ref_root: Path) -> dict:
+    src = (ref_root / "tests" / "test_warp_propagation.py").read_text()
+    tree = ast.parse(src)
+    keep = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in ("_cell_thin_ref", "_ring")]
+    mod = ast.Module(body=keep, type_ignores=[])
+    ns = {"np": np}
+    exec(compile(mod, "reference_test_helpers", "exec"), ns)
+    return ns
+
+
+def main(ref_root: str) -> None:
+    ref_root = Path(ref_root).resolve()
+    sys.path.insert(0, str(ref_root))
+    import direbm
+    from direbm import bin_fields, collide, equilibrium
+    from direbm.lattices import D2Q7, D3Q13, Lattice
+    from direbm.lbm import HexLBM
+    from direbm.reference import Moment, Simulator
+
+    helpers = _load_test_helpers(ref_root)
+
+    # -- physics (tests/test_warp_physics.py:13-37 seeds; plus D3Q13 and a harness-built D2Q9) ----
+    d2q9 = Lattice(
+        C=np.array([[0, 0], [1, 0], [0, 1], [-1, 0], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1]], float),
+        W=np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4),
+        cs2=1.0 / 3.0,
+        name="D2Q9",
+    )
+    out = {}
+    for name, lat in (("D2Q7", D2Q7), ("D2Q9", d2q9), ("D3Q13", D3Q13)):
+        rng = np.random.default_rng(0)
+        rho = rng.uniform(0.5, 2.0, size=128)
+        u = rng.uniform(-0.1, 0.1, size=(128, lat.D))
+        out[f"{name}_eq_rho"] = rho
+        out[f"{name}_eq_u"] = u
+        out[f"{name}_eq"] = equilibrium(rho, u, lat)
+        rng = np.random.default_rng(1)
+        f = rng.uniform(0.01, 1.0, size=(256, lat.Q))
+        out[f"{name}_col_f"] = f
+        out[f"{name}_col"] = collide(f, 0.6, lat)
+    np.savez_compressed(HERE / "physics.npz", **out)
+
+    # -- hexagonal LBM (tests/test_warp_lbm.py:9-39, tests/test_lbm.py) ------------------------------
+    out = {}
+    lbm = HexLBM(21, 21, tau=0.6)
+    lbm.set_pulse(1.5)
+    out["pulse21_f0"] = lbm.f.copy()
+    for _ in range(10):
+        lbm.step()
+    out["pulse21_f10"] = lbm.f.copy()
+    lbm = HexLBM(25, 25, tau=0.7)
+    lbm.set_pulse(2.0)
+    out["pulse25_f0"] = lbm.f.copy()
+    for _ in range(15):
+        lbm.step()
+    out["pulse25_f15"] = lbm.f.copy()
+    np.savez_compressed(HERE / "lbm.npz", **out)
+
+    # -- cell thinning KAT: the reference test's own numpy restatement (_cell_thin_ref) on the
+    #    FP32 component clouds of its seeds (tests/test_warp_propagation.py:43-76) ---------------
+    out = {}
+    C32 = direbm.C.astype(np.float32)
+    for seed, (n, lo, hi) in {0: (20, -5.0, 5.0), 1: (50, -5.0, 5.0), 2: (40, -3.0, 3.0)}.items():
+        rng = np.random.default_rng(seed)
+        pos_m = rng.uniform(lo, hi, size=(n, 2))
+        f_m = rng.uniform(0.01, 1.0, size=(n, 7))
+        pc = (pos_m.astype(np.float32)[:, None, :] + C32[None, :, :] * np.float32(1.0)).reshape(-1, 2)
+        cp = helpers["_cell_thin_ref"](pc, 1.0 / 4.0)
+        out[f"s{seed}_pos_m"] = pos_m
+        out[f"s{seed}_f_m"] = f_m
+        out[f"s{seed}_pos_c"] = pc
+        out[f"s{seed}_cp"] = cp
+    # ring fixtures (tests/test_warp_propagation.py:79-112)
+    ring = helpers["_ring"]
+    posA, dirA, valA = ring((0.0, 0.0), 0.2, [0, 1, 2, 3, 4, 5, 6], [0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7])
+    posB, dirB, valB = ring((10.0, 0.0), 0.2, [0, 1, 2], [0.1, 0.2, 0.3])
+    w = np.exp(valA)
+    out["ringAB_pos"] = np.vstack([posA, posB])
+    out["ringAB_dir"] = np.concatenate([dirA, dirB])
+    out["ringAB_val"] = np.concatenate([valA, valB])
+    out["ringAB_cp"] = np.array([[0.0, 0.0], [10.0, 0.0]])
+    out["ringAB_expected"] = np.array([(w[:, None] * posA).sum(0) / w.sum(), [10.0, 0.0]])
+    pos4, dir4, val4 = ring((0.0, 0.0), 0.2, [0, 1, 2, 3], [0.1, 0.3, 0.5, 0.7])
+    pos5, dir5, val5 = ring((20.0, 0.0), 0.2, [0, 1, 2, 3, 4], [0.1, 0.3, 0.5, 0.7, 0.9])
+    out["ring45_pos"] = np.vstack([pos4, pos5])
+    out["ring45_dir"] = np.concatenate([dir4, dir5])
+    out["ring45_val"] = np.concatenate([val4, val5])
+    out["ring45_cp"] = np.array([[0.0, 0.0], [20.0, 0.0]])
+    np.savez_compressed(HERE / "propagation.npz", **out)
+
+    # -- macroscopic binning (tests/test_fields.py) ---------------------------------------------
+    out = {}
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-3.0, 4.0, size=(200, 2))
+    f = rng.uniform(0.01, 0.5, size=(200, 7))
+    rho, u, _ = bin_fields(x, f, -3, 4, h=1.0)
+    out.update(x=x, f=f, rho=rho, u=u)
+    np.savez_compressed(HERE / "fields.npz", **out)
+
+    # -- reference CPU simulator: the 13x13 rest block + central pulse of
+    #    tests/test_warp_simulator.py:10-63, 3 steps, binned density --------------------------------
+    f_rest = equilibrium(np.float64(1.0), np.zeros(2))
+    pos, fs = [], []
+    for i in range(-6, 7):
+        for j in range(-6, 7):
+            pos.append([float(i), float(j)])
+            fs.append(equilibrium(np.float64(1.5), np.zeros(2)) if (i == 0 and j == 0) else f_rest.copy())
+    pos = np.array(pos)
+    fs = np.stack(fs)
+    sim = Simulator([Moment(f=fs[k].copy(), x=pos[k].copy()) for k in range(len(pos))], tau=0.6, rho_rest=1.0)
+    for _ in range(3):
+        sim.step()
+    xv = np.array([m.x for m in sim.moments])
+    fv = np.stack([m.f for m in sim.moments])
+    rv, _, _ = bin_fields(xv, fv, -3, 3, h=1.0)
+    np.savez_compressed(HERE / "simulator.npz", pos0=pos, f0=fs, x3=xv, f3=fv, rho3=rv)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,152 @@
+"""GPU parity for the BGK kernels, the radix sort and the hexagonal LBM kernel."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import lbm as olbm
+from oracle import physics
+from oracle.lattices import BY_NAME
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from direbm_gb300 import _lib
+
+    return _lib.load(), _lib
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.mark.parametrize("name", ["D2Q7", "D2Q9", "D3Q13", "D3Q19"])
+def test_collide_equilibrium_f64_exact_and_f32_reference_tolerance(golden, name):
+    lib, L = _lib()
+    lat = BY_NAME[name]
+    lid = {"D2Q7": 0, "D2Q9": 1, "D3Q13": 2, "D3Q19": 3}[name]
+    rng = np.random.default_rng(1)
+    f = rng.uniform(0.01, 1.0, size=(256, lat.Q))
+    ref = physics.collide_unguarded(f, 0.6, lat)
+    t = torch.tensor(f, dtype=torch.float64, device="cuda")
+    L.check(lib.dbm_collide_f64(t.data_ptr(), 256, lid, ctypes.c_double(0.6), _stream()))
+    np.testing.assert_allclose(t.cpu().numpy(), ref, rtol=1e-13, atol=1e-15)
+    t32 = torch.tensor(f, dtype=torch.float32, device="cuda")
+    L.check(lib.dbm_collide_f32(t32.data_ptr(), 256, lid, ctypes.c_float(0.6), _stream()))
+    np.testing.assert_allclose(t32.cpu().numpy(), ref, rtol=1e-4, atol=1e-5)  # reference tolerance
+    rng = np.random.default_rng(0)
+    rho = rng.uniform(0.5, 2.0, size=128)
+    u = rng.uniform(-0.1, 0.1, size=(128, lat.D))
+    ref = physics.equilibrium(rho, u, lat)
+    r = torch.tensor(rho, dtype=torch.float64, device="cuda")
+    uu = torch.tensor(u, dtype=torch.float64, device="cuda")
+    out = torch.empty((128, lat.Q), dtype=torch.float64, device="cuda")
+    L.check(lib.dbm_equilibrium_f64(r.data_ptr(), uu.data_ptr(), 128, lid, out.data_ptr(), _stream()))
+    np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-13, atol=1e-15)
+
+
+def test_collide_matches_reference_golden(golden):
+    lib, L = _lib()
+    g = golden("physics")
+    t = torch.tensor(g["D2Q7_col_f"], dtype=torch.float64, device="cuda")
+    L.check(lib.dbm_collide_f64(t.data_ptr(), t.shape[0], 0, ctypes.c_double(0.6), _stream()))
+    np.testing.assert_allclose(t.cpu().numpy(), g["D2Q7_col"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 255, 2048, 2049, 100_003, 1 << 20])
+@pytest.mark.parametrize("bits", [1, 7, 20, 32])
+def test_radix_sort_u32_stable_bit_exact(n, bits):
+    lib, L = _lib()
+    rng = np.random.default_rng(n + bits)
+    hi = min(1 << bits, 1 << 32)
+    keys = rng.integers(0, hi, size=n, dtype=np.uint64).astype(np.uint32)
+    if n > 10:
+        keys[: n // 3] = keys[0]  # many duplicates: stability matters
+    vals = np.arange(n, dtype=np.uint32)
+    order = np.argsort(keys, kind="stable")
+    k = torch.tensor(keys.view(np.int32), device="cuda")
+    v = torch.tensor(vals.view(np.int32), device="cuda")
+    tmp = torch.empty(max(int(lib.dbm_radix_sort_tmp_bytes(n, 4)), 1), dtype=torch.uint8, device="cuda")
+    L.check(lib.dbm_radix_sort_pairs_u32(k.data_ptr(), v.data_ptr(), n, bits, tmp.data_ptr(), _stream()))
+    np.testing.assert_array_equal(k.cpu().numpy().view(np.uint32), keys[order])
+    np.testing.assert_array_equal(v.cpu().numpy().view(np.uint32), vals[order])
+
+
+@pytest.mark.parametrize("n", [1, 5000, 300_001])
+def test_radix_sort_u64_stable_bit_exact(n):
+    lib, L = _lib()
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 1 << 63, size=n, dtype=np.uint64)
+    keys[::7] = keys[0]
+    vals = np.arange(n, dtype=np.uint32)
+    order = np.argsort(keys, kind="stable")
+    k = torch.tensor(keys.view(np.int64), device="cuda")
+    v = torch.tensor(vals.view(np.int32), device="cuda")
+    tmp = torch.empty(int(lib.dbm_radix_sort_tmp_bytes(n, 8)), dtype=torch.uint8, device="cuda")
+    L.check(lib.dbm_radix_sort_pairs_u64(k.data_ptr(), v.data_ptr(), n, 64, tmp.data_ptr(), _stream()))
+    np.testing.assert_array_equal(k.cpu().numpy().view(np.uint64), keys[order])
+    np.testing.assert_array_equal(v.cpu().numpy().view(np.uint32), vals[order])
+
+
+def test_lbm_fp64_matches_reference_golden(golden):
+    from direbm_gb300.lbm import HexLBM
+
+    g = golden("lbm")
+    lb = HexLBM(21, 21, [0.6], precision="fp64")
+    lb.set_f(g["pulse21_f0"])
+    lb.step(10)
+    np.testing.assert_allclose(lb.get_f()[0], g["pulse21_f10"], rtol=1e-13, atol=1e-15)
+    lb = HexLBM(25, 25, [0.7], precision="fp64")
+    lb.set_f(g["pulse25_f0"])
+    for _ in range(15):
+        lb.step(1)
+    np.testing.assert_allclose(lb.get_f()[0], g["pulse25_f15"], rtol=1e-13, atol=1e-15)
+
+
+def test_lbm_fp32dev_close_to_fp64_and_conserves_mass():
+    from direbm_gb300.lbm import HexLBM
+
+    f0 = olbm.set_pulse(olbm.rest_state(64, 48), 1.5)
+    ref = olbm.run(f0, 0.75, 40)
+    lb = HexLBM(64, 48, [0.75], precision="fp32dev")
+    lb.set_f(f0)
+    lb.step(40)
+    got = lb.get_f()[0]
+    dev_ref = ref - olbm.rest_state(64, 48)
+    # the deviation store keeps FP32 relative precision on the deviation, not on f
+    assert np.abs(got - ref).max() < 1e-7 * np.abs(dev_ref).max() + 1e-9
+    assert abs(got.sum() - f0.sum()) < 1e-5
+
+
+def test_lbm_batched_runs_are_independent():
+    from direbm_gb300.lbm import HexLBM
+
+    taus = [0.55, 0.8, 1.0]
+    f0 = olbm.shear_wave(32, 24, 0.01)
+    lb = HexLBM(32, 24, taus, precision="fp64")
+    lb.set_f(f0)
+    lb.step(7)
+    got = lb.get_f()
+    for r, tau in enumerate(taus):
+        np.testing.assert_allclose(got[r], olbm.run(f0, tau, 7), rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_lbm_shear_wave_decay_matches_analytic(precision):
+    """Config-2 physics on a reduced lattice: the shear mode decays at nu k^2 (nu = (tau-1/2)/4)."""
+    from direbm_gb300.lbm import HexLBM
+
+    nj, ni = 128, 16
+    taus = np.array([0.55, 0.7, 1.0])
+    lb = HexLBM(ni, nj, taus, precision=precision)
+    lb.set_f(olbm.shear_wave(ni, nj, 0.01))
+    a0 = lb.shear_amplitude()
+    steps = 400
+    lb.step(steps)
+    a1 = lb.shear_amplitude()
+    lam = -np.log(a1 / a0) / steps
+    lam_ref = np.array([olbm.shear_decay_rate(t, nj) for t in taus])
+    np.testing.assert_allclose(lam, lam_ref, rtol=0.02)

@@ -1,0 +1,260 @@
+"""Fused DiReBM step on the GPU vs the dense-grid oracle (oracle/grid_step.py).
+
+Integer outputs (occupied cells, component counts, direction masks, refined cells, sort order,
+emptiness masks, moment counts) are compared bit-exactly; FP64 values to 1e-12 relative to the
+largest magnitude (normwise); FP32DEV values against the FP64 oracle with the FP32 tolerance
+stated in each test.
+"""
+
+import numpy as np
+import pytest
+
+from _cases import bounded_box, oracle_spec, periodic_tg, rest_pulse
+from oracle import grid_step
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+
+
+def _sim(lattice, instances, precision, dx, r_res, cell, kappa_hard=4, cap=0, graphs=True):
+    from direbm_gb300.sim import Instance, Simulation
+
+    return Simulation([Instance(**i) for i in instances], lattice=lattice, precision=precision, dx=dx, r_res=r_res,
+                      cell=cell, kappa_hard=kappa_hard, moment_capacity=cap, graphs=graphs)
+
+
+def _as(buf, dtype):
+    return buf.cpu().numpy().view(dtype)
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)) if b.size else 0.0
+
+
+CASES = {
+    # name: (lattice, instances, dx, r_res, cell, builder)
+    "tg_d2q9_r15": ("D2Q9", [dict(dims=(20, 20), periodic=True, tau=0.6)], 1.0, 1.5, 1.0,
+                    lambda: periodic_tg(20, "D2Q9", seed=1)),
+    "tg_d2q7_ref": ("D2Q7", [dict(dims=(48, 48), periodic=True, tau=0.7)], 1.0, 1.0, 0.25,
+                    lambda: tuple(a for a in _scaled(periodic_tg(12, "D2Q7", seed=2), 1.0))),
+}
+
+
+def _scaled(case, s):
+    x, f = case
+    return x * s, f
+
+
+def _run_stages(name, precision="fp64"):
+    lattice, insts, dx, r, cell, build = CASES[name]
+    x, f = build()
+    dtype = np.float64 if precision == "fp64" else np.float32
+    spec = oracle_spec(lattice, insts, dx, r, cell, dtype=dtype)
+    st = grid_step.from_world(spec, np.zeros(len(x), int), x, f)
+    trace = {}
+    grid_step.step(spec, st, trace)
+    sim = _sim(lattice, insts, precision, dx, r, cell)
+    sim.set_state(None, x, f)
+    return spec, st, trace, sim
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_import_export_roundtrip(name):
+    lattice, insts, dx, r, cell, build = CASES[name]
+    x, f = build()
+    spec = oracle_spec(lattice, insts, dx, r, cell)
+    st = grid_step.from_world(spec, np.zeros(len(x), int), x, f)
+    _, xo, fo = grid_step.to_world(spec, st)
+    sim = _sim(lattice, insts, "fp64", dx, r, cell)
+    sim.set_state(None, x, f)
+    inst, xg, fg = sim.state_numpy()
+    assert len(xg) == len(x)
+    np.testing.assert_array_equal(xg, xo)
+    np.testing.assert_array_equal(fg, fo)
+    assert (inst == 0).all()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_stage_thin_refine_bit_exact(name):
+    spec, st, tr, sim = _run_stages(name)
+    sim.step_partial(2)
+    D = spec.D
+    nc = spec.ncells
+    occ = _as(sim.trace("occ"), np.uint32)
+    np.testing.assert_array_equal(np.flatnonzero(occ), tr["thin_cells"])
+    cnt = _as(sim.trace("thin_cnt"), np.uint32)
+    np.testing.assert_array_equal(cnt[tr["thin_cells"]], tr["thin_count"])
+    cen = _as(sim.trace("centroid"), np.float64).reshape(D, nc)[:, tr["thin_cells"]].T
+    assert _rel(cen, tr["centroid"]) < FP64_TOL
+    mask = _as(sim.trace("mask"), np.uint32)[tr["thin_cells"]]
+    np.testing.assert_array_equal(mask, tr["mask"])
+    fcell = _as(sim.trace("final_cell"), np.uint32)[tr["thin_cells"]]
+    np.testing.assert_array_equal(fcell, tr["final_cell"])
+    foff = _as(sim.trace("final_off"), np.float64).reshape(D, nc)[:, tr["thin_cells"]].T
+    assert _rel(foff, tr["final_off"]) < FP64_TOL
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_stage_sort_weights_gather(name):
+    spec, st, tr, sim = _run_stages(name)
+    sim.step_partial(5)
+    nc = spec.ncells
+    P = len(tr["order"])
+    counts = _as(sim.trace("counts"), np.uint32)
+    assert counts[0] == len(st.cell) and counts[1] == P
+    sp = _as(sim.trace("sorted"), np.uint32).reshape(2, nc)
+    np.testing.assert_array_equal(sp[0, :P], tr["final_cell"][tr["order"]])
+    np.testing.assert_array_equal(sp[1, :P], tr["thin_cells"][tr["order"]])
+    M = len(st.cell)
+    sw = _as(sim.trace("sw"), np.float64)
+    mcap = sw.size // spec.Q
+    sw = sw.reshape(spec.Q, mcap)[:, :M].T
+    assert _rel(sw, tr["sw"]) < FP64_TOL
+    cpf = _as(sim.trace("cpf"), np.float64)
+    ccap = cpf.size // spec.Q
+    cpf = cpf.reshape(spec.Q, ccap)[:, :P].T
+    assert _rel(cpf, tr["cp_f"]) < FP64_TOL
+    em = _as(sim.trace("empty"), np.uint32)[:P]
+    ref = (tr["empty"] * (1 << np.arange(spec.Q))).sum(1)
+    np.testing.assert_array_equal(em, ref)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("steps", [1, 4])
+def test_full_step_fp64(name, steps):
+    lattice, insts, dx, r, cell, build = CASES[name]
+    x, f = build()
+    spec = oracle_spec(lattice, insts, dx, r, cell)
+    st = grid_step.run(spec, grid_step.from_world(spec, np.zeros(len(x), int), x, f), steps)
+    _, xo, fo = grid_step.to_world(spec, st)
+    sim = _sim(lattice, insts, "fp64", dx, r, cell)
+    sim.set_state(None, x, f)
+    sim.step(steps)
+    _, xg, fg = sim.state_numpy()
+    assert len(xg) == len(xo)
+    assert np.abs(xg - xo).max() < 1e-11
+    assert _rel(fg, fo) < FP64_TOL
+    assert sim.status() == 0
+
+
+def test_bounded_reference_pulse_fp64():
+    """Reference-form parameters (D2Q7, r = dx = 1, cell = dx/4) on the reference's rest block + pulse."""
+    x, f = rest_pulse(6)
+    dims, origin = bounded_box(x, 0.25, 8.0)
+    insts = [dict(dims=dims, origin=origin, periodic=False, tau=0.6)]
+    spec = oracle_spec("D2Q7", insts, 1.0, 1.0, 0.25)
+    st = grid_step.run(spec, grid_step.from_world(spec, np.zeros(len(x), int), x, f), 3)
+    _, xo, fo = grid_step.to_world(spec, st)
+    sim = _sim("D2Q7", insts, "fp64", 1.0, 1.0, 0.25)
+    sim.set_state(None, x, f)
+    sim.step(3)
+    _, xg, fg = sim.state_numpy()
+    assert len(xg) == len(xo)
+    assert np.abs(xg - xo).max() < 1e-11
+    assert _rel(fg, fo) < FP64_TOL
+    assert sim.status() == 0
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_fp32dev_thinning_exact_and_step_close(name):
+    lattice, insts, dx, r, cell, build = CASES[name]
+    x, f = build()
+    spec32 = oracle_spec(lattice, insts, dx, r, cell, dtype=np.float32)
+    st32 = grid_step.from_world(spec32, np.zeros(len(x), int), x, f)
+    cells, cnt, _, _ = grid_step.thin(spec32, st32)
+    sim = _sim(lattice, insts, "fp32dev", dx, r, cell)
+    sim.set_state(None, x, f)
+    sim.step_partial(2)
+    occ = sim.trace("occ").cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(np.flatnonzero(occ), cells)
+    np.testing.assert_array_equal(sim.trace("thin_cnt").cpu().numpy().view(np.uint32)[cells], cnt)
+    # full step vs the FP64 oracle
+    sim2 = _sim(lattice, insts, "fp32dev", dx, r, cell)
+    sim2.set_state(None, x, f)
+    sim2.step(1)
+    _, xg, fg = sim2.state_numpy()
+    spec = oracle_spec(lattice, insts, dx, r, cell)
+    st = grid_step.step(spec, grid_step.from_world(spec, np.zeros(len(x), int), x, f))
+    _, xo, fo = grid_step.to_world(spec, st)
+    assert len(xg) == len(xo)
+    assert np.abs(xg - xo).max() < 2e-5 * cell * 8
+    assert _rel(fg, fo) < 2e-6
+
+
+def test_batch_equals_separate_runs():
+    """Instances in one batch evolve exactly as they do alone (bitwise)."""
+    insts = [dict(dims=(16, 16), periodic=True, tau=0.6), dict(dims=(24, 20), periodic=True, tau=0.8),
+             dict(dims=(12, 18), periodic=True, tau=0.55)]
+    data = []
+    for b, ins in enumerate(insts):
+        n0, n1 = ins["dims"]
+        rng = np.random.default_rng(10 + b)
+        x = np.stack(np.meshgrid(np.arange(n0) + 0.5, np.arange(n1) + 0.5, indexing="xy"), -1).reshape(-1, 2)
+        x = x + rng.uniform(-0.25, 0.25, size=x.shape)
+        x = np.mod(x, [n0, n1])
+        xo, fo = periodic_tg(4, "D2Q9", seed=b)
+        from oracle.physics import equilibrium
+        from oracle.lattices import D2Q9
+
+        u = 0.03 * np.stack([np.sin(2 * np.pi * x[:, 1] / n1), np.cos(2 * np.pi * x[:, 0] / n0)], 1)
+        f = equilibrium(np.ones(len(x)), u, D2Q9)
+        data.append((x, f))
+    sim = _sim("D2Q9", insts, "fp32dev", 1.0, 1.5, 1.0)
+    sim.set_state(np.concatenate([np.full(len(d[0]), b) for b, d in enumerate(data)]),
+                  np.concatenate([d[0] for d in data]), np.concatenate([d[1] for d in data]))
+    sim.step(3)
+    ib, xb, fb = sim.state_numpy()
+    for b, (ins, (x, f)) in enumerate(zip(insts, data)):
+        s1 = _sim("D2Q9", [ins], "fp32dev", 1.0, 1.5, 1.0)
+        s1.set_state(None, x, f)
+        s1.step(3)
+        _, x1, f1 = s1.state_numpy()
+        np.testing.assert_array_equal(xb[ib == b], x1)
+        np.testing.assert_array_equal(fb[ib == b], f1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_deterministic_and_graph_equivalent(precision):
+    x, f = periodic_tg(24, "D2Q9", seed=5)
+    insts = [dict(dims=(24, 24), periodic=True, tau=0.6)]
+    outs = []
+    for graphs in (True, True, False):
+        sim = _sim("D2Q9", insts, precision, 1.0, 1.5, 1.0, graphs=graphs)
+        sim.set_state(None, x, f)
+        sim.step(5)
+        outs.append(sim.state_numpy())
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_conservation_fp64_reduction():
+    x, f = periodic_tg(20, "D2Q9", seed=3)
+    sim = _sim("D2Q9", [dict(dims=(20, 20), periodic=True, tau=0.6)], "fp64", 1.0, 1.5, 1.0)
+    sim.set_state(None, x, f)
+    c = sim.conservation().cpu().numpy()[0]
+    np.testing.assert_allclose(c[0], f.sum(), rtol=1e-13)
+    from oracle.lattices import D2Q9
+
+    np.testing.assert_allclose(c[1:], (f @ D2Q9.C).sum(0), atol=1e-12)
+
+
+@pytest.mark.parametrize("lattice", ["D3Q19", "D3Q13"])
+def test_3d_full_step_fp64(lattice):
+    n = 10
+    x, f = periodic_tg(n, lattice, seed=7, u0=0.02)
+    insts = [dict(dims=(n, n, n), periodic=True, tau=0.6)]
+    r = 1.5
+    spec = oracle_spec(lattice, insts, 1.0, r, 1.0)
+    st = grid_step.run(spec, grid_step.from_world(spec, np.zeros(len(x), int), x, f), 2)
+    _, xo, fo = grid_step.to_world(spec, st)
+    sim = _sim(lattice, insts, "fp64", 1.0, r, 1.0)
+    sim.set_state(None, x, f)
+    sim.step(2)
+    _, xg, fg = sim.state_numpy()
+    assert len(xg) == len(xo)
+    assert np.abs(xg - xo).max() < 1e-11
+    assert _rel(fg, fo) < FP64_TOL

@@ -1,0 +1,113 @@
+"""Pin the CPU oracle against golden vectors produced by the reference's own CPU code."""
+
+import numpy as np
+import pytest
+
+from oracle import fields, grid_step, lbm, physics, stages
+from oracle.lattices import BY_NAME, D2Q7, D2Q9, D3Q13, D3Q19
+
+
+@pytest.mark.parametrize("name", ["D2Q7", "D2Q9", "D3Q13"])
+def test_physics_matches_reference(golden, name):
+    g = golden("physics")
+    lat = BY_NAME[name]
+    eq = physics.equilibrium(g[f"{name}_eq_rho"], g[f"{name}_eq_u"], lat)
+    np.testing.assert_allclose(eq, g[f"{name}_eq"], rtol=1e-13, atol=1e-15)
+    col = physics.collide(g[f"{name}_col_f"], 0.6, lat)
+    np.testing.assert_allclose(col, g[f"{name}_col"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("lat", [D2Q7, D2Q9, D3Q13, D3Q19])
+def test_lattice_moments(lat):
+    assert np.isclose(lat.W.sum(), 1.0)
+    m1 = lat.W @ lat.C
+    assert np.allclose(m1, 0.0, atol=1e-15)
+    m2 = np.einsum("i,ia,ib->ab", lat.W, lat.C, lat.C)
+    assert np.allclose(m2, lat.cs2 * np.eye(lat.D), atol=1e-14)
+
+
+def test_deviation_split_roundtrip():
+    rng = np.random.default_rng(4)
+    f = rng.uniform(0.01, 0.3, size=(64, 9))
+    rho, dev = physics.split_rest(f, D2Q9)
+    np.testing.assert_allclose(rho[:, None] * D2Q9.W + dev, f, rtol=1e-15, atol=1e-16)
+    np.testing.assert_allclose(dev.sum(axis=1), 0.0, atol=1e-15)
+
+
+def test_hex_lbm_matches_reference(golden):
+    g = golden("lbm")
+    f0 = lbm.set_pulse(lbm.rest_state(21, 21), 1.5)
+    np.testing.assert_array_equal(f0, g["pulse21_f0"])
+    np.testing.assert_allclose(lbm.run(f0, 0.6, 10), g["pulse21_f10"], rtol=1e-14, atol=1e-16)
+    f0 = lbm.set_pulse(lbm.rest_state(25, 25), 2.0)
+    np.testing.assert_allclose(lbm.run(f0, 0.7, 15), g["pulse25_f15"], rtol=1e-14, atol=1e-16)
+
+
+def test_fields_match_reference(golden):
+    g = golden("fields")
+    rho, u, _ = fields.bin_fields(g["x"], g["f"], -3, 4, 1.0)
+    np.testing.assert_allclose(rho, g["rho"], rtol=1e-14)
+    np.testing.assert_allclose(u, g["u"], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_stage_dispersion_and_thinning_match_reference_kat(golden, seed):
+    g = golden("propagation")
+    pos_c, val_c, dir_c = stages.disperse(g[f"s{seed}_pos_m"], g[f"s{seed}_f_m"], 1.0)
+    np.testing.assert_array_equal(pos_c, g[f"s{seed}_pos_c"])
+    np.testing.assert_array_equal(dir_c, np.tile(np.arange(7), len(g[f"s{seed}_pos_m"])))
+    cp, _, _, _ = stages.create_control_points(pos_c, 0.25)
+    ref = g[f"s{seed}_cp"]
+    assert len(cp) == len(ref)  # exact count, as the reference test requires
+    srt = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]  # noqa: E731
+    np.testing.assert_allclose(srt(cp.astype(np.float64)), srt(ref), atol=1e-5)
+
+
+def test_stage_refine_ring_fixtures(golden):
+    g = golden("propagation")
+    new, kappa = stages.refine_control_points(g["ringAB_cp"], g["ringAB_pos"], g["ringAB_val"], g["ringAB_dir"], 1.0, 4)
+    assert list(kappa) == [7, 3]
+    np.testing.assert_allclose(new, g["ringAB_expected"], atol=1e-6)
+    new, kappa = stages.refine_control_points(g["ring45_cp"], g["ring45_pos"], g["ring45_val"], g["ring45_dir"], 1.0, 4)
+    assert list(kappa) == [4, 5]
+    assert np.allclose(new[0], [0.0, 0.0], atol=1e-6)
+    assert not np.allclose(new[1], [20.0, 0.0], atol=1e-3)
+
+
+def _unbounded_spec(lat, dx, r, cell, box_lo, box_hi, kappa_hard=4, dtype=np.float64):
+    lo = np.floor(np.asarray(box_lo) / cell).astype(int) - 4
+    hi = np.ceil(np.asarray(box_hi) / cell).astype(int) + 4
+    inst = grid_step.Instance(dims=tuple(int(v) for v in hi - lo), origin=tuple(int(v) for v in lo), periodic=False)
+    return grid_step.GridSpec(lattice=lat, dx=dx, r_res=r, cell=cell, kappa_hard=kappa_hard, instances=[inst], dtype=dtype)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_grid_thinning_matches_reference_kat(golden, seed):
+    """The grid oracle's thinning reproduces _cell_thin_ref's CP count and centroids."""
+    g = golden("propagation")
+    pos_m, f_m = g[f"s{seed}_pos_m"], g[f"s{seed}_f_m"]
+    spec = _unbounded_spec(D2Q7, 1.0, 1.0, 0.25, pos_m.min(0) - 2, pos_m.max(0) + 2)
+    st = grid_step.from_world(spec, np.zeros(len(pos_m), int), pos_m, f_m)
+    cells, cnt, cen, _ = grid_step.thin(spec, st)
+    ref = g[f"s{seed}_cp"]
+    assert len(cells) == len(ref)
+    assert cnt.sum() == 7 * len(pos_m)
+    b, F = grid_step.decode(spec, cells)
+    origin = np.array(spec.instances[0].origin)
+    world = (origin + F + cen) * 0.25
+    srt = lambda a: a[np.lexsort((a[:, 1], a[:, 0]))]  # noqa: E731
+    np.testing.assert_allclose(srt(world), srt(ref), atol=2e-6)
+
+
+def test_grid_step_conserves_rest_field():
+    """A uniform periodic rest field stays at rest: every direction is delivered, f stays rho*W."""
+    spec = grid_step.GridSpec(lattice=D2Q9, dx=1.0, r_res=1.5, cell=1.0, kappa_hard=4,
+                              instances=[grid_step.Instance(dims=(12, 12), tau=0.6)])
+    xs = np.array([[i + 0.5, j + 0.5] for j in range(12) for i in range(12)])
+    f = np.tile(D2Q9.W, (len(xs), 1))
+    st = grid_step.from_world(spec, np.zeros(len(xs), int), xs, f)
+    st2 = grid_step.step(spec, st)
+    assert len(st2.cell) == len(xs)
+    rho, u = physics.recover(st2.f, D2Q9)
+    np.testing.assert_allclose(rho, 1.0, rtol=1e-12)
+    np.testing.assert_allclose(u, 0.0, atol=1e-13)
