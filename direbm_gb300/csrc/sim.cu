@@ -171,9 +171,11 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
               mask |= 1u << k;
               const real w = exp(fstar_at<Q, D, P>(A, m, k));
               if constexpr (std::is_same<P, PF64>::value) {
-                swd += w;
+                // separate rounding of product and sum (no FMA), in loop order: the oracle
+                // reproduces this sum bit for bit
+                swd = __dadd_rn(swd, w);
 #pragma unroll
-                for (int a = 0; a < D; ++a) sxd[a] += w * q[a];
+                for (int a = 0; a < D; ++a) sxd[a] = __dadd_rn(sxd[a], __dmul_rn(w, q[a]));
               } else {
                 sws.add(w);
 #pragma unroll

@@ -212,9 +212,40 @@ def collide_state(spec: GridSpec, st: GridState):
     return collide_unguarded(st.f, spec.tau_arr()[b], spec.lattice)
 
 
+def ordered_sums(group, order_keys, vals, ngroups):
+    """Per-group sequential sums of ``vals`` (N, ...) in the order given by ``order_keys`` (a list
+    of key arrays, most significant first): each group is summed left to right with one rounding
+    per addition, which is how one CUDA thread accumulates it."""
+    vals = np.asarray(vals, dtype=np.float64)
+    out = np.zeros((ngroups,) + vals.shape[1:])
+    if len(group) == 0:
+        return out
+    idx = np.lexsort(tuple(reversed([group] + list(order_keys))))
+    g = group[idx]
+    v = vals[idx]
+    head = np.ones(len(g), dtype=bool)
+    head[1:] = g[1:] != g[:-1]
+    starts = np.flatnonzero(head)
+    lens = np.diff(np.append(starts, len(g)))
+    gid = g[starts]
+    acc = np.zeros((len(starts),) + vals.shape[1:])
+    for j in range(int(lens.max())):
+        live = lens > j
+        acc[live] = acc[live] + v[starts[live] + j]
+    out[gid] = acc
+    return out
+
+
+def _so_keys(dS, D):
+    """Window offsets (z, y, x) as sort keys, in the kernels' loop nesting (z outer, x inner)."""
+    z = dS[:, 2] if D == 3 else np.zeros(len(dS), np.int64)
+    return [z, dS[:, 1], dS[:, 0]]
+
+
 def thin(spec: GridSpec, st: GridState):
     """Stage 2.  Returns (occupied global cells sorted, count per CP, centroid rel (P,D),
-    component landing cell per (m,k) (or -1 outside a non-periodic box))."""
+    component landing cell per (m,k) (or -1 outside a non-periodic box)).  The centroid sum runs
+    in the kernel's order: direction, then source-cell offset, then moment."""
     m, k, b, S, t = components(spec, st)
     fl = np.floor(t).astype(np.int64)
     C = encode(spec, b, S + fl)
@@ -222,8 +253,8 @@ def thin(spec: GridSpec, st: GridState):
     ok = C >= 0
     cells, inv = np.unique(C[ok], return_inverse=True)
     cnt = np.bincount(inv, minlength=len(cells))
-    sums = np.zeros((len(cells), spec.D))
-    np.add.at(sums, inv, rel[ok].astype(np.float64))
+    so = -fl[ok]
+    sums = ordered_sums(inv, [k[ok]] + _so_keys(so, spec.D) + [m[ok]], rel[ok].astype(np.float64), len(cells))
     cen = (sums / cnt[:, None]).astype(spec.dtype)
     return cells, cnt, cen, C
 
@@ -238,7 +269,7 @@ def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
     order = np.argsort(cp_cell, kind="stable")
     cs = cp_cell[order]
     Rc = int(np.ceil(float(spec.R)))
-    ci_all, pj_all, d_all, q_all = [], [], [], []
+    ci_all, pj_all, d_all, q_all, ds_all = [], [], [], [], []
     for o in _offsets(spec.D, -Rc - 1, Rc + 1):
         G = encode(spec, b, S + fl + o)
         lo = np.searchsorted(cs, G, side="left")
@@ -258,26 +289,28 @@ def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
         pj_all.append(pj[keep])
         d_all.append(d[keep])
         q_all.append(q[keep])
+        ds_all.append(dS[keep])
     if not ci_all:
         z = np.zeros(0, np.int64)
-        return z, z, np.zeros(0, spec.dtype), np.zeros((0, spec.D), spec.dtype)
-    return np.concatenate(ci_all), np.concatenate(pj_all), np.concatenate(d_all), np.concatenate(q_all)
+        return z, z, np.zeros(0, spec.dtype), np.zeros((0, spec.D), spec.dtype), np.zeros((0, spec.D), np.int64)
+    return (np.concatenate(ci_all), np.concatenate(pj_all), np.concatenate(d_all), np.concatenate(q_all),
+            np.concatenate(ds_all))
 
 
 def refine(spec: GridSpec, st: GridState, fstar, cells, cen):
     """Stage 3.  Returns (mask, kappa, final global cell, final offset) per CP (thinning order)."""
     comps = components(spec, st)
     m, k, b, S, t = comps
-    ci, pj, d, q = _pairs_comp_cp(spec, st, cells, cen, comps)
+    ci, pj, d, q, dS = _pairs_comp_cp(spec, st, cells, cen, comps)
     P = len(cells)
     mask = np.zeros(P, dtype=np.int64)
     np.bitwise_or.at(mask, pj, np.left_shift(1, k[ci]))
     kappa = np.array([bin(int(x)).count("1") for x in mask], dtype=np.int64)
     w = np.exp(fstar[m[ci], k[ci]])
-    sw = np.zeros(P)
-    sx = np.zeros((P, spec.D))
-    np.add.at(sw, pj, w)
-    np.add.at(sx, pj, w[:, None] * q.astype(np.float64))
+    # sums in the kernel's order: direction, window offset (z, y, x), moment
+    keys = [k[ci]] + _so_keys(dS, spec.D) + [m[ci]]
+    sw = ordered_sums(pj, keys, w, P)
+    sx = ordered_sums(pj, keys, w[:, None] * q.astype(np.float64), P)
     move = kappa > spec.kappa_hard
     npos = cen.astype(spec.dtype).copy()
     npos[move] = (sx[move] / sw[move, None]).astype(spec.dtype)
@@ -301,7 +334,7 @@ def weights(spec: GridSpec, st: GridState, cp_cell, cp_off, comps=None):
     if comps is None:
         comps = components(spec, st)
     m = comps[0]
-    ci, pj, d, _ = _pairs_comp_cp(spec, st, cp_cell, cp_off, comps)
+    ci, pj, d, _, _ = _pairs_comp_cp(spec, st, cp_cell, cp_off, comps)
     wv = (spec.R - d).astype(np.float64)
     sw = np.zeros(len(m))
     np.add.at(sw, ci, wv)
