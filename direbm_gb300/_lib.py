@@ -70,6 +70,7 @@ _SIGS = {
     "dbm_radix_sort_tmp_bytes": (_i64, [_i64, ctypes.c_int]),
     "dbm_radix_sort_pairs_u32": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, _vp]),
     "dbm_radix_sort_pairs_u64": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, _vp]),
+    "dbm_radix_sort_pairs_u32_noalloc": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp]),
     "dbm_disperse_f32": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _f32, _vp, _vp, _vp, _vp]),
     "dbm_create_control_points_f32": (ctypes.c_int, [_vp, _i64, _f32, _vp, ctypes.POINTER(_i64), _vp]),
     "dbm_refine_control_points_f32": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp, _i64, _f32, ctypes.c_int, _vp, _vp]),

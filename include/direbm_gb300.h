@@ -65,6 +65,18 @@ int64_t dbm_radix_sort_tmp_bytes(int64_t n, int key_bytes);
 int dbm_radix_sort_pairs_u32(uint32_t* d_keys, uint32_t* d_vals, int64_t n, int key_bits, void* d_tmp, void* stream);
 int dbm_radix_sort_pairs_u64(uint64_t* d_keys, uint32_t* d_vals, int64_t n, int key_bits, void* d_tmp, void* stream);
 
+/* The same stable sort for callers that may not allocate device memory (no counterpart in the
+ * reference).  A host program that owns all device memory in its own pool, or a latency-critical
+ * loop that cannot afford the device-wide synchronisation of cudaMalloc/cudaFree, cannot provide
+ * the scratch buffer dbm_radix_sort_pairs_u32 asks for.  This entry point uses a fixed scratch
+ * array compiled into the library instead (about 2.2 MB held on every GPU that loads it until the
+ * process exits) and never allocates or frees.  At most DBM_NOALLOC_SORT_MAX_PAIRS pairs per
+ * call (larger n returns DBM_ERR_CAPACITY).  The first call on each device looks up the scratch
+ * address; make it before any stream capture.  Calls share the scratch: calls that overlap on
+ * the GPU race, so order them on one stream. */
+#define DBM_NOALLOC_SORT_MAX_PAIRS 262144
+int dbm_radix_sort_pairs_u32_noalloc(uint32_t* d_keys, uint32_t* d_vals, int64_t n, int key_bits, void* stream);
+
 /* ---- stage functions on explicit component arrays (FP32, 2D D2Q7 layout of the reference) ---
  * disperse: direbm/warp/propagation.py:21-36,115-127.  pos_m (M,2), f_m (M,Q) -> pos_c (Q*M,2),
  * val_c (Q*M), dir_c (Q*M), component index Q*i + k. */
