@@ -19,7 +19,7 @@ FP64, FP32DEV = 0, 1
 
 TRACE = {
     "occ": 1, "thin_cnt": 2, "centroid": 3, "mask": 4, "final_cell": 5, "final_off": 6,
-    "sorted": 7, "sw": 8, "cpf": 9, "empty": 10, "fstar": 11, "counts": 12,
+    "sorted": 7, "sw": 8, "cpf": 9, "empty": 10, "fstar": 11, "counts": 12, "state_cell": 13, "state_off": 14,
 }
 
 ST_OUT_OF_BOX, ST_CAPACITY, ST_NONFINITE, ST_BAD_INPUT = 1, 2, 4, 8
@@ -87,6 +87,7 @@ _SIGS = {
     "dbm_sim_status": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_uint32), _i32, _vp]),
     "dbm_sim_conservation": (ctypes.c_int, [_vp, _vp, _vp]),
     "dbm_sim_use_graphs": (ctypes.c_int, [_vp, _i32]),
+    "dbm_sim_set_option": (ctypes.c_int, [_vp, _i32, _i32]),
     "dbm_sim_trace": (ctypes.c_int, [_vp, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp]),
     "dbm_sim_device_bytes": (_i64, [_vp]),
 }

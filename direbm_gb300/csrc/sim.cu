@@ -19,6 +19,8 @@
 // run.  FP32DEV stores f as rho (FP32) + dev_k = f_k - rho*W_k (FP32), sums with compensated
 // (TwoSum/TwoProd) FP32 accumulators and forms the emitted rho and dev in double-float.
 #include <algorithm>
+#include <cmath>
+#include <limits>
 #include <vector>
 
 #include "sim.cuh"
@@ -140,16 +142,19 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
   }
 
   // ---- refine: components within R of the centroid ---------------------------------------------
+  // The move is accumulated as displacements e from the centroid: new = cen + sum(w e) / sum(w).
   uint32_t mask = 0;
   double swd = 0, sxd[3] = {0, 0, 0};
-  CSum sws, sxs[3];
+  float swf = 0.f, sxf[3] = {0.f, 0.f, 0.f};
 #pragma unroll 1
   for (int k = 0; k < Q; ++k) {
     int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    real cdk[3] = {0, 0, 0};
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      real base = cen[a] - (real)A.L.cd[k][a];
-      lo[a] = (int)floor(base - A.R - A.tiny) - 1;
+      cdk[a] = (real)A.L.cd[k][a];
+      const real base = cen[a] - cdk[a];
+      lo[a] = (int)floor(base - A.R - A.tiny);
       hi[a] = (int)floor(base + A.R + A.tiny);
     }
 #pragma unroll 1
@@ -158,16 +163,19 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
       for (int sy = lo[1]; sy <= hi[1]; ++sy)
 #pragma unroll 1
         for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+          const int dS[3] = {sx, sy, sz};
+          real c[3] = {0, 0, 0};
+#pragma unroll
+          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], cen[a]);
+          if (cell_d2_lower<D, real>(c) > A.R2) continue;
           uint32_t Sg;
           if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
-          const int dS[3] = {sx, sy, sz};
           const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
           for (uint32_t m = m0; m < m1; ++m) {
-            real t[3], q[3];
+            real o[3] = {0, 0, 0}, e[3];
 #pragma unroll
-            for (int a = 0; a < D; ++a) t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
-            const real d = canon_dist<D, real>(dS, t, cen, q);
-            if (d <= A.R) {
+            for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+            if (canon_d2<D, real>(o, c, e) <= A.R2) {
               mask |= 1u << k;
               const real w = exp(fstar_at<Q, D, P>(A, m, k));
               if constexpr (std::is_same<P, PF64>::value) {
@@ -175,11 +183,11 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
                 // reproduces this sum bit for bit
                 swd = __dadd_rn(swd, w);
 #pragma unroll
-                for (int a = 0; a < D; ++a) sxd[a] = __dadd_rn(sxd[a], __dmul_rn(w, q[a]));
+                for (int a = 0; a < D; ++a) sxd[a] = __dadd_rn(sxd[a], __dmul_rn(w, e[a]));
               } else {
-                sws.add(w);
+                swf += w;
 #pragma unroll
-                for (int a = 0; a < D; ++a) sxs[a].add_prod(w, q[a]);
+                for (int a = 0; a < D; ++a) sxf[a] = fmaf(w, e[a], sxf[a]);
               }
             }
           }
@@ -192,9 +200,9 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
     if (kappa <= A.kappa_hard) {
       np[a] = cen[a];
     } else if constexpr (std::is_same<P, PF64>::value) {
-      np[a] = sxd[a] / swd;
+      np[a] = __dadd_rn(cen[a], __ddiv_rn(sxd[a], swd));
     } else {
-      np[a] = sxs[a].value() / sws.value();
+      np[a] = cen[a] + sxf[a] / swf;
     }
   }
   bool finite = true;
@@ -271,13 +279,15 @@ __global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q,
   const InstK I = A.inst[b];
   int Sc[3];
   decode_cell<D>(I, g, Sc);
-  real t[3] = {0, 0, 0};
+  real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
-    lo[a] = (int)floor(t[a] - A.R - A.tiny) - 1;
-    hi[a] = (int)floor(t[a] + A.R + A.tiny);
+    o[a] = A.a.off[(int64_t)a * A.mcap + m];
+    cdk[a] = (real)A.L.cd[k][a];
+    const real t = rn_add(o[a], cdk[a]);
+    lo[a] = (int)floor(t - A.R - A.tiny);
+    hi[a] = (int)floor(t + A.R + A.tiny);
   }
   double swd = 0;
   CSum sws;
@@ -287,23 +297,37 @@ __global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q,
     for (int gy = lo[1]; gy <= hi[1]; ++gy)
 #pragma unroll 1
       for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+        const int dG[3] = {gx, gy, gz};
+        // per cell: base = float(dS) + cd with dS = -dG; control-point offsets lie in [0, 1)
+        real base[3] = {0, 0, 0}, lb[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          base[a] = rn_add((real)(-dG[a]), cdk[a]);
+          // candidates have e in [fl(o + fl(base - 1)), fl(o + base)]
+          const real elo = rn_add(o[a], rn_sub(base[a], (real)1)), ehi = rn_add(o[a], base[a]);
+          lb[a] = elo > (real)0 ? elo : (ehi < (real)0 ? -ehi : (real)0);
+        }
+        real lb2 = 0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) lb2 = a == 0 ? rn_mul(lb[a], lb[a]) : rn_add(lb2, rn_mul(lb[a], lb[a]));
+        if (lb2 > A.R2) continue;
         uint32_t Gg;
         if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Gg)) continue;
-        const int dS[3] = {-gx, -gy, -gz};
         const uint32_t c0 = A.b.start[Gg], c1 = A.b.start[Gg + 1];
         for (uint32_t c = c0; c < c1; ++c) {
-          real p[3], q[3];
+          real cc[3] = {0, 0, 0}, e[3];
 #pragma unroll
-          for (int a = 0; a < D; ++a) p[a] = A.b.off[(int64_t)a * A.ccap + c];
-          const real d = canon_dist<D, real>(dS, t, p, q);
-          if (d <= A.R) {
+          for (int a = 0; a < D; ++a) cc[a] = rn_sub(base[a], A.b.off[(int64_t)a * A.ccap + c]);
+          const real d2 = canon_d2<D, real>(o, cc, e);
+          if (d2 <= A.R2) {
+            const real d = rn_sqrt(d2);
             if constexpr (std::is_same<P, PF64>::value) swd += A.R - d; else sws.add(A.R - d);
           }
         }
       }
   real sw;
   if constexpr (std::is_same<P, PF64>::value) sw = swd; else sw = sws.value();
-  A.sw[(int64_t)k * A.mcap + m] = sw;
+  A.sw[(int64_t)k * A.mcap + m] = sw > (real)0 ? (real)1 / sw : (real)0;  // stored inverted
 }
 
 template <int Q, int D, class P>
@@ -318,13 +342,14 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
   const InstK I = A.inst[b];
   int Gc[3];
   decode_cell<D>(I, G, Gc);
-  real p[3] = {0, 0, 0};
+  real p[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     p[a] = A.b.off[(int64_t)a * A.ccap + j];
-    real base = p[a] - (real)A.L.cd[k][a];
-    lo[a] = (int)floor(base - A.R - A.tiny) - 1;
+    cdk[a] = (real)A.L.cd[k][a];
+    const real base = p[a] - cdk[a];
+    lo[a] = (int)floor(base - A.R - A.tiny);
     hi[a] = (int)floor(base + A.R + A.tiny);
   }
   double acc = 0;
@@ -335,19 +360,23 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
     for (int sy = lo[1]; sy <= hi[1]; ++sy)
 #pragma unroll 1
       for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+        const int dS[3] = {sx, sy, sz};
+        real c[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], p[a]);
+        if (cell_d2_lower<D, real>(c) > A.R2) continue;
         uint32_t Sg;
         if (!cell_at<D>(I, Gc[0] + sx, Gc[1] + sy, Gc[2] + sz, &Sg)) continue;
-        const int dS[3] = {sx, sy, sz};
         const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
         for (uint32_t m = m0; m < m1; ++m) {
-          real t[3], q[3];
+          real o[3] = {0, 0, 0}, e[3];
 #pragma unroll
-          for (int a = 0; a < D; ++a) t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
-          const real d = canon_dist<D, real>(dS, t, p, q);
-          if (d <= A.R) {
-            const real s = A.sw[(int64_t)k * A.mcap + m];
-            if (s > (real)0) {
-              const real wgt = (A.R - d) / s;
+          for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+          const real d2 = canon_d2<D, real>(o, c, e);
+          if (d2 <= A.R2) {
+            const real inv = A.sw[(int64_t)k * A.mcap + m];
+            if (inv > (real)0) {
+              const real wgt = (A.R - rn_sqrt(d2)) * inv;
               if constexpr (std::is_same<P, PF64>::value) {
                 acc += wgt * A.a.f64[(int64_t)k * A.mcap + m];
               } else {
@@ -395,7 +424,7 @@ __global__ void __launch_bounds__(256) k_emit(const __grid_constant__ Args<Q, D,
 #pragma unroll
       for (int a = 0; a < D; ++a) {
         p[a] = A.b.off[(int64_t)a * A.ccap + j];
-        lo[a] = (int)floor(p[a] - A.R - A.tiny) - 1;
+        lo[a] = (int)floor(p[a] - A.R - A.tiny);
         hi[a] = (int)floor(p[a] + A.R + A.tiny);
       }
       CSum sws[Q];
@@ -405,19 +434,23 @@ __global__ void __launch_bounds__(256) k_emit(const __grid_constant__ Args<Q, D,
         for (int gy = lo[1]; gy <= hi[1]; ++gy)
 #pragma unroll 1
           for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+            const int dS[3] = {gx, gy, gz};
+            real cc[3] = {0, 0, 0};
+#pragma unroll
+            for (int a = 0; a < D; ++a) cc[a] = canon_c<real>(dS[a], (real)0, p[a]);
+            if (cell_d2_lower<D, real>(cc) > A.R2) continue;
             uint32_t Hg;
             if (!cell_at<D>(I, Gc[0] + gx, Gc[1] + gy, Gc[2] + gz, &Hg)) continue;
-            const int dS[3] = {gx, gy, gz};
             const uint32_t c0 = A.b.start[Hg], c1 = A.b.start[Hg + 1];
             for (uint32_t c = c0; c < c1; ++c) {
               const uint32_t both = A.emask[c] & em;
               if (!both) continue;
-              real t[3], q[3];
+              real o[3] = {0, 0, 0}, e[3];
 #pragma unroll
-              for (int a = 0; a < D; ++a) t[a] = A.b.off[(int64_t)a * A.ccap + c];
-              const real d = canon_dist<D, real>(dS, t, p, q);
-              if (d <= A.R) {
-                const real w = A.R - d;
+              for (int a = 0; a < D; ++a) o[a] = A.b.off[(int64_t)a * A.ccap + c];
+              const real d2 = canon_d2<D, real>(o, cc, e);
+              if (d2 <= A.R2) {
+                const real w = A.R - rn_sqrt(d2);
 #pragma unroll
                 for (int k = 0; k < Q; ++k) {
                   if ((both >> k) & 1u) {
@@ -587,7 +620,27 @@ __global__ void __launch_bounds__(256) k_conservation(const __grid_constant__ Ar
   }
 }
 
+}  // namespace dbm
+
+#include "sim_tiled.cuh"
+
+namespace dbm {
+
 // ---- host side ------------------------------------------------------------------------------------
+
+// Largest x with correctly rounded sqrt(x) <= R: the squared-distance test d2 <= R2 then takes
+// exactly the decisions of sqrt(d2) <= R (sqrt is monotonic and correctly rounded on host and
+// device).
+template <class T>
+static T sqrt_threshold(T R) {
+  T x = R * R;
+  for (int i = 0; i < 64; ++i) {
+    const T n = std::nextafter(x, std::numeric_limits<T>::infinity());
+    if (std::sqrt(n) <= R) x = n; else break;
+  }
+  for (int i = 0; i < 64 && std::sqrt(x) > R; ++i) x = std::nextafter(x, (T)0);
+  return x;
+}
 
 struct SimBase {
   virtual ~SimBase() = default;
@@ -602,6 +655,8 @@ struct SimBase {
   virtual int trace(int, void*, int64_t, int64_t*, cudaStream_t) = 0;
   virtual int64_t device_bytes() const = 0;
   int use_graphs = 1;
+  int use_tiles = 1;
+  virtual void invalidate_graphs() = 0;
 };
 
 template <int Q, int D, class P>
@@ -627,6 +682,12 @@ struct SimImpl : SimBase {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   unsigned long long graph_kernels = 0;
   int trace_on = 0;
+  // shared-memory tiling (2D)
+  bool tiled = false;
+  Tile2* d_tiles = nullptr;
+  int ntiles = 0;
+  TileGeo geo{};
+  size_t sm_refine = 0, sm_weights = 0, sm_gather = 0;
 
   ~SimImpl() override {
     for (auto& g : graph)
@@ -725,6 +786,7 @@ struct SimImpl : SimBase {
     A.n_inst = n;
     A.ncells = ncells;
     A.R = (real)R;
+    A.R2 = sqrt_threshold<real>(A.R);
     A.tiny = (real)1e-4;
     A.kappa_hard = d.kappa_hard;
     A.eps = (real)d.eps;
@@ -758,10 +820,106 @@ struct SimImpl : SimBase {
     DBM_TRY(alloc(&A.d_P, 1));
     DBM_CUDA(cudaMemset(A.status, 0, 4));
     DBM_CUDA(cudaMemset(A.d_P, 0, 4));
+    if constexpr (D == 2) DBM_TRY(init_tiles(LH, R));
     DBM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
     return DBM_OK;
+  }
+
+  // Tile table, halos and shared-memory budgets of the tiled kernels (2D only).
+  static size_t carve_bytes(const std::vector<std::pair<size_t, size_t>>& parts) {
+    size_t off = 0;
+    for (auto& pr : parts) off = ((off + 15) & ~(size_t)15) + pr.first * pr.second;
+    return off + 16;
+  }
+  size_t smem_for(int kind, int cap) const {
+    const size_t rs = sizeof(real);
+    const size_t ct = (size_t)geo.cap_tile;
+    const size_t cp = (size_t)cap;
+    if (kind == 0) {  // thin+refine
+      const size_t cells = (size_t)(geo.tx + geo.mom.xh - geo.mom.xl) * (geo.ty + geo.mom.yh - geo.mom.yl);
+      const size_t rh = geo.ty + geo.mom.yh - geo.mom.yl;
+      return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4 * rs}, {(size_t)Q * cp, rs}});
+    } else if (kind == 1) {  // weights
+      const size_t cells = (size_t)(geo.tx + geo.cp.xh - geo.cp.xl) * (geo.ty + geo.cp.yh - geo.cp.yl);
+      const size_t rh = geo.ty + geo.cp.yh - geo.cp.yl;
+      return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4 * rs}, {(size_t)2 * geo.ty + 2, 4}, {ct, 4},
+                          {ct, 2}, {ct, 2}, {ct, 2 * rs}});
+    } else {  // gather
+      const size_t cells = (size_t)(geo.tx + geo.mom.xh - geo.mom.xl) * (geo.ty + geo.mom.yh - geo.mom.yl);
+      const size_t rh = geo.ty + geo.mom.yh - geo.mom.yl;
+      return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4}, {cp, 4 * rs}, {cp, rs}, {cp, 2 * rs},
+                          {(size_t)2 * geo.ty + 2, 4}, {ct, 4}, {ct, 2}, {ct, 2}, {ct, 2 * rs}});
+    }
+  }
+  int pick_cap(int kind, int cells, size_t budget) const {
+    int cap = cells + cells / 2 + 64;  // 1.5 items per region cell; denser regions read global memory
+    while (cap > 64 && smem_for(kind, cap) > budget) cap = cap * 7 / 8;
+    return cap;
+  }
+
+  int init_tiles(const LatHost& LH, double R) {
+    geo.tx = 32;
+    geo.ty = 8;
+    const double tiny = 2e-4;
+    Halo m{0, 0, 0, 0}, c{0, 0, 0, 0};
+    for (int k = 0; k < Q; ++k) {
+      for (int a = 0; a < 2; ++a) {
+        // cover both the FP64 displacement and its FP32 rounding (the FP32 kernels use the latter)
+        const double cd64 = LH.c[k][a] * desc.dx / desc.cell;
+        const double cd32 = (double)(float)cd64;
+        const double cdmin = std::min(cd64, cd32), cdmax = std::max(cd64, cd32);
+        int lo = (int)std::floor(-cdmax - R - tiny), hi = (int)std::floor(1.0 - cdmin + R + tiny);
+        lo = std::min(lo, -(int)std::floor(cdmax) - 1);
+        hi = std::max(hi, -(int)std::floor(cdmin));
+        const int clo = (int)std::floor(cdmin - R - tiny), chi = (int)std::floor(cdmax + 1.0 + R + tiny);
+        if (a == 0) {
+          m.xl = std::min(m.xl, lo); m.xh = std::max(m.xh, hi);
+          c.xl = std::min(c.xl, clo); c.xh = std::max(c.xh, chi);
+        } else {
+          m.yl = std::min(m.yl, lo); m.yh = std::max(m.yh, hi);
+          c.yl = std::min(c.yl, clo); c.yh = std::max(c.yh, chi);
+        }
+      }
+    }
+    geo.mom = m;
+    geo.cp = c;
+    const int mcells = (geo.tx + m.xh - m.xl) * (geo.ty + m.yh - m.yl);
+    const int ccells = (geo.tx + c.xh - c.xl) * (geo.ty + c.yh - c.yl);
+    const size_t budget = std::is_same<P, PF64>::value ? 112 * 1024 : 56 * 1024;
+    geo.cap_tile = 2 * geo.tx * geo.ty;
+    geo.cap_refine = pick_cap(0, mcells, budget);
+    geo.cap_weights = pick_cap(1, ccells, budget);
+    geo.cap_gather = pick_cap(2, mcells, budget);
+    sm_refine = smem_for(0, geo.cap_refine);
+    sm_weights = smem_for(1, geo.cap_weights);
+    sm_gather = smem_for(2, geo.cap_gather);
+    std::vector<Tile2> tiles;
+    for (int i = 0; i < (int)inst_h.size(); ++i)
+      for (int y0 = 0; y0 < inst_h[i].dims[1]; y0 += geo.ty)
+        for (int x0 = 0; x0 < inst_h[i].dims[0]; x0 += geo.tx) tiles.push_back({i, x0, y0});
+    ntiles = (int)tiles.size();
+    DBM_TRY(alloc(&d_tiles, ntiles));
+    DBM_CUDA(cudaMemcpy(d_tiles, tiles.data(), sizeof(Tile2) * ntiles, cudaMemcpyHostToDevice));
+    if constexpr (D == 2) {
+      DBM_CUDA(cudaFuncSetAttribute((const void*)k_thin_refine_t<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sm_refine));
+      DBM_CUDA(cudaFuncSetAttribute((const void*)k_weights_t<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sm_weights));
+      DBM_CUDA(cudaFuncSetAttribute((const void*)k_gather_t<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sm_gather));
+    }
+    tiled = true;
+    return DBM_OK;
+  }
+
+  void invalidate_graphs() override {
+    for (auto& g : graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
   }
 
   void bind() {
@@ -818,7 +976,12 @@ struct SimImpl : SimBase {
     DBM_LAUNCH_CHECK();
     mark(1, s);
     if (upto <= 1) return DBM_OK;
-    k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
+    if constexpr (D == 2) {
+      if (tiled && use_tiles) k_thin_refine_t<Q, P><<<ntiles, 256, sm_refine, s>>>(A, d_tiles, geo);
+      else k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
+    } else {
+      k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
+    }
     DBM_LAUNCH_CHECK();
     mark(2, s);
     if (upto <= 2) return DBM_OK;
@@ -836,12 +999,22 @@ struct SimImpl : SimBase {
     DBM_LAUNCH_CHECK();
     mark(3, s);
     if (upto <= 3) return DBM_OK;
-    k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
+    if constexpr (D == 2) {
+      if (tiled && use_tiles) k_weights_t<Q, P><<<ntiles, 256, sm_weights, s>>>(A, d_tiles, geo);
+      else k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
+    } else {
+      k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
+    }
     DBM_LAUNCH_CHECK();
     mark(4, s);
     if (upto <= 4) return DBM_OK;
     DBM_CUDA(cudaMemsetAsync(A.emask, 0, (size_t)ccap * 4, s));
-    k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
+    if constexpr (D == 2) {
+      if (tiled && use_tiles) k_gather_t<Q, P><<<ntiles, 256, sm_gather, s>>>(A, d_tiles, geo);
+      else k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
+    } else {
+      k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
+    }
     DBM_LAUNCH_CHECK();
     mark(5, s);
     if (upto <= 5) return DBM_OK;
@@ -994,6 +1167,8 @@ struct SimImpl : SimBase {
         }
         return DBM_OK;
       }
+      case DBM_TRACE_STATE_CELL: src = A.a.cell; sz = mcap * 4; break;
+      case DBM_TRACE_STATE_OFF: src = A.a.off; sz = (int64_t)D * mcap * sizeof(real); break;
       case DBM_TRACE_COUNTS: {
         sz = 8;
         if (needed) *needed = sz;
@@ -1105,6 +1280,17 @@ int dbm_sim_conservation(dbm_sim* s, double* out, void* stream) {
   SIM_CHECK(s);
   if (!out) return DBM_ERR_INVALID;
   return s->impl->conservation(out, (cudaStream_t)stream);
+}
+int dbm_sim_set_option(dbm_sim* s, int32_t option, int32_t value) {
+  SIM_CHECK(s);
+  if (option == DBM_OPT_GRAPHS) s->impl->use_graphs = value ? 1 : 0;
+  else if (option == DBM_OPT_TILES) s->impl->use_tiles = value ? 1 : 0;
+  else {
+    set_last_error("dbm_sim_set_option: unknown option %d", option);
+    return DBM_ERR_INVALID;
+  }
+  s->impl->invalidate_graphs();
+  return DBM_OK;
 }
 int dbm_sim_use_graphs(dbm_sim* s, int32_t on) {
   SIM_CHECK(s);

@@ -55,6 +55,7 @@ struct Args {
   int n_inst;
   uint32_t ncells;
   real R;          // r_res / cell
+  real R2;         // largest d2 with rn_sqrt(d2) <= R (so d2 <= R2 <=> rn_sqrt(d2) <= R)
   real tiny;       // window safety margin (cell units)
   int kappa_hard;
   real eps;
@@ -126,19 +127,39 @@ __device__ __forceinline__ bool cell_at(const InstK& I, int x, int y, int z, uin
   return true;
 }
 
-// e = (float(dS) + t) - p and |e| with round-to-nearest steps in a fixed order (the oracle's
-// canonical displacement; see oracle/grid_step.py).
+// The canonical displacement of a candidate from a reference point (the oracle's order, see
+// oracle/grid_step.py): per window cell  c = (float(dS) + cd) - p,  per candidate  e = off + c,
+// d2 = sum e*e, every step rounded to nearest with no contraction.  inside <=> sqrt(d2) <= R,
+// which is decided as d2 <= R2 with R2 the largest value whose rounded square root is <= R
+// (computed exactly on the host), so misses never pay for a square root.
+template <class T>
+__device__ __forceinline__ T canon_c(int dS, T cd, T p) {
+  return rn_sub(rn_add((T)dS, cd), p);
+}
 template <int D, class T>
-__device__ __forceinline__ T canon_dist(const int (&dS)[3], const T (&t)[3], const T (&p)[3], T (&q)[3]) {
+__device__ __forceinline__ T canon_d2(const T (&off)[3], const T (&c)[3], T (&e)[3]) {
   T s = 0;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    q[a] = rn_add((T)dS[a], t[a]);
-    T e = rn_sub(q[a], p[a]);
-    T e2 = rn_mul(e, e);
+    e[a] = rn_add(off[a], c[a]);
+    const T e2 = rn_mul(e[a], e[a]);
     s = a == 0 ? e2 : rn_add(s, e2);
   }
-  return rn_sqrt(s);
+  return s;
+}
+// Lower bound (rounded exactly like canon_d2) of d2 over all candidates of a window cell: every
+// offset lies in [0, 1), so e_a lies in [c_a, fl(c_a + 1)] and rounding is monotonic.
+template <int D, class T>
+__device__ __forceinline__ T cell_d2_lower(const T (&c)[3]) {
+  T s = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const T hi = rn_add(c[a], (T)1);
+    const T m = c[a] > (T)0 ? c[a] : (hi < (T)0 ? -hi : (T)0);
+    const T m2 = rn_mul(m, m);
+    s = a == 0 ? m2 : rn_add(s, m2);
+  }
+  return s;
 }
 
 template <class P>

@@ -65,6 +65,7 @@ class Simulation:
         eps: float = 1e-6,
         moment_capacity: int = 0,
         graphs: bool = True,
+        tiles: bool = True,
         device=None,
     ):
         self.device = _require_cuda(device)
@@ -101,7 +102,8 @@ class Simulation:
             _lib.check(self.lib.dbm_sim_create(ctypes.byref(desc), arr, len(self.instances), ctypes.byref(h)),
                        "dbm_sim_create")
         self._h = h
-        self.lib.dbm_sim_use_graphs(self._h, 1 if graphs else 0)
+        _lib.check(self.lib.dbm_sim_set_option(self._h, 1, 1 if graphs else 0), "dbm_sim_set_option")
+        _lib.check(self.lib.dbm_sim_set_option(self._h, 2, 1 if tiles else 0), "dbm_sim_set_option")
         self.iteration = 0
 
     # ---- lifecycle ------------------------------------------------------------------------------

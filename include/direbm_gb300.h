@@ -152,6 +152,11 @@ int dbm_sim_status(dbm_sim* sim, uint32_t* flags, int32_t clear, void* stream);
 int dbm_sim_conservation(dbm_sim* sim, double* d_out, void* stream);
 /* Graph capture on/off for dbm_sim_step (default on). */
 int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
+/* Execution options: DBM_OPT_GRAPHS (capture steps in CUDA graphs, default 1) and DBM_OPT_TILES
+ * (2D: shared-memory tiled window kernels, default 1; results are bit-identical either way). */
+#define DBM_OPT_GRAPHS 1
+#define DBM_OPT_TILES 2
+int dbm_sim_set_option(dbm_sim* sim, int32_t option, int32_t value);
 /* Run one step but stop after `stage` (1 collide, 2 thin+refine, 3 sort, 4 weights, 5 gather,
  * 6 emit) so intermediates can be exported with dbm_sim_trace. */
 int dbm_sim_step_partial(dbm_sim* sim, int32_t stage, void* stream);
@@ -171,11 +176,13 @@ int64_t dbm_sim_device_bytes(dbm_sim* sim);
 #define DBM_TRACE_FINAL_CELL 5 /* u32[ncells]   refined CP cell */
 #define DBM_TRACE_FINAL_OFF 6  /* real[D][ncells] refined CP offset */
 #define DBM_TRACE_SORTED 7     /* u32[2][P]     sorted (cell, origin cell) pairs */
-#define DBM_TRACE_SW 8         /* real[Q][Mcap] weight sums per component (FP32DEV: float) */
+#define DBM_TRACE_SW 8         /* real[Q][Mcap] 1/sw per component, 0 if dropped (FP32DEV: float) */
 #define DBM_TRACE_CPF 9        /* FP64: double[Q][cap]; FP32DEV: float[2][Q][cap] (hi, lo) */
 #define DBM_TRACE_EMPTY 10     /* u32[cap]      empty-direction mask per CP */
 #define DBM_TRACE_FSTAR 11     /* collided f of the input moments, layout of the state */
 #define DBM_TRACE_COUNTS 12    /* u32[2]: M (moments in), P (control points) */
+#define DBM_TRACE_STATE_CELL 13 /* u32[Mcap]    cell of each current moment */
+#define DBM_TRACE_STATE_OFF 14  /* real[D][Mcap] offsets of each current moment */
 
 #ifdef __cplusplus
 }

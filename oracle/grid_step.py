@@ -18,18 +18,24 @@ Step, in order (each line cites the reference function it follows):
   2. thin: one control point (CP) per occupied cell, at the centroid of the components landing
      there                                                         (propagation.py:130-153)
   3. refine: kappa = number of distinct directions among components within r (inclusive); keep the
-     CP if kappa <= kappa_hard, else move it to sum(e^f q)/sum(e^f)  (propagation.py:77-112)
+     CP if kappa <= kappa_hard, else move it to the exp(f)-weighted mean position, computed as
+     p + sum(e^f e)/sum(e^f) with e the component's displacement from p  (propagation.py:77-112)
   4. stable-sort the CPs by the cell of their refined position (the next step's moment order)
   5. per component: sw = sum over CPs within r of (r - d); dropped if sw <= 0 (propagation.py:156-178)
-  6. per CP and direction: f = sum over components within r of (r - d)/sw * f   (propagation.py:179-186)
+  6. per CP and direction: f = sum over components within r of (r - d)*(1/sw) * f (propagation.py:179-186)
   7. gap fill: directions with f < eps get (r / sum_{CPs within r, also empty}(r - d)) * f_rest;
      emptiness is judged on the pre-fill values; emit one moment per CP      (propagation.py:189-218)
 
-The radius test and every floor use one canonical operation order (no fused multiply-add):
-    t = off + cd ;  q = float(S - F) + t ;  e = q - p ;  d = sqrt(sum e*e) ;  inside = d <= R
-evaluated in the working precision (float64, or float32 for the FP32 store), so integer
-decisions are bit-identical to the CUDA kernels.  Sums are in float64 here; the CUDA FP64 path
-agrees to ~1e-15 relative, the FP32 path to its stated tolerance.
+The radius test uses one canonical operation order (each step rounded, no fused multiply-add),
+with dS the integer cell difference (component cell - reference cell), cd = c*dx/cell and p the
+reference point's offset in its cell:
+    c = (float(dS) + cd) - p ;  e = off + c ;  d2 = sum e*e ;  inside = sqrt(d2) <= R
+(c is shared by every candidate of one window cell, so a kernel pays one add per axis per
+candidate).  It is evaluated in the working precision (float64, or float32 for the FP32 store),
+so integer decisions are bit-identical to the CUDA kernels.  Sums are in float64 here unless
+the kernel's order is reproduced (thinning centroids and refine sums, see ordered_sums); the
+CUDA FP64 path then agrees bit for bit up to exp() rounding, the FP32 path to its stated
+tolerance.
 
 Parity pinning: stage 2 reduces to the reference tests' own numpy restatement of cell thinning
 (tests/test_warp_propagation.py:27-36) when all components of an unbounded domain are given, and
@@ -175,10 +181,11 @@ def to_world(spec: GridSpec, st: GridState):
 
 # ---- canonical distance ------------------------------------------------------------------------
 
-def disp(spec: GridSpec, dS, t, p):
-    """e = (float(dS) + t) - p in the working precision."""
+def disp(spec: GridSpec, dS, cd, p, off):
+    """e = off + ((float(dS) + cd) - p), each step rounded in the working precision."""
     dt = spec.dtype
-    return ((dS.astype(dt) + t.astype(dt)).astype(dt) - p.astype(dt)).astype(dt)
+    c = ((dS.astype(dt) + np.asarray(cd, dt)).astype(dt) - p.astype(dt)).astype(dt)
+    return (off.astype(dt) + c).astype(dt)
 
 
 def norm(spec: GridSpec, e):
@@ -261,7 +268,8 @@ def thin(spec: GridSpec, st: GridState):
 
 def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
     """(component, CP) pairs within R.  CPs are (global cell, offset), any number per cell.
-    Returns comp index into the (m,k) list, CP index, d, and q = float(S - G) + t (rel to CP cell)."""
+    Returns comp index into the (m,k) list, CP index, d, the displacement e of the component from
+    the CP (canonical order, see disp) and the integer cell difference dS = S - G."""
     if comps is None:
         comps = components(spec, st)
     m, k, b, S, t = comps
@@ -281,14 +289,13 @@ def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
         within = np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)
         pj = order[np.repeat(lo, cnt) + within]
         dS = -(fl[ci] + o)
-        q = (dS.astype(spec.dtype) + t[ci]).astype(spec.dtype)
-        e = (q - cp_off[pj].astype(spec.dtype)).astype(spec.dtype)
+        e = disp(spec, dS, spec.cd[k[ci]], cp_off[pj], st.off[m[ci]])
         d = norm(spec, e)
         keep = d <= spec.R
         ci_all.append(ci[keep])
         pj_all.append(pj[keep])
         d_all.append(d[keep])
-        q_all.append(q[keep])
+        q_all.append(e[keep])
         ds_all.append(dS[keep])
     if not ci_all:
         z = np.zeros(0, np.int64)
@@ -301,7 +308,7 @@ def refine(spec: GridSpec, st: GridState, fstar, cells, cen):
     """Stage 3.  Returns (mask, kappa, final global cell, final offset) per CP (thinning order)."""
     comps = components(spec, st)
     m, k, b, S, t = comps
-    ci, pj, d, q, dS = _pairs_comp_cp(spec, st, cells, cen, comps)
+    ci, pj, d, e, dS = _pairs_comp_cp(spec, st, cells, cen, comps)
     P = len(cells)
     mask = np.zeros(P, dtype=np.int64)
     np.bitwise_or.at(mask, pj, np.left_shift(1, k[ci]))
@@ -310,10 +317,11 @@ def refine(spec: GridSpec, st: GridState, fstar, cells, cen):
     # sums in the kernel's order: direction, window offset (z, y, x), moment
     keys = [k[ci]] + _so_keys(dS, spec.D) + [m[ci]]
     sw = ordered_sums(pj, keys, w, P)
-    sx = ordered_sums(pj, keys, w[:, None] * q.astype(np.float64), P)
+    sx = ordered_sums(pj, keys, w[:, None] * e.astype(np.float64), P)
     move = kappa > spec.kappa_hard
     npos = cen.astype(spec.dtype).copy()
-    npos[move] = (sx[move] / sw[move, None]).astype(spec.dtype)
+    step_ = (sx[move] / sw[move, None]).astype(spec.dtype)
+    npos[move] = (npos[move] + step_).astype(spec.dtype)
     shift = np.floor(npos).astype(np.int64)
     off = (npos - shift.astype(spec.dtype)).astype(spec.dtype)
     over = off >= spec.dtype(1.0)
@@ -349,7 +357,9 @@ def gather(spec: GridSpec, st: GridState, fstar, cp_cell, cp_off):
     live = sw[ci] > 0.0
     P = len(cp_cell)
     cp_f = np.zeros((P, spec.Q))
-    np.add.at(cp_f, (pj[live], k[ci[live]]), (wv[live] / sw[ci[live]]) * fstar[m[ci[live]], k[ci[live]]])
+    inv = np.zeros_like(sw)
+    np.divide(1.0, sw, out=inv, where=sw > 0.0)
+    np.add.at(cp_f, (pj[live], k[ci[live]]), (wv[live] * inv[ci[live]]) * fstar[m[ci[live]], k[ci[live]]])
     return cp_f, sw.reshape(-1, spec.Q)
 
 
@@ -372,7 +382,7 @@ def gapfill(spec: GridSpec, cp_cell, cp_off, cp_f):
         ai = np.repeat(np.arange(P), cnt)
         within = np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)
         cj = order[np.repeat(lo, cnt) + within]
-        e = disp(spec, np.broadcast_to(o, (len(ai), spec.D)), cp_off[cj], cp_off[ai])
+        e = disp(spec, np.broadcast_to(o, (len(ai), spec.D)), 0.0, cp_off[ai], cp_off[cj])
         d = norm(spec, e)
         keep = d <= spec.R
         a_all.append(ai[keep])
