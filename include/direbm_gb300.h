@@ -108,6 +108,15 @@ int dbm_resample_f32(const float* d_pos_c, const float* d_val_c, const int32_t* 
 int dbm_lbm_step(int precision, const void* d_src, void* d_dst, int32_t ni, int32_t nj, int32_t runs,
                  const double* d_tau, double rho0, int32_t steps, void* d_tmp, void* stream);
 
+/* ---- macroscopic fields --------------------------------------------------------------------
+ * Replaces direbm/fields.py:17-41 (bin_fields) on the device: bins n moments (x (n,2), f (n,Q)
+ * FP64) onto the grid of edge arrays ex (nex) x ey (ney) with numpy histogram2d's bin rule and
+ * writes per-bin mass and momentum, indexed [iy][ix].  Bins sum their moments in input order. */
+int64_t dbm_bin_fields_tmp_bytes(int64_t n);
+int dbm_bin_fields_f64(const double* d_x, const double* d_f, int64_t n, int lattice, const double* d_ex, int nex,
+                       const double* d_ey, int ney, double* d_mass, double* d_momx, double* d_momy, void* d_tmp,
+                       void* stream);
+
 /* ---- the fused DiReBM simulator -----------------------------------------------------------
  * Replaces direbm/warp/simulator.py:25-77 (GpuSimulator) and the pipeline it drives.  A handle
  * holds a batch of independent instances, each a box of `dims` cells of size `cell` (periodic or

@@ -150,3 +150,31 @@ def test_lbm_shear_wave_decay_matches_analytic(precision):
     lam = -np.log(a1 / a0) / steps
     lam_ref = np.array([olbm.shear_decay_rate(t, nj) for t in taus])
     np.testing.assert_allclose(lam, lam_ref, rtol=0.02)
+
+
+def test_bin_fields_on_device_matches_reference_golden(golden):
+    """direbm/fields.py:17-41 on the device: the reference's golden binning of 200 moments."""
+    from direbm_gb300.fields import bin_fields
+
+    g = golden("fields")
+    rho, u, ext = bin_fields(g["x"], g["f"], -3, 4, 1.0)
+    np.testing.assert_allclose(rho, g["rho"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(u, g["u"], rtol=1e-12, atol=1e-15)
+    assert ext == (-3, 4, -3, 4)
+
+
+def test_bin_fields_edges_and_empty_bins():
+    from direbm_gb300.fields import bin_fields
+    from oracle.fields import bin_fields as ref
+
+    rng = np.random.default_rng(7)
+    x = rng.uniform(-5, 5, size=(5000, 2))
+    x[:10] = [[-3.0, -3.0], [3.0, 3.0], [3.0, 0.0], [-3.0000001, 0.0], [2.9999999, 0.5]] * 2  # edges
+    f = rng.uniform(0.01, 0.3, size=(5000, 7))
+    for h in (0.5, 1.0, 0.7):
+        rg, ug, _ = bin_fields(x, f, -3, 3, h)
+        ro, uo, _ = ref(x, f, -3, 3, h)
+        np.testing.assert_allclose(rg, ro, rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(ug, uo, rtol=1e-12, atol=1e-15)
+    rg, _, _ = bin_fields(np.zeros((0, 2)), np.zeros((0, 7)), -3, 3, 1.0)
+    assert (rg == 0).all()
