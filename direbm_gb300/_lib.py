@@ -20,6 +20,21 @@ FP64, FP32DEV = 0, 1
 TRACE = {
     "occ": 1, "thin_cnt": 2, "centroid": 3, "mask": 4, "final_cell": 5, "final_off": 6,
     "sorted": 7, "sw": 8, "cpf": 9, "empty": 10, "fstar": 11, "counts": 12, "state_cell": 13, "state_off": 14,
+    "import_order": 15,
+}
+
+# Arrays of a recorded step (dbm_tape_export): name -> (id, dtype, shape kind).  Shape kinds: "M",
+# "QM" (Q, M), "DM" (D, M), "P", "DP", "P+1", "PQ+1", "nref", "Dnref", "nres", "Dnres", "ngap",
+# "Dngap", "I+1" (instances + 1).
+TAPE = {
+    "in_cell": (1, "u32", "M"), "in_off": (2, "f64", "DM"), "in_f": (3, "f64", "QM"), "fstar": (4, "f64", "QM"),
+    "thin_cell": (5, "u32", "QM"), "cp_thin": (6, "u32", "P"), "cp_count": (7, "u32", "P"),
+    "cp_cen": (8, "f64", "DP"), "cp_moved": (9, "u32", "P"), "out_cell": (10, "u32", "P"),
+    "out_off": (11, "f64", "DP"), "empty": (12, "u32", "P"), "inv_sw": (13, "f64", "QM"),
+    "ref_start": (14, "u32", "P+1"), "ref_item": (15, "u32", "nref"), "ref_e": (16, "f64", "Dnref"),
+    "res_start": (17, "u32", "PQ+1"), "res_item": (18, "u32", "nres"), "res_e": (19, "f64", "Dnres"),
+    "gap_start": (20, "u32", "P+1"), "gap_item": (21, "u32", "ngap"), "gap_bits": (22, "u32", "ngap"),
+    "gap_e": (23, "f64", "Dngap"), "inst_start": (24, "u32", "I+1"),
 }
 
 ST_OUT_OF_BOX, ST_CAPACITY, ST_NONFINITE, ST_BAD_INPUT = 1, 2, 4, 8
@@ -93,6 +108,17 @@ _SIGS = {
     "dbm_sim_set_option": (ctypes.c_int, [_vp, _i32, _i32]),
     "dbm_sim_trace": (ctypes.c_int, [_vp, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp]),
     "dbm_sim_device_bytes": (_i64, [_vp]),
+    "dbm_sim_set_tau": (ctypes.c_int, [_vp, _vp, _i32]),
+    "dbm_sim_snapshot": (ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp]),
+    "dbm_sim_restore": (ctypes.c_int, [_vp, _vp, _i64, _vp]),
+    "dbm_tape_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "dbm_tape_destroy": (ctypes.c_int, [_vp]),
+    "dbm_tape_clear": (ctypes.c_int, [_vp]),
+    "dbm_tape_step": (ctypes.c_int, [_vp, _vp]),
+    "dbm_tape_length": (_i32, [_vp]),
+    "dbm_tape_counts": (ctypes.c_int, [_vp, _i32, _vp]),
+    "dbm_tape_backward": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "dbm_tape_export": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp]),
 }
 
 EXPORTED = tuple(_SIGS)

@@ -1,0 +1,1166 @@
+// Reverse mode of the DiReBM step with its discrete structure held fixed.
+//
+// The reference has no derivative of its step (differentiation is future work in the reference,
+// idea.md:250); this file adds one for the fused step of sim.cu (itself a restatement of
+// direbm/warp/simulator.py:50-73 and direbm/warp/propagation.py:21-275).
+//
+// Held fixed per step (the "tape", recorded while the step runs): which components land in which
+// thinning cell, which control points (CPs) refine moved and the components within r of their
+// centroids, the CP sort order, the resampling pairs (component, CP) within r, the dropped
+// components, the gap-filled directions and the CP pairs of the gap fill.  With those fixed the
+// step is a smooth map of the input offsets x (cell units), the input f and tau:
+//   f*    = f + (feq(rho, u) - f) / tau                                   (collision)
+//   y_i   = x_m + cd_k                                                    (dispersion, i = (m, k))
+//   cen_t = mean of y_i over the components thinned into cell t
+//   p_t   = cen_t, or sum w_i y_i / sum w_i over its refine pairs, w_i = exp(f*_i)  (refine)
+//   sw_i  = sum over resample pairs (i, j) of (r - |y_i - p_j|)
+//   F_jk  = sum over resample pairs (i, j), k_i = k, of (r - |y_i - p_j|) / sw_i * f*_i
+//   F_jk  = r rho_rest W_k / sum over gap pairs (j, l) of (r - |p_l - p_j|)      (filled entries)
+// and the next state is (p_j, F_j).  dbm_tape_backward applies the transpose of its Jacobian,
+// pair by pair, in fixed order (no float atomics): every accumulation is owned by one thread,
+// scatters go through the lists' transposes (stable radix sort of each list by its item).
+// |y - p| has the subgradient 0 at zero distance.
+#include <algorithm>
+#include <vector>
+
+#include "sim.cuh"
+#include "sortscan.cuh"
+
+namespace dbm {
+
+constexpr uint32_t kNone = 0xffffffffu;
+
+// ---- device memory: a chunked bump allocator ----------------------------------------------------
+struct DevArena {
+  struct Chunk {
+    char* p;
+    size_t cap, used;
+  };
+  std::vector<Chunk> chunks;
+  size_t total = 0;
+  ~DevArena() {
+    for (auto& c : chunks) cudaFree(c.p);
+  }
+  void reset() {
+    for (auto& c : chunks) c.used = 0;
+  }
+  template <class T>
+  int get(T** out, int64_t n) {
+    const size_t b = (((size_t)std::max<int64_t>(n, 1) * sizeof(T)) + 255) & ~(size_t)255;
+    for (auto& c : chunks)
+      if (c.cap - c.used >= b) {
+        *out = (T*)(c.p + c.used);
+        c.used += b;
+        return DBM_OK;
+      }
+    const size_t cap = std::max<size_t>(b, (size_t)64 << 20);
+    void* p = nullptr;
+    DBM_CUDA(cudaMalloc(&p, cap));
+    chunks.push_back({(char*)p, cap, b});
+    total += cap;
+    *out = (T*)p;
+    return DBM_OK;
+  }
+};
+
+// ---- the recorded step ----------------------------------------------------------------------
+template <class real>
+struct PairCSR {
+  int64_t rows = 0, items = 0, n = 0;
+  uint32_t* start = nullptr;   // [rows + 1]
+  uint32_t* row = nullptr;     // [n] the CP of each pair
+  uint32_t* item = nullptr;    // [n] component m*Q + k (gap fill: the neighbour CP)
+  uint32_t* bits = nullptr;    // [n] gap fill only: directions empty in both CPs
+  real* e = nullptr;           // [D][n] displacement item - reference point, as the step computed it
+  uint32_t* tperm = nullptr;   // [n] pair indices ordered by item (stable)
+  uint32_t* tstart = nullptr;  // [items + 1]
+};
+
+template <class real>
+struct StepRec {
+  int64_t M = 0, P = 0;
+  uint32_t* in_cell = nullptr;    // [M]
+  real* in_off = nullptr;         // [D][M]
+  real* in_f = nullptr;           // FP64: f [Q][M]; FP32DEV: dev [Q][M]
+  float* in_rho = nullptr;        // FP32DEV: rho [M]
+  real* fs = nullptr;             // FP64: f* [Q][M]; FP32DEV: dev* [Q][M] (rho is unchanged)
+  uint32_t* thin_cell = nullptr;  // [Q][M]
+  real* inv_sw = nullptr;         // [Q][M]
+  uint32_t* inst_start = nullptr; // [n_inst + 1]
+  uint32_t* cp_thin = nullptr;    // [P]
+  uint32_t* cp_n = nullptr;       // [P]
+  uint32_t* cp_moved = nullptr;   // [P]
+  real* cp_cen = nullptr;         // [D][P]
+  uint32_t* out_cell = nullptr;   // [P]
+  real* out_off = nullptr;        // [D][P]
+  uint32_t* emask = nullptr;      // [P]
+  PairCSR<real> ref, res, gap;
+};
+
+// Everything a backward kernel reads, by value.
+template <int Q, int D, class P>
+struct RecK {
+  using real = typename P::real;
+  LatK<Q, D> L;
+  const InstK* inst;
+  const uint32_t* inst_base;
+  int n_inst;
+  real R;
+  StepRec<real> r;
+};
+
+template <int Q, int D, class P>
+__device__ __forceinline__ typename P::real rec_fstar(const RecK<Q, D, P>& K, int64_t m, int k) {
+  if constexpr (std::is_same<P, PF64>::value) return K.r.fs[(int64_t)k * K.r.M + m];
+  else return __fmaf_rn(K.r.in_rho[m], K.L.wf[k], K.r.fs[(int64_t)k * K.r.M + m]);
+}
+
+template <int D, class real>
+__device__ __forceinline__ real unit_of(const real* e, int64_t n, int64_t p, real (&u)[3]) {
+  real d2 = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    u[a] = e[(int64_t)a * n + p];
+    d2 += u[a] * u[a];
+  }
+  const real d = sqrt(d2);
+  const real inv = d > (real)0 ? (real)1 / d : (real)0;  // subgradient 0 at zero distance
+#pragma unroll
+  for (int a = 0; a < D; ++a) u[a] *= inv;
+  return d;
+}
+
+// ---- recording kernels (read the step's buffers through Args, see StepHook) --------------------
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_rec_thin_cell(const __grid_constant__ Args<Q, D, P> A, int64_t M,
+                                                       uint32_t* __restrict__ thin_cell) {
+  using real = typename P::real;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t g = A.a.cell[m];
+    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
+    int Sc[3];
+    decode_cell<D>(I, g, Sc);
+#pragma unroll 1
+    for (int k = 0; k < Q; ++k) {
+      int x[3] = {Sc[0], Sc[1], Sc[2]};
+#pragma unroll
+      for (int a = 0; a < D; ++a) x[a] += (int)floor(rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]));
+      uint32_t F;
+      thin_cell[(int64_t)k * M + m] = cell_at<D>(I, x[0], x[1], x[2], &F) ? F : kNone;
+    }
+  }
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_rec_cp(const __grid_constant__ Args<Q, D, P> A, StepRec<typename P::real> r) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < r.P; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t F = A.svals[j];
+    r.cp_thin[j] = F;
+    r.cp_n[j] = A.tcnt[F];
+    r.cp_moved[j] = __popc(A.mask[F]) > A.kappa_hard ? 1u : 0u;
+    r.out_cell[j] = A.b.cell[j];
+    r.emask[j] = A.emask[j];
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      r.cp_cen[(int64_t)a * r.P + j] = A.cen[(int64_t)a * A.ncells + F];
+      r.out_off[(int64_t)a * r.P + j] = A.b.off[(int64_t)a * A.ccap + j];
+    }
+  }
+}
+
+template <int Q, int D, class P>
+__global__ void k_rec_inst_start(const __grid_constant__ Args<Q, D, P> A, uint32_t* __restrict__ inst_start) {
+  for (int b = threadIdx.x; b <= A.n_inst; b += blockDim.x) inst_start[b] = A.a.start[A.inst_base[b]];
+}
+
+// Refine pairs of moved CP j: the components within r of its centroid, enumerated exactly as the
+// forward refine decides them (thin cell window, canonical displacement).  FILL = false writes the
+// count of row j into start[j]; FILL = true writes the pairs at start[j]...
+template <int Q, int D, class P, bool FILL>
+__global__ void __launch_bounds__(128) k_list_refine(const __grid_constant__ Args<Q, D, P> A,
+                                                     StepRec<typename P::real> r) {
+  using real = typename P::real;
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= r.P) return;
+  if (!r.cp_moved[j]) {
+    if (!FILL) r.ref.start[j] = 0;
+    return;
+  }
+  const uint32_t F = r.cp_thin[j];
+  const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, F)];
+  int Fc[3];
+  decode_cell<D>(I, F, Fc);
+  real cen[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) cen[a] = r.cp_cen[(int64_t)a * r.P + j];
+  uint32_t cnt = 0, pos = FILL ? r.ref.start[j] : 0u;
+#pragma unroll 1
+  for (int k = 0; k < Q; ++k) {
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    real cdk[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      cdk[a] = (real)A.L.cd[k][a];
+      const real base = cen[a] - cdk[a];
+      lo[a] = (int)floor(base - A.R - A.tiny);
+      hi[a] = (int)floor(base + A.R + A.tiny);
+    }
+#pragma unroll 1
+    for (int sz = lo[2]; sz <= hi[2]; ++sz)
+#pragma unroll 1
+      for (int sy = lo[1]; sy <= hi[1]; ++sy)
+#pragma unroll 1
+        for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+          const int dS[3] = {sx, sy, sz};
+          real c[3] = {0, 0, 0};
+#pragma unroll
+          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], cen[a]);
+          if (cell_d2_lower<D, real>(c) > A.R2) continue;
+          uint32_t Sg;
+          if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
+          const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
+          for (uint32_t m = m0; m < m1; ++m) {
+            real o[3] = {0, 0, 0}, e[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+            if (canon_d2<D, real>(o, c, e) <= A.R2) {
+              if (FILL) {
+                r.ref.row[pos] = (uint32_t)j;
+                r.ref.item[pos] = m * (uint32_t)Q + (uint32_t)k;
+#pragma unroll
+                for (int a = 0; a < D; ++a) r.ref.e[(int64_t)a * r.ref.n + pos] = e[a];
+                ++pos;
+              }
+              ++cnt;
+            }
+          }
+        }
+  }
+  if (!FILL) r.ref.start[j] = cnt;
+}
+
+// Resampling pairs of (CP j, direction k), row j*Q + k: the components of direction k within r of
+// the CP, as the forward gather (and, with the same arithmetic, the weights pass) decides them.
+template <int Q, int D, class P, bool FILL>
+__global__ void __launch_bounds__(256) k_list_resample(const __grid_constant__ Args<Q, D, P> A,
+                                                       StepRec<typename P::real> r) {
+  using real = typename P::real;
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (j >= r.P) return;
+  const int64_t rowid = j * Q + k;
+  const uint32_t G = A.b.cell[j];
+  const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
+  int Gc[3];
+  decode_cell<D>(I, G, Gc);
+  real p[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    p[a] = A.b.off[(int64_t)a * A.ccap + j];
+    cdk[a] = (real)A.L.cd[k][a];
+    const real base = p[a] - cdk[a];
+    lo[a] = (int)floor(base - A.R - A.tiny);
+    hi[a] = (int)floor(base + A.R + A.tiny);
+  }
+  uint32_t cnt = 0, pos = FILL ? r.res.start[rowid] : 0u;
+#pragma unroll 1
+  for (int sz = lo[2]; sz <= hi[2]; ++sz)
+#pragma unroll 1
+    for (int sy = lo[1]; sy <= hi[1]; ++sy)
+#pragma unroll 1
+      for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+        const int dS[3] = {sx, sy, sz};
+        real c[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], p[a]);
+        if (cell_d2_lower<D, real>(c) > A.R2) continue;
+        uint32_t Sg;
+        if (!cell_at<D>(I, Gc[0] + sx, Gc[1] + sy, Gc[2] + sz, &Sg)) continue;
+        const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
+        for (uint32_t m = m0; m < m1; ++m) {
+          real o[3] = {0, 0, 0}, e[3];
+#pragma unroll
+          for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+          if (canon_d2<D, real>(o, c, e) <= A.R2) {
+            if (FILL) {
+              r.res.row[pos] = (uint32_t)j;
+              r.res.item[pos] = m * (uint32_t)Q + (uint32_t)k;
+#pragma unroll
+              for (int a = 0; a < D; ++a) r.res.e[(int64_t)a * r.res.n + pos] = e[a];
+              ++pos;
+            }
+            ++cnt;
+          }
+        }
+      }
+  if (!FILL) r.res.start[rowid] = cnt;
+}
+
+// Gap-fill pairs of CP j: the CPs within r (from j's side, as the emit pass computes it) that share
+// an empty direction with j.
+template <int Q, int D, class P, bool FILL>
+__global__ void __launch_bounds__(256) k_list_gap(const __grid_constant__ Args<Q, D, P> A,
+                                                  StepRec<typename P::real> r) {
+  using real = typename P::real;
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= r.P) return;
+  const uint32_t em = A.emask[j];
+  if (!em) {
+    if (!FILL) r.gap.start[j] = 0;
+    return;
+  }
+  const uint32_t G = A.b.cell[j];
+  const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
+  int Gc[3];
+  decode_cell<D>(I, G, Gc);
+  real p[3] = {0, 0, 0};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    p[a] = A.b.off[(int64_t)a * A.ccap + j];
+    lo[a] = (int)floor(p[a] - A.R - A.tiny);
+    hi[a] = (int)floor(p[a] + A.R + A.tiny);
+  }
+  uint32_t cnt = 0, pos = FILL ? r.gap.start[j] : 0u;
+#pragma unroll 1
+  for (int gz = lo[2]; gz <= hi[2]; ++gz)
+#pragma unroll 1
+    for (int gy = lo[1]; gy <= hi[1]; ++gy)
+#pragma unroll 1
+      for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+        const int dS[3] = {gx, gy, gz};
+        real cc[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a) cc[a] = canon_c<real>(dS[a], (real)0, p[a]);
+        if (cell_d2_lower<D, real>(cc) > A.R2) continue;
+        uint32_t Hg;
+        if (!cell_at<D>(I, Gc[0] + gx, Gc[1] + gy, Gc[2] + gz, &Hg)) continue;
+        const uint32_t c0 = A.b.start[Hg], c1 = A.b.start[Hg + 1];
+        for (uint32_t c = c0; c < c1; ++c) {
+          const uint32_t both = A.emask[c] & em;
+          if (!both) continue;
+          real o[3] = {0, 0, 0}, e[3];
+#pragma unroll
+          for (int a = 0; a < D; ++a) o[a] = A.b.off[(int64_t)a * A.ccap + c];
+          if (canon_d2<D, real>(o, cc, e) <= A.R2) {
+            if (FILL) {
+              r.gap.row[pos] = (uint32_t)j;
+              r.gap.item[pos] = c;
+              r.gap.bits[pos] = both;
+#pragma unroll
+              for (int a = 0; a < D; ++a) r.gap.e[(int64_t)a * r.gap.n + pos] = e[a];
+              ++pos;
+            }
+            ++cnt;
+          }
+        }
+      }
+  if (!FILL) r.gap.start[j] = cnt;
+}
+
+__global__ void k_iota(uint32_t* __restrict__ v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = (uint32_t)i;
+}
+
+// start[c] = number of sorted keys < c, c in [0, items].
+__global__ void k_start_sorted(const uint32_t* __restrict__ keys, int64_t n, int64_t items, uint32_t* __restrict__ start) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= items; c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (keys[mid] < (uint32_t)c) lo = mid + 1; else hi = mid;
+    }
+    start[c] = (uint32_t)lo;
+  }
+}
+
+// ---- backward kernels ---------------------------------------------------------------------------
+
+// Output cotangents (row-major FP64) -> working layout [D][P], [Q][P].
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_in(const __grid_constant__ RecK<Q, D, P> K, const double* __restrict__ goff,
+                                                const double* __restrict__ gf, typename P::real* __restrict__ xbarP,
+                                                typename P::real* __restrict__ fbarG) {
+  using real = typename P::real;
+  const int64_t Pn = K.r.P;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] = (real)goff[j * D + a];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) fbarG[(int64_t)k * Pn + j] = (real)gf[j * Q + k];
+  }
+}
+
+// Gap fill, CP side: F_jk = r rho_rest W_k / s_jk for the filled entries.  d s_jk / d p_j = sum of
+// unit vectors u_jl (e = p_l - p_j); the neighbour's share (-u_jl) is left in cpair for k_bwd_gap_t.
+// Filled entries do not depend on the gather, so their cotangent is cleared for it.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_gap(const __grid_constant__ RecK<Q, D, P> K, typename P::real* __restrict__ xbarP,
+                                                 typename P::real* __restrict__ fbarG, typename P::real* __restrict__ cpair) {
+  using real = typename P::real;
+  const int64_t Pn = K.r.P;
+  const auto& L = K.r.gap;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t em = K.r.emask[j];
+    if (!em) continue;
+    const InstK I = K.inst[find_instance(K.inst_base, K.n_inst, K.r.out_cell[j])];
+    const uint32_t p0 = L.start[j], p1 = L.start[j + 1];
+    real s[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) s[k] = 0;
+    for (uint32_t p = p0; p < p1; ++p) {
+      real u[3];
+      const real w = K.R - unit_of<D, real>(L.e, L.n, p, u);
+      const uint32_t bits = L.bits[p];
+#pragma unroll
+      for (int k = 0; k < Q; ++k)
+        if ((bits >> k) & 1u) s[k] += w;
+    }
+    real sbar[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      sbar[k] = 0;
+      if (((em >> k) & 1u) && s[k] > (real)0) {
+        const real Fk = (K.R / s[k]) * (real)(I.rho_rest * K.L.w[k]);
+        sbar[k] = -fbarG[(int64_t)k * Pn + j] * Fk / s[k];
+        fbarG[(int64_t)k * Pn + j] = 0;
+      }
+    }
+    real xj[3] = {0, 0, 0};
+    for (uint32_t p = p0; p < p1; ++p) {
+      real u[3];
+      unit_of<D, real>(L.e, L.n, p, u);
+      const uint32_t bits = L.bits[p];
+      real c = 0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k)
+        if ((bits >> k) & 1u) c += sbar[k];
+      cpair[p] = c;
+#pragma unroll
+      for (int a = 0; a < D; ++a) xj[a] += c * u[a];
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] += xj[a];
+  }
+}
+
+// Gap fill, neighbour side: p_l receives -c u_jl from every pair (j, l).
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_gap_t(const __grid_constant__ RecK<Q, D, P> K, const typename P::real* __restrict__ cpair,
+                                                   typename P::real* __restrict__ xbarP) {
+  using real = typename P::real;
+  const int64_t Pn = K.r.P;
+  const auto& L = K.r.gap;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < Pn; l += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t q0 = L.tstart[l], q1 = L.tstart[l + 1];
+    if (q0 == q1) continue;
+    real xl[3] = {0, 0, 0};
+    for (uint32_t q = q0; q < q1; ++q) {
+      const uint32_t p = L.tperm[q];
+      real u[3];
+      unit_of<D, real>(L.e, L.n, p, u);
+      const real c = cpair[p];
+#pragma unroll
+      for (int a = 0; a < D; ++a) xl[a] -= c * u[a];
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + l] += xl[a];
+  }
+}
+
+// Gather + weights, component side (one thread per input moment, all its directions):
+//   G_i = sum_j a_ij Fbar_jk,  a_ij = (r - d_ij)/sw_i           -> f*bar_i
+//   wbar_ij = f*_i / sw_i (Fbar_jk - G_i)   (cotangent of r - d_ij through F and sw)
+//   ybar_i -= sum_j wbar_ij u_ij;  wbar is kept per pair for the CP side.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK<Q, D, P> K,
+                                                    const typename P::real* __restrict__ fbarG,
+                                                    typename P::real* __restrict__ fsbar, typename P::real* __restrict__ xbarM,
+                                                    typename P::real* __restrict__ wbar) {
+  using real = typename P::real;
+  const int64_t M = K.r.M, Pn = K.r.P;
+  const auto& L = K.r.res;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+    real xm[3] = {0, 0, 0};
+#pragma unroll 1
+    for (int k = 0; k < Q; ++k) {
+      const int64_t i = m * Q + k;
+      const real inv = K.r.inv_sw[(int64_t)k * M + m];
+      const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
+      real G = 0;
+      if (inv > (real)0) {
+        for (uint32_t q = q0; q < q1; ++q) {
+          const uint32_t p = L.tperm[q];
+          real u[3];
+          const real d = unit_of<D, real>(L.e, L.n, p, u);
+          G += (K.R - d) * inv * fbarG[(int64_t)k * Pn + L.row[p]];
+        }
+      }
+      fsbar[(int64_t)k * M + m] = G;
+      const real fsi = rec_fstar<Q, D, P>(K, m, k) * inv;
+      for (uint32_t q = q0; q < q1; ++q) {
+        const uint32_t p = L.tperm[q];
+        real u[3];
+        unit_of<D, real>(L.e, L.n, p, u);
+        const real wb = inv > (real)0 ? fsi * (fbarG[(int64_t)k * Pn + L.row[p]] - G) : (real)0;
+        wbar[p] = wb;
+#pragma unroll
+        for (int a = 0; a < D; ++a) xm[a] -= wb * u[a];
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) xbarM[(int64_t)a * M + m] = xm[a];
+  }
+}
+
+// Gather + weights, CP side: p_j receives +wbar_ij u_ij from each of its pairs.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_gather_cp(const __grid_constant__ RecK<Q, D, P> K,
+                                                       const typename P::real* __restrict__ wbar,
+                                                       typename P::real* __restrict__ xbarP) {
+  using real = typename P::real;
+  const int64_t Pn = K.r.P;
+  const auto& L = K.r.res;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t p0 = L.start[j * Q], p1 = L.start[(j + 1) * Q];
+    real xj[3] = {0, 0, 0};
+    for (uint32_t p = p0; p < p1; ++p) {
+      real u[3];
+      unit_of<D, real>(L.e, L.n, p, u);
+      const real wb = wbar[p];
+#pragma unroll
+      for (int a = 0; a < D; ++a) xj[a] += wb * u[a];
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] += xj[a];
+  }
+}
+
+// Refine, CP side.  A moved CP is p = sum w_i y_i / W (its centroid cancels): keep W and the move
+// s = sum w_i e_i / W for the component side.  An unmoved CP is its centroid: its cotangent goes to
+// the thin cell (already divided by the component count).
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_refine_cp(const __grid_constant__ RecK<Q, D, P> K,
+                                                       const typename P::real* __restrict__ xbarP,
+                                                       typename P::real* __restrict__ Wj, typename P::real* __restrict__ sj,
+                                                       typename P::real* __restrict__ cenbar, int64_t ncells) {
+  using real = typename P::real;
+  const int64_t Pn = K.r.P;
+  const auto& L = K.r.ref;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
+    if (K.r.cp_moved[j]) {
+      real W = 0, sx[3] = {0, 0, 0};
+      for (uint32_t p = L.start[j]; p < L.start[j + 1]; ++p) {
+        const uint32_t i = L.item[p];
+        const real w = exp(rec_fstar<Q, D, P>(K, i / Q, (int)(i % Q)));
+        W += w;
+#pragma unroll
+        for (int a = 0; a < D; ++a) sx[a] += w * L.e[(int64_t)a * L.n + p];
+      }
+      Wj[j] = W;
+#pragma unroll
+      for (int a = 0; a < D; ++a) sj[(int64_t)a * Pn + j] = W > (real)0 ? sx[a] / W : (real)0;
+    } else {
+      const uint32_t F = K.r.cp_thin[j];
+      const real invn = (real)1 / (real)K.r.cp_n[j];
+#pragma unroll
+      for (int a = 0; a < D; ++a) cenbar[(int64_t)a * ncells + F] = xbarP[(int64_t)a * Pn + j] * invn;
+    }
+  }
+}
+
+// Component side of refine and thinning, the dispersion sum over directions, and the collision:
+//   ybar_i += w_i/W_j pbar_j,  f*bar_i += w_i ((e_i - s_j) . pbar_j)/W_j   (refine pairs of i)
+//   ybar_i += cenbar[thin cell of i]                                        (thinning)
+//   xbar_m  = sum_k ybar_(m,k)                                              (y = x + cd_k)
+//   fbar    = (1 - 1/tau) f*bar + (1/tau) J_feq^T f*bar,  taubar_m = -(1/tau^2) f*bar . (feq - f)
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_moment(const __grid_constant__ RecK<Q, D, P> K,
+                                                    const typename P::real* __restrict__ fsbar,
+                                                    const typename P::real* __restrict__ xbarM,
+                                                    const typename P::real* __restrict__ xbarP,
+                                                    const typename P::real* __restrict__ Wj, const typename P::real* __restrict__ sj,
+                                                    const typename P::real* __restrict__ cenbar, int64_t ncells,
+                                                    double* __restrict__ goff_in, double* __restrict__ gf_in,
+                                                    double* __restrict__ taupart) {
+  using real = typename P::real;
+  const int64_t M = K.r.M, Pn = K.r.P;
+  const auto& L = K.r.ref;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+    real x[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) x[a] = xbarM[(int64_t)a * M + m];
+    real g[Q];
+#pragma unroll 1
+    for (int k = 0; k < Q; ++k) {
+      const int64_t i = m * Q + k;
+      real gk = fsbar[(int64_t)k * M + m];
+      const uint32_t F = K.r.thin_cell[(int64_t)k * M + m];
+      if (F != kNone) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) x[a] += cenbar[(int64_t)a * ncells + F];
+      }
+      const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
+      if (q0 < q1) {
+        const real w = exp(rec_fstar<Q, D, P>(K, m, k));
+        for (uint32_t q = q0; q < q1; ++q) {
+          const uint32_t p = L.tperm[q];
+          const uint32_t j = L.row[p];
+          const real wW = w / Wj[j];
+          real dot = 0;
+#pragma unroll
+          for (int a = 0; a < D; ++a) {
+            const real pb = xbarP[(int64_t)a * Pn + j];
+            x[a] += wW * pb;
+            dot += (L.e[(int64_t)a * L.n + p] - sj[(int64_t)a * Pn + j]) * pb;
+          }
+          gk += wW * dot;
+        }
+      }
+      g[k] = gk;
+    }
+    // collision
+    const InstK I = K.inst[find_instance(K.inst_base, K.n_inst, K.r.in_cell[m])];
+    const real tau = (real)I.tau, itau = (real)1 / tau;
+    const real inv = (real)K.L.inv_cs2;
+    real rho, u[D], fmfeq[Q], feqw[Q];  // fmfeq = feq - f;  feqw = feq / rho
+    if constexpr (std::is_same<P, PF64>::value) {
+      real f[Q], mom[D];
+      rho = 0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) mom[a] = 0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        f[k] = K.r.in_f[(int64_t)k * M + m];
+        rho += f[k];
+#pragma unroll
+        for (int a = 0; a < D; ++a) mom[a] += f[k] * K.L.c[k][a];
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a) u[a] = mom[a] / rho;
+      real feq[Q];
+      equilibrium_all<Q, D, real>(rho, u, K.L, feq);
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        fmfeq[k] = feq[k] - f[k];
+        feqw[k] = feq[k] / rho;
+      }
+    } else {
+      float dv[Q], mom[D];
+      rho = K.r.in_rho[m];
+#pragma unroll
+      for (int a = 0; a < D; ++a) mom[a] = 0.f;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        dv[k] = K.r.in_f[(int64_t)k * M + m];
+#pragma unroll
+        for (int a = 0; a < D; ++a) mom[a] += dv[k] * K.L.cf[k][a];
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a) u[a] = mom[a] / rho;
+      float deq[Q];
+      eq_deviation_f32<Q, D>(rho, u, K.L, deq);
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        fmfeq[k] = deq[k] - dv[k];
+        feqw[k] = K.L.wf[k] + deq[k] / rho;
+      }
+    }
+    real phi = 0, h[D], tb = 0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) h[a] = 0;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      phi += g[k] * feqw[k];
+      tb += g[k] * fmfeq[k];
+      real cu = 0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) cu += (real)K.L.c[k][a] * u[a];
+      const real gw = g[k] * (real)K.L.w[k] * inv;
+#pragma unroll
+      for (int a = 0; a < D; ++a) h[a] += gw * ((real)K.L.c[k][a] * ((real)1 + inv * cu) - u[a]);
+    }
+    real hu = 0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) hu += h[a] * u[a];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      real hc = 0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) hc += h[a] * (real)K.L.c[q][a];
+      gf_in[m * Q + q] = (double)(((real)1 - itau) * g[q] + itau * (phi + hc - hu));
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) goff_in[m * D + a] = (double)x[a];
+    taupart[m] = -(double)tb * (double)itau * (double)itau;
+  }
+}
+
+// Per-instance sum of the tau partials in a fixed order (strided per thread, then a tree).
+__global__ void __launch_bounds__(256) k_bwd_tau(const uint32_t* __restrict__ inst_start, const double* __restrict__ part,
+                                                 double* __restrict__ gtau) {
+  __shared__ double sh[256];
+  const int b = blockIdx.x;
+  const uint32_t m0 = inst_start[b], m1 = inst_start[b + 1];
+  double s = 0;
+  for (uint32_t m = m0 + threadIdx.x; m < m1; m += blockDim.x) s += part[m];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) gtau[b] += sh[0];
+}
+
+// Export helpers: real -> double, FP32DEV f -> rho*W + dev.
+template <class real>
+__global__ void k_to_f64(const real* __restrict__ src, int64_t n, double* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+template <int Q>
+__global__ void k_dev_to_f64(const float* __restrict__ rho, const float* __restrict__ dev, const double* __restrict__ w, int64_t M,
+                             double* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)Q * M; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = i / M, m = i - k * M;
+    dst[i] = (double)rho[m] * w[k] + (double)dev[i];
+  }
+}
+
+// ---- the tape ------------------------------------------------------------------------------
+
+struct TapeBase {
+  virtual ~TapeBase() = default;
+  virtual int clear() = 0;
+  virtual int step(cudaStream_t) = 0;
+  virtual int length() const = 0;
+  virtual int counts(int, int64_t*) const = 0;
+  virtual int backward(int, const double*, const double*, double*, double*, double*, cudaStream_t) = 0;
+  virtual int export_(int, int, void*, int64_t, int64_t*, cudaStream_t) = 0;
+};
+
+inline unsigned grid_for(int64_t n, int threads = 256) {
+  return std::max(1u, std::min<unsigned>(div_up(std::max<int64_t>(n, 1), threads), (unsigned)sm_count() * 16));
+}
+
+template <int Q, int D, class P>
+struct TapeImpl : TapeBase, StepHook {
+  using real = typename P::real;
+  SimBase* sim;
+  std::vector<StepRec<real>> steps;
+  DevArena rec_mem, tmp_mem, bwd_mem;
+  StepRec<real> cur{};
+  LatK<Q, D> L{};
+  const InstK* inst = nullptr;
+  const uint32_t* inst_base = nullptr;
+  int n_inst = 0;
+  real R = 0;
+  int64_t ncells = 0;
+  double* wk = nullptr;  // W_k in FP64 (export of FP32DEV f)
+  cudaEvent_t done = nullptr;
+
+  explicit TapeImpl(SimBase* s) : sim(s) {}
+  ~TapeImpl() override {
+    if (done) cudaEventDestroy(done);
+  }
+
+  int init() {
+    DBM_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    DBM_TRY(rec_mem.get(&wk, Q));
+    return DBM_OK;
+  }
+
+  int clear() override {
+    steps.clear();
+    rec_mem.reset();
+    wk = nullptr;
+    DBM_TRY(rec_mem.get(&wk, Q));
+    return DBM_OK;
+  }
+  int length() const override { return (int)steps.size(); }
+  int counts(int i, int64_t* c) const override {
+    if (i < 0 || i >= (int)steps.size()) { set_last_error("tape: no step %d", i); return DBM_ERR_INVALID; }
+    const auto& r = steps[i];
+    c[0] = r.M; c[1] = r.P; c[2] = r.ref.n; c[3] = r.res.n; c[4] = r.gap.n; c[5] = 0; c[6] = 0; c[7] = 0;
+    return DBM_OK;
+  }
+
+  int step(cudaStream_t s) override {
+    cur = StepRec<real>{};
+    DBM_TRY(sim->step_hooked(this, s));
+    steps.push_back(cur);
+    DBM_CUDA(cudaStreamSynchronize(s));
+    return DBM_OK;
+  }
+
+  static uint32_t read_u32(const uint32_t* d, cudaStream_t s, int* rc) {
+    uint32_t h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      set_last_error("tape: %s", cudaGetErrorString(e));
+      *rc = DBM_ERR_CUDA;
+    }
+    return h;
+  }
+
+  int before(const void* av, cudaStream_t s) override {
+    const Args<Q, D, P>& A = *(const Args<Q, D, P>*)av;
+    L = A.L;
+    inst = A.inst;
+    inst_base = A.inst_base;
+    n_inst = A.n_inst;
+    R = A.R;
+    ncells = A.ncells;
+    if (wk) DBM_CUDA(cudaMemcpyAsync(wk, L.w, sizeof(double) * Q, cudaMemcpyHostToDevice, s));
+    int rc = DBM_OK;
+    const uint32_t M = read_u32(A.a.count, s, &rc);
+    DBM_TRY(rc);
+    StepRec<real>& r = cur;
+    r.M = M;
+    DBM_TRY(rec_mem.get(&r.in_cell, M));
+    DBM_TRY(rec_mem.get(&r.in_off, (int64_t)D * M));
+    DBM_TRY(rec_mem.get(&r.in_f, (int64_t)Q * M));
+    DBM_TRY(rec_mem.get(&r.fs, (int64_t)Q * M));
+    DBM_TRY(rec_mem.get(&r.thin_cell, (int64_t)Q * M));
+    DBM_TRY(rec_mem.get(&r.inv_sw, (int64_t)Q * M));
+    DBM_TRY(rec_mem.get(&r.inst_start, n_inst + 1));
+    if (M == 0) return DBM_OK;
+    DBM_CUDA(cudaMemcpyAsync(r.in_cell, A.a.cell, (size_t)M * 4, cudaMemcpyDeviceToDevice, s));
+    DBM_CUDA(cudaMemcpy2DAsync(r.in_off, (size_t)M * sizeof(real), A.a.off, (size_t)A.mcap * sizeof(real),
+                               (size_t)M * sizeof(real), D, cudaMemcpyDeviceToDevice, s));
+    if constexpr (std::is_same<P, PF64>::value) {
+      DBM_CUDA(cudaMemcpy2DAsync(r.in_f, (size_t)M * 8, A.a.f64, (size_t)A.mcap * 8, (size_t)M * 8, Q,
+                                 cudaMemcpyDeviceToDevice, s));
+    } else {
+      DBM_TRY(rec_mem.get(&r.in_rho, M));
+      DBM_CUDA(cudaMemcpyAsync(r.in_rho, A.a.rho, (size_t)M * 4, cudaMemcpyDeviceToDevice, s));
+      DBM_CUDA(cudaMemcpy2DAsync(r.in_f, (size_t)M * 4, A.a.dev, (size_t)A.mcap * 4, (size_t)M * 4, Q,
+                                 cudaMemcpyDeviceToDevice, s));
+    }
+    return DBM_OK;
+  }
+
+  // Count, scan and fill one pair list, then build its transpose.
+  template <class Count, class Fill>
+  int build_list(PairCSR<real>& Lst, int64_t rows, int64_t items, bool with_bits, Count&& count, Fill&& fill,
+                 cudaStream_t s) {
+    Lst.rows = rows;
+    Lst.items = items;
+    DBM_TRY(rec_mem.get(&Lst.start, rows + 1));
+    DBM_CUDA(cudaMemsetAsync(Lst.start + rows, 0, 4, s));
+    DBM_TRY(count());
+    void* stmp;
+    DBM_TRY(tmp_mem.get((char**)&stmp, (int64_t)scan_tmp_bytes(rows + 1)));
+    DBM_TRY(scan_exclusive_u32(Lst.start, Lst.start, rows + 1, nullptr, nullptr, stmp, s));
+    int rc = DBM_OK;
+    const uint32_t n = read_u32(Lst.start + rows, s, &rc);
+    DBM_TRY(rc);
+    Lst.n = n;
+    DBM_TRY(rec_mem.get(&Lst.row, n));
+    DBM_TRY(rec_mem.get(&Lst.item, n));
+    DBM_TRY(rec_mem.get(&Lst.e, (int64_t)D * n));
+    if (with_bits) DBM_TRY(rec_mem.get(&Lst.bits, n));
+    DBM_TRY(rec_mem.get(&Lst.tperm, n));
+    DBM_TRY(rec_mem.get(&Lst.tstart, items + 1));
+    if (n > 0) DBM_TRY(fill());
+    // transpose: stable sort of (item, pair index)
+    uint32_t *k0, *v0, *k1, *v1;
+    DBM_TRY(tmp_mem.get(&k0, n));
+    DBM_TRY(tmp_mem.get(&v0, n));
+    DBM_TRY(tmp_mem.get(&k1, n));
+    DBM_TRY(tmp_mem.get(&v1, n));
+    char* rtmp;
+    DBM_TRY(tmp_mem.get(&rtmp, (int64_t)radix_tmp_bytes(std::max<int64_t>(n, 1))));
+    const uint32_t* ks = k0;
+    const uint32_t* vs = v0;
+    if (n > 0) {
+      DBM_CUDA(cudaMemcpyAsync(k0, Lst.item, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+      k_iota<<<grid_for(n), 256, 0, s>>>(v0, n);
+      DBM_LAUNCH_CHECK();
+      int bits = 1;
+      while (bits < 32 && ((int64_t)1 << bits) <= items) ++bits;
+      bool alt = false;
+      DBM_TRY(radix_sort_pairs<uint32_t>(k0, v0, k1, v1, n, nullptr, bits, rtmp, s, &alt));
+      ks = alt ? k1 : k0;
+      vs = alt ? v1 : v0;
+      DBM_CUDA(cudaMemcpyAsync(Lst.tperm, vs, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    k_start_sorted<<<grid_for(items + 1), 256, 0, s>>>(ks, n, items, Lst.tstart);
+    DBM_LAUNCH_CHECK();
+    return DBM_OK;
+  }
+
+  int after(const void* av, cudaStream_t s) override {
+    const Args<Q, D, P>& A = *(const Args<Q, D, P>*)av;
+    StepRec<real>& r = cur;
+    tmp_mem.reset();
+    int rc = DBM_OK;
+    const uint32_t st = read_u32(A.status, s, &rc);
+    DBM_TRY(rc);
+    if (st & ST_NONFINITE) {
+      set_last_error("tape: the step produced a non-finite refine move; it has no derivative");
+      return DBM_ERR_INVALID;
+    }
+    r.P = read_u32(A.d_P, s, &rc);
+    DBM_TRY(rc);
+    const int64_t M = r.M, Pn = r.P;
+    if (M > 0) {
+      if constexpr (std::is_same<P, PF64>::value) {
+        DBM_CUDA(cudaMemcpy2DAsync(r.fs, (size_t)M * 8, A.a.f64, (size_t)A.mcap * 8, (size_t)M * 8, Q,
+                                   cudaMemcpyDeviceToDevice, s));
+      } else {
+        DBM_CUDA(cudaMemcpy2DAsync(r.fs, (size_t)M * 4, A.a.dev, (size_t)A.mcap * 4, (size_t)M * 4, Q,
+                                   cudaMemcpyDeviceToDevice, s));
+      }
+      DBM_CUDA(cudaMemcpy2DAsync(r.inv_sw, (size_t)M * sizeof(real), A.sw, (size_t)A.mcap * sizeof(real),
+                                 (size_t)M * sizeof(real), Q, cudaMemcpyDeviceToDevice, s));
+      k_rec_thin_cell<Q, D, P><<<grid_for(M), 256, 0, s>>>(A, M, r.thin_cell);
+      DBM_LAUNCH_CHECK();
+    }
+    k_rec_inst_start<Q, D, P><<<1, 256, 0, s>>>(A, r.inst_start);
+    DBM_LAUNCH_CHECK();
+    DBM_TRY(rec_mem.get(&r.cp_thin, Pn));
+    DBM_TRY(rec_mem.get(&r.cp_n, Pn));
+    DBM_TRY(rec_mem.get(&r.cp_moved, Pn));
+    DBM_TRY(rec_mem.get(&r.cp_cen, (int64_t)D * Pn));
+    DBM_TRY(rec_mem.get(&r.out_cell, Pn));
+    DBM_TRY(rec_mem.get(&r.out_off, (int64_t)D * Pn));
+    DBM_TRY(rec_mem.get(&r.emask, Pn));
+    if (Pn > 0) {
+      k_rec_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(A, r);
+      DBM_LAUNCH_CHECK();
+    }
+    const unsigned gp = div_up(std::max<int64_t>(Pn, 1), 128);
+    // refine pairs (rows: CPs)
+    DBM_TRY(build_list(r.ref, Pn, (int64_t)Q * M, false,
+                       [&]() -> int {
+                         if (Pn > 0) { k_list_refine<Q, D, P, false><<<gp, 128, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
+                         return DBM_OK;
+                       },
+                       [&]() -> int {
+                         k_list_refine<Q, D, P, true><<<gp, 128, 0, s>>>(A, r);
+                         DBM_LAUNCH_CHECK();
+                         return DBM_OK;
+                       },
+                       s));
+    // resampling pairs (rows: CP x direction)
+    const dim3 gr(div_up(std::max<int64_t>(Pn, 1), 256), Q);
+    DBM_TRY(build_list(r.res, Pn * Q, (int64_t)Q * M, false,
+                       [&]() -> int {
+                         if (Pn > 0) { k_list_resample<Q, D, P, false><<<gr, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
+                         return DBM_OK;
+                       },
+                       [&]() -> int {
+                         k_list_resample<Q, D, P, true><<<gr, 256, 0, s>>>(A, r);
+                         DBM_LAUNCH_CHECK();
+                         return DBM_OK;
+                       },
+                       s));
+    // gap-fill pairs (rows: CPs, items: CPs)
+    const unsigned gg = div_up(std::max<int64_t>(Pn, 1), 256);
+    DBM_TRY(build_list(r.gap, Pn, Pn, true,
+                       [&]() -> int {
+                         if (Pn > 0) { k_list_gap<Q, D, P, false><<<gg, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
+                         return DBM_OK;
+                       },
+                       [&]() -> int {
+                         k_list_gap<Q, D, P, true><<<gg, 256, 0, s>>>(A, r);
+                         DBM_LAUNCH_CHECK();
+                         return DBM_OK;
+                       },
+                       s));
+    return DBM_OK;
+  }
+
+  RecK<Q, D, P> reck(const StepRec<real>& r) const {
+    RecK<Q, D, P> K;
+    K.L = L;
+    K.inst = inst;
+    K.inst_base = inst_base;
+    K.n_inst = n_inst;
+    K.R = R;
+    K.r = r;
+    return K;
+  }
+
+  int backward(int idx, const double* goff_out, const double* gf_out, double* goff_in, double* gf_in, double* gtau,
+               cudaStream_t s) override {
+    if (idx < 0 || idx >= (int)steps.size()) { set_last_error("tape: no step %d", idx); return DBM_ERR_INVALID; }
+    const StepRec<real>& r = steps[idx];
+    const int64_t M = r.M, Pn = r.P;
+    if ((Pn > 0 && (!goff_out || !gf_out)) || (M > 0 && (!goff_in || !gf_in)) || !gtau) {
+      set_last_error("tape backward: null cotangent");
+      return DBM_ERR_INVALID;
+    }
+    DBM_CUDA(cudaStreamWaitEvent(s, done, 0));  // the previous call's scratch is free
+    bwd_mem.reset();
+    real *xbarP, *fbarG, *cpair, *fsbar, *xbarM, *wbar, *Wj, *sj, *cenbar;
+    double* taupart;
+    DBM_TRY(bwd_mem.get(&xbarP, (int64_t)D * Pn));
+    DBM_TRY(bwd_mem.get(&fbarG, (int64_t)Q * Pn));
+    DBM_TRY(bwd_mem.get(&cpair, r.gap.n));
+    DBM_TRY(bwd_mem.get(&fsbar, (int64_t)Q * M));
+    DBM_TRY(bwd_mem.get(&xbarM, (int64_t)D * M));
+    DBM_TRY(bwd_mem.get(&wbar, r.res.n));
+    DBM_TRY(bwd_mem.get(&Wj, Pn));
+    DBM_TRY(bwd_mem.get(&sj, (int64_t)D * Pn));
+    DBM_TRY(bwd_mem.get(&cenbar, (int64_t)D * ncells));
+    DBM_TRY(bwd_mem.get(&taupart, M));
+    const RecK<Q, D, P> K = reck(r);
+    DBM_CUDA(cudaMemsetAsync(cenbar, 0, sizeof(real) * (size_t)D * ncells, s));
+    if (Pn > 0) {
+      k_bwd_in<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, goff_out, gf_out, xbarP, fbarG);
+      DBM_LAUNCH_CHECK();
+      if (r.gap.n > 0) {
+        k_bwd_gap<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xbarP, fbarG, cpair);
+        DBM_LAUNCH_CHECK();
+        k_bwd_gap_t<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, cpair, xbarP);
+        DBM_LAUNCH_CHECK();
+      }
+    }
+    if (M > 0) {
+      k_bwd_gather<Q, D, P><<<grid_for(M), 256, 0, s>>>(K, fbarG, fsbar, xbarM, wbar);
+      DBM_LAUNCH_CHECK();
+    }
+    if (Pn > 0) {
+      k_bwd_gather_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, wbar, xbarP);
+      DBM_LAUNCH_CHECK();
+      k_bwd_refine_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xbarP, Wj, sj, cenbar, ncells);
+      DBM_LAUNCH_CHECK();
+    }
+    if (M > 0) {
+      k_bwd_moment<Q, D, P><<<grid_for(M), 256, 0, s>>>(K, fsbar, xbarM, xbarP, Wj, sj, cenbar, ncells, goff_in, gf_in,
+                                                        taupart);
+      DBM_LAUNCH_CHECK();
+      k_bwd_tau<<<n_inst, 256, 0, s>>>(r.inst_start, taupart, gtau);
+      DBM_LAUNCH_CHECK();
+    }
+    DBM_CUDA(cudaEventRecord(done, s));
+    return DBM_OK;
+  }
+
+  int export_(int idx, int what, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) override {
+    if (idx < 0 || idx >= (int)steps.size()) { set_last_error("tape: no step %d", idx); return DBM_ERR_INVALID; }
+    const StepRec<real>& r = steps[idx];
+    const void* src = nullptr;
+    int64_t n = 0;
+    bool conv = false;  // real -> f64
+    switch (what) {
+      case DBM_TAPE_IN_CELL: src = r.in_cell; n = r.M; break;
+      case DBM_TAPE_IN_OFF: src = r.in_off; n = (int64_t)D * r.M; conv = true; break;
+      case DBM_TAPE_IN_F:
+      case DBM_TAPE_FSTAR: src = what == DBM_TAPE_IN_F ? r.in_f : r.fs; n = (int64_t)Q * r.M; conv = true; break;
+      case DBM_TAPE_THIN_CELL: src = r.thin_cell; n = (int64_t)Q * r.M; break;
+      case DBM_TAPE_CP_THIN: src = r.cp_thin; n = r.P; break;
+      case DBM_TAPE_CP_COUNT: src = r.cp_n; n = r.P; break;
+      case DBM_TAPE_CP_CEN: src = r.cp_cen; n = (int64_t)D * r.P; conv = true; break;
+      case DBM_TAPE_CP_MOVED: src = r.cp_moved; n = r.P; break;
+      case DBM_TAPE_OUT_CELL: src = r.out_cell; n = r.P; break;
+      case DBM_TAPE_OUT_OFF: src = r.out_off; n = (int64_t)D * r.P; conv = true; break;
+      case DBM_TAPE_EMPTY: src = r.emask; n = r.P; break;
+      case DBM_TAPE_INV_SW: src = r.inv_sw; n = (int64_t)Q * r.M; conv = true; break;
+      case DBM_TAPE_REFINE_START: src = r.ref.start; n = r.P + 1; break;
+      case DBM_TAPE_REFINE_ITEM: src = r.ref.item; n = r.ref.n; break;
+      case DBM_TAPE_REFINE_E: src = r.ref.e; n = (int64_t)D * r.ref.n; conv = true; break;
+      case DBM_TAPE_RES_START: src = r.res.start; n = r.P * Q + 1; break;
+      case DBM_TAPE_RES_ITEM: src = r.res.item; n = r.res.n; break;
+      case DBM_TAPE_RES_E: src = r.res.e; n = (int64_t)D * r.res.n; conv = true; break;
+      case DBM_TAPE_GAP_START: src = r.gap.start; n = r.P + 1; break;
+      case DBM_TAPE_GAP_ITEM: src = r.gap.item; n = r.gap.n; break;
+      case DBM_TAPE_GAP_BITS: src = r.gap.bits; n = r.gap.n; break;
+      case DBM_TAPE_GAP_E: src = r.gap.e; n = (int64_t)D * r.gap.n; conv = true; break;
+      case DBM_TAPE_INST_START: src = r.inst_start; n = n_inst + 1; break;
+      default: set_last_error("tape export: unknown array %d", what); return DBM_ERR_INVALID;
+    }
+    const int64_t sz = n * (conv ? 8 : 4);
+    if (needed) *needed = sz;
+    if (!dst || n == 0) return DBM_OK;
+    if (nbytes < sz) { set_last_error("tape export: destination too small"); return DBM_ERR_INVALID; }
+    if (!conv) {
+      DBM_CUDA(cudaMemcpyAsync(dst, src, (size_t)sz, cudaMemcpyDeviceToDevice, s));
+    } else if (!std::is_same<P, PF64>::value && (what == DBM_TAPE_IN_F || what == DBM_TAPE_FSTAR)) {
+      k_dev_to_f64<Q><<<grid_for(n), 256, 0, s>>>((const float*)r.in_rho, (const float*)src, wk, r.M, (double*)dst);
+      DBM_LAUNCH_CHECK();
+    } else {
+      k_to_f64<real><<<grid_for(n), 256, 0, s>>>((const real*)src, n, (double*)dst);
+      DBM_LAUNCH_CHECK();
+    }
+    return DBM_OK;
+  }
+};
+
+}  // namespace dbm
+
+using namespace dbm;
+
+struct dbm_tape {
+  TapeBase* impl;
+};
+
+template <class P>
+static int make_tape(SimBase* sim, TapeBase** out) {
+  return dispatch_lattice(sim->lattice, [&](auto tag) -> int {
+    using LT = decltype(tag);
+    auto* t = new TapeImpl<LT::Q, LT::D, P>(sim);
+    int rc = t->init();
+    if (rc != DBM_OK) { delete t; return rc; }
+    *out = t;
+    return DBM_OK;
+  });
+}
+
+#define TAPE_CHECK(t)                        \
+  if (!(t) || !(t)->impl) {                  \
+    set_last_error("null tape handle");      \
+    return DBM_ERR_INVALID;                  \
+  }
+
+extern "C" {
+
+int dbm_tape_create(dbm_sim* sim, dbm_tape** out) {
+  if (!sim || !sim->impl || !out) { set_last_error("dbm_tape_create: bad arguments"); return DBM_ERR_INVALID; }
+  TapeBase* impl = nullptr;
+  int rc = sim->impl->precision == DBM_FP64 ? make_tape<PF64>(sim->impl, &impl) : make_tape<PF32>(sim->impl, &impl);
+  if (rc != DBM_OK) return rc;
+  *out = new dbm_tape{impl};
+  return DBM_OK;
+}
+int dbm_tape_destroy(dbm_tape* t) {
+  if (!t) return DBM_OK;
+  delete t->impl;
+  delete t;
+  return DBM_OK;
+}
+int dbm_tape_clear(dbm_tape* t) {
+  TAPE_CHECK(t);
+  return t->impl->clear();
+}
+int dbm_tape_step(dbm_tape* t, void* stream) {
+  TAPE_CHECK(t);
+  return t->impl->step((cudaStream_t)stream);
+}
+int32_t dbm_tape_length(dbm_tape* t) {
+  if (!t || !t->impl) return -1;
+  return t->impl->length();
+}
+int dbm_tape_counts(dbm_tape* t, int32_t index, int64_t* counts) {
+  TAPE_CHECK(t);
+  if (!counts) return DBM_ERR_INVALID;
+  return t->impl->counts(index, counts);
+}
+int dbm_tape_backward(dbm_tape* t, int32_t index, const double* goff_out, const double* gf_out, double* goff_in,
+                      double* gf_in, double* gtau, void* stream) {
+  TAPE_CHECK(t);
+  return t->impl->backward(index, goff_out, gf_out, goff_in, gf_in, gtau, (cudaStream_t)stream);
+}
+int dbm_tape_export(dbm_tape* t, int32_t index, int32_t what, void* dst, int64_t bytes, int64_t* needed, void* stream) {
+  TAPE_CHECK(t);
+  return t->impl->export_(index, what, dst, bytes, needed, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -642,22 +642,16 @@ static T sqrt_threshold(T R) {
   return x;
 }
 
-struct SimBase {
-  virtual ~SimBase() = default;
-  virtual int set_state(const int32_t*, const double*, const double*, int64_t, cudaStream_t) = 0;
-  virtual int step(int, cudaStream_t) = 0;
-  virtual int step_partial(int, cudaStream_t) = 0;
-  virtual int profile_step(float*, cudaStream_t) = 0;
-  virtual int count(int64_t*, cudaStream_t) = 0;
-  virtual int get_state(int32_t*, double*, double*, cudaStream_t) = 0;
-  virtual int status(uint32_t*, int, cudaStream_t) = 0;
-  virtual int conservation(double*, cudaStream_t) = 0;
-  virtual int trace(int, void*, int64_t, int64_t*, cudaStream_t) = 0;
-  virtual int64_t device_bytes() const = 0;
-  int use_graphs = 1;
-  int use_tiles = 1;
-  virtual void invalidate_graphs() = 0;
+// Snapshot blob: this header, then cell u32[M], off real[D][M] and f (FP64: double[Q][M];
+// FP32DEV: float rho[M], float dev[Q][M]), each section starting on a 256-byte boundary.
+struct SnapHeader {
+  uint32_t magic;
+  uint32_t m;
+  int32_t lattice;
+  int32_t precision;
 };
+constexpr uint32_t kSnapMagic = 0x44424d53u;  // "DBMS"
+inline size_t snap_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
 template <int Q, int D, class P>
 struct SimImpl : SimBase {
@@ -675,6 +669,8 @@ struct SimImpl : SimBase {
   // sort buffers
   uint32_t *k_in = nullptr, *v_in = nullptr, *k_alt = nullptr, *v_alt = nullptr;
   bool sorted_in_alt = false;
+  bool import_in_alt = false;  // where set_state's sort left the import order
+  InstK* dinst = nullptr;
   void* sort_tmp = nullptr;
   void* compact_tmp = nullptr;
   cudaStream_t own = nullptr;
@@ -744,13 +740,16 @@ struct SimImpl : SimBase {
     }
     if (total + 1 >= 0xffffffffull) { set_last_error("too many cells (%llu)", (unsigned long long)total); return DBM_ERR_CAPACITY; }
     ncells = (uint32_t)total;
+    lattice = d.lattice;
+    precision = d.precision;
+    n_inst = n;
+    n_cells = ncells;
     key_bits = 1;
     while (((uint64_t)1 << key_bits) <= (uint64_t)ncells) ++key_bits;
     ccap = ncells;
     mcap = std::max<int64_t>(d.moment_capacity, ncells);
     if (mcap >= 0x7fffffffLL) { set_last_error("moment capacity too large"); return DBM_ERR_CAPACITY; }
 
-    InstK* dinst;
     uint32_t* dbase;
     DBM_TRY(alloc(&dinst, n));
     DBM_TRY(alloc(&dbase, n + 1));
@@ -937,6 +936,7 @@ struct SimImpl : SimBase {
     DBM_LAUNCH_CHECK();
     bool alt = false;
     DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, m, nullptr, 32, sort_tmp, s, &alt));
+    import_in_alt = alt;
     const uint32_t* ks = alt ? k_alt : k_in;
     const uint32_t* vs = alt ? v_alt : v_in;
     k_import_gather<Q, D, P><<<grid, 256, 0, s>>>(args, fin, m, ks, vs, toff);
@@ -1092,6 +1092,120 @@ struct SimImpl : SimBase {
     return DBM_OK;
   }
 
+  // One full step launched stage by stage with every intermediate kept, and `h` called before the
+  // collision and after the emit (the adjoint records its tape there).
+  int step_hooked(StepHook* h, cudaStream_t s) override {
+    const int keep = trace_on;
+    trace_on = 1;
+    DBM_CUDA(cudaEventRecord(ev_in, s));
+    DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
+    bind();
+    int rc = h->before(&args, own);
+    if (rc == DBM_OK) rc = launch_step(own, 99);
+    if (rc == DBM_OK) rc = h->after(&args, own);
+    trace_on = keep;
+    if (rc != DBM_OK) return rc;
+    cur ^= 1;
+    bind();
+    DBM_CUDA(cudaEventRecord(ev_out, own));
+    DBM_CUDA(cudaStreamWaitEvent(s, ev_out, 0));
+    return DBM_OK;
+  }
+
+  int set_tau(const double* tau, int n) override {
+    if (n != (int)inst_h.size()) { set_last_error("set_tau: expected %d values, got %d", (int)inst_h.size(), n); return DBM_ERR_INVALID; }
+    for (int i = 0; i < n; ++i)
+      if (!(tau[i] > 0.5)) { set_last_error("set_tau: tau must be > 1/2 (instance %d)", i); return DBM_ERR_INVALID; }
+    DBM_CUDA(cudaStreamSynchronize(own));  // no step may still read the table
+    for (int i = 0; i < n; ++i) inst_h[i].tau = tau[i];
+    DBM_CUDA(cudaMemcpy(dinst, inst_h.data(), sizeof(InstK) * n, cudaMemcpyHostToDevice));
+    return DBM_OK;
+  }
+
+  size_t snap_bytes(uint32_t m) const {
+    size_t b = snap_align(sizeof(SnapHeader));
+    b += snap_align((size_t)m * 4) + snap_align((size_t)D * m * sizeof(real));
+    if constexpr (std::is_same<P, PF64>::value) b += snap_align((size_t)Q * m * 8);
+    else b += snap_align((size_t)m * 4) + snap_align((size_t)Q * m * 4);
+    return b;
+  }
+
+  // Copy the current state (count, cells, offsets, f) into a compact device blob.
+  int snapshot(void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) override {
+    int64_t m64 = 0;
+    DBM_CUDA(cudaEventRecord(ev_in, s));
+    DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
+    DBM_TRY(count(&m64, own));
+    const uint32_t m = (uint32_t)m64;
+    const size_t sz = snap_bytes(m);
+    if (needed) *needed = (int64_t)sz;
+    if (!dst) return DBM_OK;
+    if (nbytes < (int64_t)sz) { set_last_error("snapshot: destination too small"); return DBM_ERR_INVALID; }
+    SnapHeader hd{kSnapMagic, m, lattice, precision};
+    char* p = (char*)dst;
+    DBM_CUDA(cudaMemcpyAsync(p, &hd, sizeof(hd), cudaMemcpyHostToDevice, s));
+    p += snap_align(sizeof(SnapHeader));
+    const StateP<P>& S = st[cur];
+    if (m > 0) {
+      DBM_CUDA(cudaMemcpyAsync(p, S.cell, (size_t)m * 4, cudaMemcpyDeviceToDevice, s));
+      p += snap_align((size_t)m * 4);
+      DBM_CUDA(cudaMemcpy2DAsync(p, (size_t)m * sizeof(real), S.off, (size_t)mcap * sizeof(real), (size_t)m * sizeof(real),
+                                 D, cudaMemcpyDeviceToDevice, s));
+      p += snap_align((size_t)D * m * sizeof(real));
+      if constexpr (std::is_same<P, PF64>::value) {
+        DBM_CUDA(cudaMemcpy2DAsync(p, (size_t)m * 8, S.f64, (size_t)mcap * 8, (size_t)m * 8, Q, cudaMemcpyDeviceToDevice, s));
+      } else {
+        DBM_CUDA(cudaMemcpyAsync(p, S.rho, (size_t)m * 4, cudaMemcpyDeviceToDevice, s));
+        p += snap_align((size_t)m * 4);
+        DBM_CUDA(cudaMemcpy2DAsync(p, (size_t)m * 4, S.dev, (size_t)mcap * 4, (size_t)m * 4, Q, cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    DBM_CUDA(cudaStreamSynchronize(s));  // the header lives on this thread's stack
+    return DBM_OK;
+  }
+
+  // Make a snapshot the current state again (bit for bit) and rebuild its cell ranges.
+  int restore(const void* src, int64_t nbytes, cudaStream_t s) override {
+    if (!src || nbytes < (int64_t)snap_align(sizeof(SnapHeader))) { set_last_error("restore: bad blob"); return DBM_ERR_INVALID; }
+    SnapHeader hd{};
+    DBM_CUDA(cudaMemcpy(&hd, src, sizeof(hd), cudaMemcpyDeviceToHost));
+    if (hd.magic != kSnapMagic || hd.lattice != lattice || hd.precision != precision) {
+      set_last_error("restore: blob is not a snapshot of this kind of simulator");
+      return DBM_ERR_INVALID;
+    }
+    const uint32_t m = hd.m;
+    if ((int64_t)m > mcap || (int64_t)snap_bytes(m) > nbytes) { set_last_error("restore: blob too small or too large"); return DBM_ERR_INVALID; }
+    DBM_CUDA(cudaEventRecord(ev_in, s));
+    DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
+    cur = 0;
+    bind();
+    StateP<P>& S = st[0];
+    const char* p = (const char*)src + snap_align(sizeof(SnapHeader));
+    if (m > 0) {
+      DBM_CUDA(cudaMemcpyAsync(S.cell, p, (size_t)m * 4, cudaMemcpyDeviceToDevice, own));
+      p += snap_align((size_t)m * 4);
+      DBM_CUDA(cudaMemcpy2DAsync(S.off, (size_t)mcap * sizeof(real), p, (size_t)m * sizeof(real), (size_t)m * sizeof(real),
+                                 D, cudaMemcpyDeviceToDevice, own));
+      p += snap_align((size_t)D * m * sizeof(real));
+      if constexpr (std::is_same<P, PF64>::value) {
+        DBM_CUDA(cudaMemcpy2DAsync(S.f64, (size_t)mcap * 8, p, (size_t)m * 8, (size_t)m * 8, Q, cudaMemcpyDeviceToDevice, own));
+      } else {
+        DBM_CUDA(cudaMemcpyAsync(S.rho, p, (size_t)m * 4, cudaMemcpyDeviceToDevice, own));
+        p += snap_align((size_t)m * 4);
+        DBM_CUDA(cudaMemcpy2DAsync(S.dev, (size_t)mcap * 4, p, (size_t)m * 4, (size_t)m * 4, Q, cudaMemcpyDeviceToDevice, own));
+      }
+    }
+    DBM_CUDA(cudaMemcpyAsync(S.count, &m, 4, cudaMemcpyHostToDevice, own));
+    DBM_CUDA(cudaMemcpyAsync(args.d_P, &m, 4, cudaMemcpyHostToDevice, own));
+    k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, own>>>(
+        S.cell, args.d_P, ncells, S.start);
+    DBM_LAUNCH_CHECK();
+    DBM_CUDA(cudaStreamSynchronize(own));  // `m` lives on this thread's stack
+    DBM_CUDA(cudaEventRecord(ev_out, own));
+    DBM_CUDA(cudaStreamWaitEvent(s, ev_out, 0));
+    return DBM_OK;
+  }
+
   int count(int64_t* m, cudaStream_t s) override {
     uint32_t h = 0;
     DBM_CUDA(cudaMemcpyAsync(&h, st[cur].count, 4, cudaMemcpyDeviceToHost, s));
@@ -1167,6 +1281,7 @@ struct SimImpl : SimBase {
         }
         return DBM_OK;
       }
+      case DBM_TRACE_IMPORT_ORDER: src = import_in_alt ? v_alt : v_in; sz = mcap * 4; break;
       case DBM_TRACE_STATE_CELL: src = A.a.cell; sz = mcap * 4; break;
       case DBM_TRACE_STATE_OFF: src = A.a.off; sz = (int64_t)D * mcap * sizeof(real); break;
       case DBM_TRACE_COUNTS: {
@@ -1195,10 +1310,6 @@ struct SimImpl : SimBase {
 }  // namespace dbm
 
 using namespace dbm;
-
-struct dbm_sim {
-  SimBase* impl;
-};
 
 template <class P>
 static int make_impl(const dbm_sim_desc& d, const dbm_instance_desc* in, int n, SimBase** out) {
@@ -1304,6 +1415,19 @@ int dbm_sim_trace(dbm_sim* s, int32_t what, void* dst, int64_t bytes, int64_t* n
 int64_t dbm_sim_device_bytes(dbm_sim* s) {
   if (!s || !s->impl) return -1;
   return s->impl->device_bytes();
+}
+int dbm_sim_set_tau(dbm_sim* s, const double* tau, int32_t n) {
+  SIM_CHECK(s);
+  if (!tau) { set_last_error("dbm_sim_set_tau: null tau"); return DBM_ERR_INVALID; }
+  return s->impl->set_tau(tau, n);
+}
+int dbm_sim_snapshot(dbm_sim* s, void* dst, int64_t bytes, int64_t* needed, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->snapshot(dst, bytes, needed, (cudaStream_t)stream);
+}
+int dbm_sim_restore(dbm_sim* s, const void* src, int64_t bytes, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->restore(src, bytes, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -165,4 +165,44 @@ __device__ __forceinline__ T cell_d2_lower(const T (&c)[3]) {
 template <class P>
 __device__ __forceinline__ typename P::real floor_r(typename P::real x) { return floor(x); }
 
+// Called around one step by SimBase::step_hooked.  `before` sees the input state (args->a, not
+// yet collided); `after` sees every buffer of the step (a = the collided input moments, b = the
+// output moments, the per-cell thinning/refine scratch, the sorted pairs, 1/sw, the gathered f
+// and the empty masks) before the two state buffers swap roles.  `args` is an Args<Q, D, P>.
+struct StepHook {
+  virtual ~StepHook() = default;
+  virtual int before(const void* args, cudaStream_t s) = 0;
+  virtual int after(const void* args, cudaStream_t s) = 0;
+};
+
+// Type-erased simulator (SimImpl<Q, D, P> in sim.cu).
+struct SimBase {
+  virtual ~SimBase() = default;
+  virtual int set_state(const int32_t*, const double*, const double*, int64_t, cudaStream_t) = 0;
+  virtual int step(int, cudaStream_t) = 0;
+  virtual int step_partial(int, cudaStream_t) = 0;
+  virtual int step_hooked(StepHook*, cudaStream_t) = 0;
+  virtual int profile_step(float*, cudaStream_t) = 0;
+  virtual int count(int64_t*, cudaStream_t) = 0;
+  virtual int get_state(int32_t*, double*, double*, cudaStream_t) = 0;
+  virtual int status(uint32_t*, int, cudaStream_t) = 0;
+  virtual int conservation(double*, cudaStream_t) = 0;
+  virtual int trace(int, void*, int64_t, int64_t*, cudaStream_t) = 0;
+  virtual int set_tau(const double*, int) = 0;
+  virtual int snapshot(void*, int64_t, int64_t*, cudaStream_t) = 0;
+  virtual int restore(const void*, int64_t, cudaStream_t) = 0;
+  virtual int64_t device_bytes() const = 0;
+  virtual void invalidate_graphs() = 0;
+  int use_graphs = 1;
+  int use_tiles = 1;
+  int lattice = 0;
+  int precision = 0;
+  int n_inst = 0;
+  uint32_t n_cells = 0;
+};
+
 }  // namespace dbm
+
+struct dbm_sim {
+  dbm::SimBase* impl;
+};

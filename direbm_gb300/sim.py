@@ -219,3 +219,35 @@ class Simulation:
             _lib.check(self.lib.dbm_sim_trace(self._h, what, buf.data_ptr(), buf.numel(), ctypes.byref(need), _stream()),
                        "dbm_sim_trace")
         return buf
+
+    # ---- parameters, checkpoints ----------------------------------------------------------------
+    def set_tau(self, tau):
+        """Replace every instance's tau (one value per instance, each > 1/2)."""
+        t = np.ascontiguousarray(np.asarray(tau, dtype=np.float64).reshape(-1))
+        if t.shape[0] != len(self.instances):
+            raise ValueError(f"set_tau: expected {len(self.instances)} values")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_set_tau(self._h, t.ctypes.data, len(t)), "dbm_sim_set_tau")
+        for inst, v in zip(self.instances, t):
+            inst.tau = float(v)
+
+    def snapshot(self) -> torch.Tensor:
+        """The current state as a device blob (uint8 tensor); ``restore`` makes it current again."""
+        need = ctypes.c_int64()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_snapshot(self._h, None, 0, ctypes.byref(need), _stream()), "dbm_sim_snapshot")
+            blob = torch.empty(int(need.value), dtype=torch.uint8, device=self.device)
+            _lib.check(self.lib.dbm_sim_snapshot(self._h, blob.data_ptr(), blob.numel(), ctypes.byref(need), _stream()),
+                       "dbm_sim_snapshot")
+        return blob
+
+    def restore(self, blob: torch.Tensor, iteration: int | None = None):
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_restore(self._h, blob.data_ptr(), blob.numel(), _stream()), "dbm_sim_restore")
+        if iteration is not None:
+            self.iteration = int(iteration)
+
+    def import_order(self, m: int) -> torch.Tensor:
+        """After ``set_state`` (before any step): input index of each sorted moment, int64 (m,)."""
+        buf = self.trace("import_order")
+        return buf.view(torch.int32)[:m].to(torch.int64)

@@ -177,6 +177,70 @@ int dbm_sim_profile_step(dbm_sim* sim, float* stage_ms, void* stream);
 int dbm_sim_trace(dbm_sim* sim, int32_t what, void* d_dst, int64_t bytes, int64_t* needed, void* stream);
 /* Device memory held by the handle. */
 int64_t dbm_sim_device_bytes(dbm_sim* sim);
+/* Replace every instance's tau (n = number of instances, each > 1/2).  Synchronises.  The
+ * reference fixes tau at construction (warp/simulator.py:25-44); a new tau is what a gradient
+ * step on tau needs. */
+int dbm_sim_set_tau(dbm_sim* sim, const double* h_tau, int32_t n);
+/* Checkpoint / resume (the reference has none): copy the current state into a device blob of
+ * *needed bytes (call with d_dst = NULL to size it; synchronises), and make such a blob the
+ * current state again, bit for bit. */
+int dbm_sim_snapshot(dbm_sim* sim, void* d_dst, int64_t bytes, int64_t* needed, void* stream);
+int dbm_sim_restore(dbm_sim* sim, const void* d_src, int64_t bytes, void* stream);
+
+/* ---- adjoint of the step (no reference counterpart: differentiation is future work in the
+ * reference, idea.md:250) ---------------------------------------------------------------------
+ * A tape records steps of a simulator: the input moments, the collided f, each component's thin
+ * cell, each control point's thin cell / count / centroid / refine decision, and three neighbour
+ * lists -- refine (control point -> components within r of its centroid, moved points only),
+ * resample (control point and direction -> components within r) and gap fill (control point ->
+ * control points within r sharing an empty direction) -- with the displacement of every pair as
+ * the forward step computed it.  dbm_tape_backward applies the transpose of the step's Jacobian
+ * with those discrete decisions held fixed (a hand-written vector-Jacobian product of the
+ * collision, the dispersion, thinning, refine, resampling weights, gather and gap fill).
+ * Cotangents are FP64, row-major, in the sorted moment order of each state:
+ *   g_off_out (P, D), g_f_out (P, Q): d loss / d (output offsets in cell units, output f)
+ *   g_off_in (M, D), g_f_in (M, Q):  written, d loss / d (input offsets, input f)
+ *   g_tau (n_inst): accumulated (+=), d loss / d tau of each instance. */
+typedef struct dbm_tape dbm_tape;
+int dbm_tape_create(dbm_sim* sim, dbm_tape** out);
+int dbm_tape_destroy(dbm_tape* tape);
+/* Forget every recorded step (device memory is kept for reuse). */
+int dbm_tape_clear(dbm_tape* tape);
+/* Advance the tape's simulator by one step and record it.  Synchronises. */
+int dbm_tape_step(dbm_tape* tape, void* stream);
+int32_t dbm_tape_length(dbm_tape* tape);
+/* counts[8] of recorded step `index`: M, P, refine pairs, resample pairs, gap-fill pairs. */
+int dbm_tape_counts(dbm_tape* tape, int32_t index, int64_t* counts);
+int dbm_tape_backward(dbm_tape* tape, int32_t index, const double* d_g_off_out, const double* d_g_f_out,
+                      double* d_g_off_in, double* d_g_f_in, double* d_g_tau, void* stream);
+/* Copy a recorded array (DBM_TAPE_*) of step `index` into d_dst, converted to the listed type;
+ * *needed returns its size in bytes. */
+int dbm_tape_export(dbm_tape* tape, int32_t index, int32_t what, void* d_dst, int64_t bytes, int64_t* needed,
+                    void* stream);
+#define DBM_TAPE_IN_CELL 1       /* u32[M] */
+#define DBM_TAPE_IN_OFF 2        /* f64[D][M] */
+#define DBM_TAPE_IN_F 3          /* f64[Q][M] (FP32DEV: rho*W + dev) */
+#define DBM_TAPE_FSTAR 4         /* f64[Q][M] collided f */
+#define DBM_TAPE_THIN_CELL 5     /* u32[Q][M] cell each component lands in (0xffffffff: outside) */
+#define DBM_TAPE_CP_THIN 6       /* u32[P] thin cell of each output control point */
+#define DBM_TAPE_CP_COUNT 7      /* u32[P] components thinned into it */
+#define DBM_TAPE_CP_CEN 8        /* f64[D][P] centroid offset in its thin cell */
+#define DBM_TAPE_CP_MOVED 9      /* u32[P] 1 if refine moved it */
+#define DBM_TAPE_OUT_CELL 10     /* u32[P] */
+#define DBM_TAPE_OUT_OFF 11      /* f64[D][P] */
+#define DBM_TAPE_EMPTY 12        /* u32[P] gap-filled directions (bit k) */
+#define DBM_TAPE_INV_SW 13       /* f64[Q][M] 1/sw per component (0 if dropped) */
+#define DBM_TAPE_REFINE_START 14 /* u32[P+1] */
+#define DBM_TAPE_REFINE_ITEM 15  /* u32[n] component m*Q + k */
+#define DBM_TAPE_REFINE_E 16     /* f64[D][n] component minus centroid */
+#define DBM_TAPE_RES_START 17    /* u32[P*Q+1], row j*Q + k */
+#define DBM_TAPE_RES_ITEM 18     /* u32[n] component m*Q + k */
+#define DBM_TAPE_RES_E 19        /* f64[D][n] component minus control point */
+#define DBM_TAPE_GAP_START 20    /* u32[P+1] */
+#define DBM_TAPE_GAP_ITEM 21     /* u32[n] neighbour control point */
+#define DBM_TAPE_GAP_BITS 22     /* u32[n] directions empty in both */
+#define DBM_TAPE_GAP_E 23        /* f64[D][n] neighbour minus control point */
+#define DBM_TAPE_INST_START 24   /* u32[n_inst+1] first input moment of each instance */
 
 #define DBM_TRACE_OCC 1        /* u32[ncells]   occupied flag per cell after thinning */
 #define DBM_TRACE_THIN_CNT 2   /* u32[ncells]   components per occupied cell */
@@ -192,6 +256,8 @@ int64_t dbm_sim_device_bytes(dbm_sim* sim);
 #define DBM_TRACE_COUNTS 12    /* u32[2]: M (moments in), P (control points) */
 #define DBM_TRACE_STATE_CELL 13 /* u32[Mcap]    cell of each current moment */
 #define DBM_TRACE_STATE_OFF 14  /* real[D][Mcap] offsets of each current moment */
+#define DBM_TRACE_IMPORT_ORDER 15 /* u32[Mcap] after dbm_sim_set_state (and before any step):
+                                     input index of each sorted moment */
 
 #ifdef __cplusplus
 }

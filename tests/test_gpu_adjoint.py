@@ -1,0 +1,256 @@
+"""The CUDA adjoint (dbm_tape_* through direbm_gb300.adjoint) against the FP64 torch restatement of
+the fixed-structure step (oracle/adjoint_ref.py), against central finite differences, and the
+recorded neighbour lists against the numpy oracle's."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import adjoint_ref, grid_step
+from tests._cases import bounded_box, oracle_spec, periodic_tg, rest_pulse
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(lattice, instances, dx, r_res, cell, precision, kappa_hard=4, cap=0):
+    from direbm_gb300.sim import Instance, Simulation
+
+    insts = [Instance(dims=tuple(i["dims"]), origin=tuple(i.get("origin", (0,) * len(i["dims"]))),
+                      periodic=i.get("periodic", True), tau=i.get("tau", 0.6)) for i in instances]
+    return Simulation(insts, lattice=lattice, precision=precision, dx=dx, r_res=r_res, cell=cell,
+                      kappa_hard=kappa_hard, moment_capacity=cap)
+
+
+def _tg(n=24, lattice="D2Q9", seed=3, tau=0.6):
+    x, f = periodic_tg(n, lattice, seed=seed, u0=0.05)
+    return dict(lattice=lattice, instances=[{"dims": (n, n), "tau": tau}], dx=1.0, r_res=1.5, cell=1.0,
+                inst=np.zeros(len(x), np.int32), x=x, f=f)
+
+
+def _pulse(jitter=0.1):
+    x, f = rest_pulse(6, "D2Q7", 1.5)
+    x = x + np.random.default_rng(11).uniform(-jitter, jitter, size=x.shape)
+    dims, origin = bounded_box(x, 0.25, 3.0)
+    return dict(lattice="D2Q7", instances=[{"dims": dims, "origin": origin, "periodic": False, "tau": 0.7}], dx=1.0,
+                r_res=1.0, cell=0.25, inst=np.zeros(len(x), np.int32), x=x, f=f)
+
+
+def _two_instances():
+    a, b = _tg(16, seed=1, tau=0.55), _tg(16, seed=2, tau=0.9)
+    return dict(lattice="D2Q9", instances=a["instances"] + b["instances"], dx=1.0, r_res=1.5, cell=1.0,
+                inst=np.concatenate([a["inst"], np.ones(len(b["x"]), np.int32)]),
+                x=np.concatenate([a["x"], b["x"]]), f=np.concatenate([a["f"], b["f"]]))
+
+
+def _d3q19(n=10):
+    x, f = periodic_tg(n, "D3Q19", seed=4, u0=0.04)
+    return dict(lattice="D3Q19", instances=[{"dims": (n, n, n), "tau": 0.6}], dx=1.0, r_res=1.5, cell=1.0,
+                inst=np.zeros(len(x), np.int32), x=x, f=f)
+
+
+CASES = {"tg_d2q9": _tg, "pulse_d2q7": _pulse, "two_inst_d2q9": _two_instances, "d3q19": _d3q19}
+
+
+def _spec(c, dtype=np.float64):
+    return oracle_spec(c["lattice"], c["instances"], c["dx"], c["r_res"], c["cell"], 4, dtype=dtype)
+
+
+def _record(c, precision, nsteps, noneq=0.0):
+    """Record nsteps; noneq > 0 scales each input f_k by 1 + U(-noneq, noneq) (seeded) so that the
+    first collision has a non-zero tau derivative."""
+    from direbm_gb300.adjoint import Tape
+
+    sim = _sim(c["lattice"], c["instances"], c["dx"], c["r_res"], c["cell"], precision, cap=4 * len(c["x"]))
+    f = c["f"] * (1.0 + np.random.default_rng(17).uniform(-noneq, noneq, size=c["f"].shape))
+    sim.set_state(c["inst"], c["x"], f)
+    order = sim.import_order(len(c["x"])).cpu().numpy()
+    tape = Tape(sim)
+    for _ in range(nsteps):
+        tape.step()
+    sim.check_status()
+    return sim, tape, order
+
+
+def _torch_step(spec, T, off, f, tau):
+    return adjoint_ref.step_fixed(T, spec.lattice, float(spec.R), spec.base, [i.rho_rest for i in spec.instances],
+                                  off, f, tau)
+
+
+def _rowsets(start, item, row_of=None):
+    start = np.asarray(start)
+    return [tuple(sorted(item[start[r]:start[r + 1]])) for r in range(len(start) - 1)]
+
+
+@pytest.mark.parametrize("case", ["tg_d2q9", "pulse_d2q7", "two_inst_d2q9"])
+def test_tape_lists_match_oracle_structure(case):
+    """FP64: the recorded structure (thinning, refine pairs, resampling pairs, gap-fill pairs) is the
+    oracle's, pair for pair."""
+    c = CASES[case]()
+    spec = _spec(c)
+    sim, tape, _ = _record(c, "fp64", 1)
+    G = tape.export(0)
+    st = grid_step.from_world(spec, c["inst"], c["x"], c["f"])
+    T, _ = adjoint_ref.tape_from_oracle(spec, st)
+    assert G["counts"] == T["counts"]
+    for k in ("in_cell", "cp_thin", "cp_count", "cp_moved", "out_cell", "empty", "inst_start"):
+        np.testing.assert_array_equal(G[k], T[k], err_msg=k)
+    thin = np.where(G["thin_cell"] == 0xFFFFFFFF, -1, G["thin_cell"])
+    np.testing.assert_array_equal(thin, T["thin_cell"])
+    np.testing.assert_allclose(G["out_off"], T["out_off"], rtol=0, atol=1e-13)
+    for pre in ("ref", "res", "gap"):
+        assert _rowsets(G[f"{pre}_start"], G[f"{pre}_item"]) == _rowsets(T[f"{pre}_start"], T[f"{pre}_item"]), pre
+    np.testing.assert_array_equal(G["res_start"], T["res_start"])
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_one_step_backward_matches_torch_reference(case, precision):
+    """dbm_tape_backward of one step against torch.autograd of the FP64 fixed-structure step built
+    from the same recorded tape (FP64: 1e-9 relative; FP32DEV: 2e-4 relative)."""
+    c = CASES[case]()
+    spec = _spec(c)
+    sim, tape, _ = _record(c, precision, 1, noneq=0.1)
+    T = tape.export(0)
+    P, M, Q, D = T["counts"]["P"], T["counts"]["M"], spec.Q, spec.D
+    rng = np.random.default_rng(7)
+    go = rng.normal(size=(P, D))
+    gf = rng.normal(size=(P, Q))
+    gt = torch.zeros(len(spec.instances), dtype=torch.float64, device="cuda")
+    g_off, g_f = tape.backward(0, torch.as_tensor(go, device="cuda"), torch.as_tensor(gf, device="cuda"), gt)
+    off = torch.as_tensor(T["in_off"]).requires_grad_(True)
+    f = torch.as_tensor(T["in_f"]).requires_grad_(True)
+    tau = torch.tensor([i["tau"] for i in c["instances"]], dtype=torch.float64, requires_grad=True)
+    o, F = _torch_step(spec, T, off, f, tau)
+    ((o * torch.as_tensor(go)).sum() + (F * torch.as_tensor(gf)).sum()).backward()
+    tol = 1e-9 if precision == "fp64" else 2e-4
+    for name, got, ref in (("off", g_off.cpu().numpy(), off.grad.numpy()), ("f", g_f.cpu().numpy(), f.grad.numpy()),
+                           ("tau", gt.cpu().numpy(), tau.grad.numpy())):
+        err = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300)
+        assert err < tol, (name, err)
+    assert M == len(c["x"])
+
+
+def _mode_problem(n=24, steps=6):
+    from direbm_gb300.adjoint import ModeField
+
+    x, _ = periodic_tg(n, "D2Q9", seed=5, u0=0.0)
+    field = ModeField(n, seed=21, points=x)
+    target = ModeField(n, seed=1000, points=x)
+    return x, field, target
+
+
+def _loss_torch_chain(spec, tapes, order, x, field, target, coeffs, tau, lattice):
+    """The same loss as direbm_gb300.adjoint.inverse_problem_loss, through the FP64 torch chain of
+    fixed-structure steps."""
+    from direbm_gb300.adjoint import equilibrium, velocity
+
+    xs = torch.as_tensor(x)[torch.as_tensor(order)]
+    f = equilibrium(torch.ones(len(x), dtype=torch.float64), field(xs, coeffs), lattice)
+    off = torch.as_tensor(tapes[0]["in_off"])
+    for T in tapes:
+        off, f = _torch_step(spec, T, off, f, tau)
+    T = tapes[-1]
+    cells = T["out_cell"]
+    n = spec.instances[0].dims[0]
+    pos = torch.stack([torch.as_tensor((cells % n).astype(np.float64)), torch.as_tensor((cells // n).astype(np.float64))],
+                      1) + off
+    du = velocity(f, lattice) - target(pos * spec.cell, target.coeffs)
+    return (du * du).sum(1).mean()
+
+
+@pytest.mark.parametrize("every", [1, 4, 6])
+def test_rollout_gradient_matches_torch_chain_and_finite_differences(every):
+    """The inverse problem on 24x24 points, 6 steps, FP64: gradient w.r.t. the 16 mode coefficients
+    and tau through the checkpointed autograd Function, against torch.autograd of the fixed-structure
+    FP64 chain (1e-9) and against central differences of that chain (1e-6)."""
+    from direbm_gb300.adjoint import Tape, inverse_problem_loss
+    from direbm_gb300.lattices import D2Q9
+
+    n, steps = 24, 6
+    x, field, target = _mode_problem(n, steps)
+    c = dict(lattice="D2Q9", instances=[{"dims": (n, n), "tau": 0.6}], dx=1.0, r_res=1.5, cell=1.0)
+    sim = _sim("D2Q9", c["instances"], 1.0, 1.5, 1.0, "fp64", cap=4 * len(x))
+    coeffs = torch.tensor(field.coeffs, dtype=torch.float64, device="cuda", requires_grad=True)
+    tau = torch.tensor([0.6], dtype=torch.float64, device="cuda", requires_grad=True)
+    x_d = torch.as_tensor(x, device="cuda")
+    loss = inverse_problem_loss(sim, x_d, field, coeffs, tau, target, steps, every)
+    loss.backward()
+    g = torch.cat([coeffs.grad, tau.grad]).cpu().numpy()
+    assert np.all(np.isfinite(g)) and np.abs(g).max() > 0
+
+    # the same trajectory recorded step by step, then the FP64 torch chain
+    from direbm_gb300.adjoint import equilibrium
+
+    f0 = equilibrium(torch.ones(len(x), dtype=torch.float64, device="cuda"), field(x_d, coeffs.detach()), D2Q9)
+    sim.set_tau([0.6])
+    sim.set_state(None, x_d, f0)
+    order = sim.import_order(len(x)).cpu().numpy()
+    tape = Tape(sim)
+    for _ in range(steps):
+        tape.step()
+    tapes = [tape.export(i) for i in range(steps)]
+    spec = _spec(c)
+    cc = torch.tensor(field.coeffs, dtype=torch.float64, requires_grad=True)
+    tt = torch.tensor([0.6], dtype=torch.float64, requires_grad=True)
+    lt = _loss_torch_chain(spec, tapes, order, x, field, target, cc, tt, D2Q9)
+    assert abs(lt.item() - loss.item()) <= 1e-12 * abs(lt.item())
+    lt.backward()
+    gref = torch.cat([cc.grad, tt.grad]).numpy()
+    assert np.linalg.norm(g - gref) <= 1e-9 * np.linalg.norm(gref), (g, gref)
+    # central differences of the fixed-structure chain along a few random directions
+    rng = np.random.default_rng(3)
+    h = 1e-5
+    for _ in range(3):
+        v = rng.normal(size=17)
+        with torch.no_grad():
+            lp = _loss_torch_chain(spec, tapes, order, x, field, target, torch.as_tensor(field.coeffs + h * v[:16]),
+                                   torch.tensor([0.6 + h * v[16]]), D2Q9)
+            lm = _loss_torch_chain(spec, tapes, order, x, field, target, torch.as_tensor(field.coeffs - h * v[:16]),
+                                   torch.tensor([0.6 - h * v[16]]), D2Q9)
+        fd = float(lp - lm) / (2 * h)
+        assert abs(fd - float(g @ v)) <= 1e-6 * abs(fd), (fd, float(g @ v))
+
+
+def test_rollout_checkpointing_is_exact_and_leaves_final_state():
+    """Gradients do not depend on the checkpoint interval (bit for bit), and the simulator is left at
+    the final state of the rollout."""
+    from direbm_gb300.adjoint import inverse_problem_loss
+
+    n, steps = 24, 5
+    x, field, target = _mode_problem(n, steps)
+    x_d = torch.as_tensor(x, device="cuda")
+    grads = []
+    for every in (1, 2, 5):
+        sim = _sim("D2Q9", [{"dims": (n, n), "tau": 0.6}], 1.0, 1.5, 1.0, "fp32dev", cap=4 * len(x))
+        coeffs = torch.tensor(field.coeffs, dtype=torch.float64, device="cuda", requires_grad=True)
+        tau = torch.tensor([0.6], dtype=torch.float64, device="cuda", requires_grad=True)
+        loss = inverse_problem_loss(sim, x_d, field, coeffs, tau, target, steps, every)
+        _, pos_a, f_a = sim.state()
+        loss.backward()
+        _, pos_b, f_b = sim.state()
+        assert torch.equal(pos_a, pos_b) and torch.equal(f_a, f_b)
+        grads.append(torch.cat([coeffs.grad, tau.grad]).cpu().numpy())
+    np.testing.assert_array_equal(grads[0], grads[1])
+    np.testing.assert_array_equal(grads[0], grads[2])
+
+
+def test_fp32dev_rollout_gradient_close_to_fp64():
+    """The FP32-deviation forward + adjoint against the FP64 one on the same problem (relative L2
+    error of the 17-vector stated in the assertion)."""
+    from direbm_gb300.adjoint import inverse_problem_loss
+
+    n, steps = 32, 10
+    x, field, target = _mode_problem(n, steps)
+    x_d = torch.as_tensor(x, device="cuda")
+    out = {}
+    for prec in ("fp64", "fp32dev"):
+        sim = _sim("D2Q9", [{"dims": (n, n), "tau": 0.6}], 1.0, 1.5, 1.0, prec, cap=4 * len(x))
+        coeffs = torch.tensor(field.coeffs, dtype=torch.float64, device="cuda", requires_grad=True)
+        tau = torch.tensor([0.6], dtype=torch.float64, device="cuda", requires_grad=True)
+        loss = inverse_problem_loss(sim, x_d, field, coeffs, tau, target, steps, 5)
+        loss.backward()
+        out[prec] = (float(loss), torch.cat([coeffs.grad, tau.grad]).cpu().numpy())
+    l64, g64 = out["fp64"]
+    l32, g32 = out["fp32dev"]
+    assert abs(l32 - l64) <= 1e-5 * abs(l64)
+    assert np.linalg.norm(g32 - g64) <= 1e-3 * np.linalg.norm(g64), np.linalg.norm(g32 - g64) / np.linalg.norm(g64)
