@@ -14,6 +14,8 @@ Keys beyond the base contract:
   fp64          the same workload in the FP64 store (fewer steps: GB300 FP64 is slow)
   accuracy      velocity L2 error vs the FP64 oracle on a 4096-point instance
   lbm           hexagonal D2Q7 shear wave 1024x1024 (FP32DEV and FP64), node-steps/s
+  adjoint       inverse problem on 64k points, 100 steps, checkpoint every 10: adjoint steps/s, its
+                cost relative to the forward step, FP32DEV gradient error vs FP64
   cpu_baseline  the CPU oracle (numpy restatement of the reference step) on the host cores
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -330,6 +332,63 @@ def e2e_leg(sim, ib, x, f, steps=2):
             "path": "Simulation.set_state/step/state (C ABI dbm_sim_*) with pinned host buffers"}
 
 
+def adjoint_leg(n=256, steps=100, every=10, tau=0.6):
+    """Inverse problem: one periodic D2Q9 run of n x n = 64k jittered points, unit density, initial
+    velocity from 8 Fourier modes (16 coefficients, seed 21, RMS 0.02); loss = mean |u(f_T) - u*(x_T)|^2
+    against a target 8-mode field (seed 1000); gradient w.r.t. the 16 coefficients and tau through
+    the checkpointed adjoint (checkpoint every `every` steps).  Times the plain forward (graphs),
+    the forward with checkpoints and the backward (recomputation + tape + VJP) with CUDA events,
+    in FP32DEV and FP64, and compares the two gradients."""
+    import torch
+
+    from direbm_gb300.adjoint import ModeField, Tape, inverse_problem_loss
+    from direbm_gb300.lattices import D2Q9, equilibrium as eq_np
+
+    x = instance_points(n, 5)
+    field = ModeField(n, seed=21, points=x)
+    target = ModeField(n, seed=1000, points=x)
+    x_d = torch.as_tensor(x, device="cuda")
+    out = {"config": f"{n}x{n} jittered points, periodic D2Q9, tau {tau}, r 1.5h, cell h, {steps} steps, "
+                     f"checkpoint every {every}; 16 mode coefficients + tau", "steps": steps, "checkpoint_every": every}
+    grads = {}
+    for prec in ("fp32dev", "fp64"):
+        sim = make_sim([n], [tau], prec, 4 * len(x))
+        # plain forward step (captured graphs), the reference cost of one step
+        f0 = eq_np(np.ones(len(x)), field(torch.as_tensor(x), torch.as_tensor(field.coeffs)).numpy(), D2Q9)
+        sim.set_state(None, x, f0)
+        ms_plain, _ = timed_steps(sim, steps, 3)
+        tape = Tape(sim)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        res = None
+        for rep in range(2):  # the first repetition warms up allocations
+            coeffs = torch.tensor(field.coeffs, dtype=torch.float64, device="cuda", requires_grad=True)
+            tt = torch.tensor([tau], dtype=torch.float64, device="cuda", requires_grad=True)
+            torch.cuda.synchronize()
+            ev[0].record()
+            loss = inverse_problem_loss(sim, x_d, field, coeffs, tt, target, steps, every, tape)
+            ev[1].record()
+            loss.backward()
+            ev[2].record()
+            torch.cuda.synchronize()
+            res = (float(loss.item()), torch.cat([coeffs.grad, tt.grad]).cpu().numpy(), ev[0].elapsed_time(ev[1]),
+                   ev[1].elapsed_time(ev[2]))
+        loss_v, g, ms_f, ms_b = res
+        grads[prec] = g
+        step_ms = ms_plain / steps
+        out[prec] = {
+            "loss": loss_v, "forward_ms_per_step": step_ms, "forward_ckpt_ms_per_step": ms_f / steps,
+            "backward_ms_per_step": ms_b / steps, "adjoint_steps_per_s": steps / (ms_b * 1e-3),
+            "gradient_steps_per_s": steps / ((ms_f + ms_b) * 1e-3),
+            "backward_over_forward": (ms_b / steps) / step_ms, "gradient_over_forward": ((ms_f + ms_b) / steps) / step_ms,
+            "grad_norm": float(np.linalg.norm(g)), "dL_dtau": float(g[-1]),
+        }
+        tape.close()
+        sim.close()
+    out["fp32dev_grad_rel_err_vs_fp64"] = float(np.linalg.norm(grads["fp32dev"] - grads["fp64"]) /
+                                                 np.linalg.norm(grads["fp64"]))
+    return out
+
+
 # ---- CPU oracle legs -----------------------------------------------------------------------------
 
 def _oracle_instance_steps(args):
@@ -464,6 +523,7 @@ def run_ours(args):
 
     acc = accuracy_leg()
     lbm = lbm_leg()
+    adj = adjoint_leg()
     cpu = cpu_baseline_leg()
     line = {
         "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
@@ -476,6 +536,7 @@ def run_ours(args):
         "roofline": roof, "stage_ms": stage_ms, "step_roofline": step_roof,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
         "fp64": fp64, "speedup_fp32dev_vs_fp64": value / world / fp64["value"], "accuracy": acc, "lbm": lbm,
+        "adjoint": adj,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -490,10 +551,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=N_INST, help="first N ensemble members (profiling runs)")
-    ap.add_argument("--legs", default="all", choices=["all", "main"], help="main = timed step only")
+    ap.add_argument("--legs", default="all", choices=["all", "main", "adjoint"],
+                    help="main = timed step only; adjoint = the inverse-problem leg only")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.legs == "adjoint" and args.impl == "ours":
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"adjoint": adjoint_leg()}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -31,7 +31,7 @@ TAPE = {
     "thin_cell": (5, "u32", "QM"), "cp_thin": (6, "u32", "P"), "cp_count": (7, "u32", "P"),
     "cp_cen": (8, "f64", "DP"), "cp_moved": (9, "u32", "P"), "out_cell": (10, "u32", "P"),
     "out_off": (11, "f64", "DP"), "empty": (12, "u32", "P"), "inv_sw": (13, "f64", "QM"),
-    "ref_start": (14, "u32", "P+1"), "ref_item": (15, "u32", "nref"), "ref_e": (16, "f64", "Dnref"),
+    "ref_start": (14, "u32", "PQ+1"), "ref_item": (15, "u32", "nref"), "ref_e": (16, "f64", "Dnref"),
     "res_start": (17, "u32", "PQ+1"), "res_item": (18, "u32", "nres"), "res_e": (19, "f64", "Dnres"),
     "gap_start": (20, "u32", "P+1"), "gap_item": (21, "u32", "ngap"), "gap_bits": (22, "u32", "ngap"),
     "gap_e": (23, "f64", "Dngap"), "inst_start": (24, "u32", "I+1"),

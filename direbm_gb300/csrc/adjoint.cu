@@ -64,19 +64,29 @@ struct DevArena {
 };
 
 // ---- the recorded step ----------------------------------------------------------------------
-template <class real>
-struct PairCSR {
-  int64_t rows = 0, items = 0, n = 0;
-  uint32_t* start = nullptr;   // [rows + 1]
-  uint32_t* row = nullptr;     // [n] the CP of each pair
-  uint32_t* item = nullptr;    // [n] component m*Q + k (gap fill: the neighbour CP)
-  uint32_t* bits = nullptr;    // [n] gap fill only: directions empty in both CPs
-  real* e = nullptr;           // [D][n] displacement item - reference point, as the step computed it
-  uint32_t* tperm = nullptr;   // [n] pair indices ordered by item (stable)
-  uint32_t* tstart = nullptr;  // [items + 1]
+
+// One recorded pair: the reference point (row: a CP), the other end (item: a component m*Q + k, or
+// a neighbour CP in the gap fill) and the displacement e = other end - reference point exactly as
+// the step computed it.  One record is one aligned store / load (16 bytes for FP32 in 2D).  In a
+// transposed list `item` holds the pair's index in the row-ordered list instead.
+template <class real, int D>
+struct alignas((sizeof(real) * D + 8) <= 16 ? 16 : 8) PairRec {
+  uint32_t row;
+  uint32_t item;
+  real e[D];
 };
 
-template <class real>
+template <class real, int D>
+struct PairCSR {
+  int64_t rows = 0, items = 0, n = 0;
+  uint32_t* start = nullptr;         // [rows + 1]
+  PairRec<real, D>* rec = nullptr;   // [n] grouped by row
+  uint32_t* bits = nullptr;          // [n] gap fill only: directions empty in both CPs
+  PairRec<real, D>* trec = nullptr;  // [n] grouped by item, ascending row-list index inside a group
+  uint32_t* tstart = nullptr;        // [items + 1]
+};
+
+template <class real, int D>
 struct StepRec {
   int64_t M = 0, P = 0;
   uint32_t* in_cell = nullptr;    // [M]
@@ -94,7 +104,7 @@ struct StepRec {
   uint32_t* out_cell = nullptr;   // [P]
   real* out_off = nullptr;        // [D][P]
   uint32_t* emask = nullptr;      // [P]
-  PairCSR<real> ref, res, gap;
+  PairCSR<real, D> ref, res, gap;
 };
 
 // Everything a backward kernel reads, by value.
@@ -106,7 +116,7 @@ struct RecK {
   const uint32_t* inst_base;
   int n_inst;
   real R;
-  StepRec<real> r;
+  StepRec<real, D> r;
 };
 
 template <int Q, int D, class P>
@@ -115,19 +125,30 @@ __device__ __forceinline__ typename P::real rec_fstar(const RecK<Q, D, P>& K, in
   else return __fmaf_rn(K.r.in_rho[m], K.L.wf[k], K.r.fs[(int64_t)k * K.r.M + m]);
 }
 
+// Unit vector of a pair's displacement and its length (subgradient 0 at zero distance).
 template <int D, class real>
-__device__ __forceinline__ real unit_of(const real* e, int64_t n, int64_t p, real (&u)[3]) {
+__device__ __forceinline__ real unit_of(const PairRec<real, D>& pr, real (&u)[3]) {
   real d2 = 0;
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    u[a] = e[(int64_t)a * n + p];
+    u[a] = pr.e[a];
     d2 += u[a] * u[a];
   }
   const real d = sqrt(d2);
-  const real inv = d > (real)0 ? (real)1 / d : (real)0;  // subgradient 0 at zero distance
+  const real inv = d > (real)0 ? (real)1 / d : (real)0;
 #pragma unroll
   for (int a = 0; a < D; ++a) u[a] *= inv;
   return d;
+}
+
+template <int D, class real>
+__device__ __forceinline__ PairRec<real, D> make_rec(uint32_t row, uint32_t item, const real (&e)[3]) {
+  PairRec<real, D> pr;
+  pr.row = row;
+  pr.item = item;
+#pragma unroll
+  for (int a = 0; a < D; ++a) pr.e[a] = e[a];
+  return pr;
 }
 
 // ---- recording kernels (read the step's buffers through Args, see StepHook) --------------------
@@ -153,10 +174,12 @@ __global__ void __launch_bounds__(256) k_rec_thin_cell(const __grid_constant__ A
 }
 
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_rec_cp(const __grid_constant__ Args<Q, D, P> A, StepRec<typename P::real> r) {
+__global__ void __launch_bounds__(256) k_rec_cp(const __grid_constant__ Args<Q, D, P> A, StepRec<typename P::real, D> r,
+                                                uint32_t* __restrict__ cp_of_cell) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < r.P; j += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t F = A.svals[j];
     r.cp_thin[j] = F;
+    cp_of_cell[F] = (uint32_t)j;
     r.cp_n[j] = A.tcnt[F];
     r.cp_moved[j] = __popc(A.mask[F]) > A.kappa_hard ? 1u : 0u;
     r.out_cell[j] = A.b.cell[j];
@@ -174,77 +197,71 @@ __global__ void k_rec_inst_start(const __grid_constant__ Args<Q, D, P> A, uint32
   for (int b = threadIdx.x; b <= A.n_inst; b += blockDim.x) inst_start[b] = A.a.start[A.inst_base[b]];
 }
 
-// Refine pairs of moved CP j: the components within r of its centroid, enumerated exactly as the
-// forward refine decides them (thin cell window, canonical displacement).  FILL = false writes the
-// count of row j into start[j]; FILL = true writes the pairs at start[j]...
+// Refine pairs of moved CP j in direction k (row j*Q + k): the components of direction k within r of
+// its centroid, enumerated exactly as the forward refine decides them (thin cell window, canonical
+// displacement).  FILL = false writes the row's count into start[row]; FILL = true writes the pairs
+// at start[row]...
 template <int Q, int D, class P, bool FILL>
-__global__ void __launch_bounds__(128) k_list_refine(const __grid_constant__ Args<Q, D, P> A,
-                                                     StepRec<typename P::real> r) {
+__global__ void __launch_bounds__(256) k_list_refine(const __grid_constant__ Args<Q, D, P> A,
+                                                     StepRec<typename P::real, D> r) {
   using real = typename P::real;
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
   if (j >= r.P) return;
+  const int64_t rowid = j * Q + k;
   if (!r.cp_moved[j]) {
-    if (!FILL) r.ref.start[j] = 0;
+    if (!FILL) r.ref.start[rowid] = 0;
     return;
   }
   const uint32_t F = r.cp_thin[j];
   const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, F)];
   int Fc[3];
   decode_cell<D>(I, F, Fc);
-  real cen[3] = {0, 0, 0};
+  real cen[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
-  for (int a = 0; a < D; ++a) cen[a] = r.cp_cen[(int64_t)a * r.P + j];
-  uint32_t cnt = 0, pos = FILL ? r.ref.start[j] : 0u;
+  for (int a = 0; a < D; ++a) {
+    cen[a] = r.cp_cen[(int64_t)a * r.P + j];
+    cdk[a] = (real)A.L.cd[k][a];
+    const real base = cen[a] - cdk[a];
+    lo[a] = (int)floor(base - A.R - A.tiny);
+    hi[a] = (int)floor(base + A.R + A.tiny);
+  }
+  uint32_t cnt = 0, pos = FILL ? r.ref.start[rowid] : 0u;
 #pragma unroll 1
-  for (int k = 0; k < Q; ++k) {
-    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    real cdk[3] = {0, 0, 0};
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      cdk[a] = (real)A.L.cd[k][a];
-      const real base = cen[a] - cdk[a];
-      lo[a] = (int)floor(base - A.R - A.tiny);
-      hi[a] = (int)floor(base + A.R + A.tiny);
-    }
+  for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
-    for (int sz = lo[2]; sz <= hi[2]; ++sz)
+    for (int sy = lo[1]; sy <= hi[1]; ++sy)
 #pragma unroll 1
-      for (int sy = lo[1]; sy <= hi[1]; ++sy)
-#pragma unroll 1
-        for (int sx = lo[0]; sx <= hi[0]; ++sx) {
-          const int dS[3] = {sx, sy, sz};
-          real c[3] = {0, 0, 0};
+      for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+        const int dS[3] = {sx, sy, sz};
+        real c[3] = {0, 0, 0};
 #pragma unroll
-          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], cen[a]);
-          if (cell_d2_lower<D, real>(c) > A.R2) continue;
-          uint32_t Sg;
-          if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
-          const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
-          for (uint32_t m = m0; m < m1; ++m) {
-            real o[3] = {0, 0, 0}, e[3];
+        for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], cen[a]);
+        if (cell_d2_lower<D, real>(c) > A.R2) continue;
+        uint32_t Sg;
+        if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
+        const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
+        for (uint32_t m = m0; m < m1; ++m) {
+          real o[3] = {0, 0, 0}, e[3];
 #pragma unroll
-            for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
-            if (canon_d2<D, real>(o, c, e) <= A.R2) {
-              if (FILL) {
-                r.ref.row[pos] = (uint32_t)j;
-                r.ref.item[pos] = m * (uint32_t)Q + (uint32_t)k;
-#pragma unroll
-                for (int a = 0; a < D; ++a) r.ref.e[(int64_t)a * r.ref.n + pos] = e[a];
-                ++pos;
-              }
-              ++cnt;
+          for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+          if (canon_d2<D, real>(o, c, e) <= A.R2) {
+            if (FILL) {
+              r.ref.rec[pos++] = make_rec<D, real>((uint32_t)j, m * (uint32_t)Q + (uint32_t)k, e);
             }
+            ++cnt;
           }
         }
-  }
-  if (!FILL) r.ref.start[j] = cnt;
+      }
+  if (!FILL) r.ref.start[rowid] = cnt;
 }
 
 // Resampling pairs of (CP j, direction k), row j*Q + k: the components of direction k within r of
 // the CP, as the forward gather (and, with the same arithmetic, the weights pass) decides them.
 template <int Q, int D, class P, bool FILL>
 __global__ void __launch_bounds__(256) k_list_resample(const __grid_constant__ Args<Q, D, P> A,
-                                                       StepRec<typename P::real> r) {
+                                                       StepRec<typename P::real, D> r) {
   using real = typename P::real;
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int k = blockIdx.y;
@@ -285,11 +302,7 @@ __global__ void __launch_bounds__(256) k_list_resample(const __grid_constant__ A
           for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
           if (canon_d2<D, real>(o, c, e) <= A.R2) {
             if (FILL) {
-              r.res.row[pos] = (uint32_t)j;
-              r.res.item[pos] = m * (uint32_t)Q + (uint32_t)k;
-#pragma unroll
-              for (int a = 0; a < D; ++a) r.res.e[(int64_t)a * r.res.n + pos] = e[a];
-              ++pos;
+              r.res.rec[pos++] = make_rec<D, real>((uint32_t)j, m * (uint32_t)Q + (uint32_t)k, e);
             }
             ++cnt;
           }
@@ -302,7 +315,7 @@ __global__ void __launch_bounds__(256) k_list_resample(const __grid_constant__ A
 // an empty direction with j.
 template <int Q, int D, class P, bool FILL>
 __global__ void __launch_bounds__(256) k_list_gap(const __grid_constant__ Args<Q, D, P> A,
-                                                  StepRec<typename P::real> r) {
+                                                  StepRec<typename P::real, D> r) {
   using real = typename P::real;
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= r.P) return;
@@ -346,12 +359,8 @@ __global__ void __launch_bounds__(256) k_list_gap(const __grid_constant__ Args<Q
           for (int a = 0; a < D; ++a) o[a] = A.b.off[(int64_t)a * A.ccap + c];
           if (canon_d2<D, real>(o, cc, e) <= A.R2) {
             if (FILL) {
-              r.gap.row[pos] = (uint32_t)j;
-              r.gap.item[pos] = c;
               r.gap.bits[pos] = both;
-#pragma unroll
-              for (int a = 0; a < D; ++a) r.gap.e[(int64_t)a * r.gap.n + pos] = e[a];
-              ++pos;
+              r.gap.rec[pos++] = make_rec<D, real>((uint32_t)j, c, e);
             }
             ++cnt;
           }
@@ -360,20 +369,142 @@ __global__ void __launch_bounds__(256) k_list_gap(const __grid_constant__ Args<Q
   if (!FILL) r.gap.start[j] = cnt;
 }
 
-__global__ void k_iota(uint32_t* __restrict__ v, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    v[i] = (uint32_t)i;
+// Component-side copies of the resampling and refine lists (the transposes), enumerated from each
+// component's own window with the same canonical arithmetic as the CP side, so they hold exactly
+// the same pairs; each component's pairs land in its slot range [tstart[i], tstart[i+1]) (from the
+// CP-side counts) in window order.  A count mismatch would be a bug: it sets *bad and writes nothing
+// out of range.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_tlist_resample(const __grid_constant__ Args<Q, D, P> A,
+                                                        StepRec<typename P::real, D> r, uint32_t* __restrict__ bad) {
+  using real = typename P::real;
+  const int64_t M = r.M, QM = (int64_t)Q * M;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / M);
+    const uint32_t m = (uint32_t)(t - (int64_t)k * M);
+    const uint32_t i = m * (uint32_t)Q + (uint32_t)k;
+    const uint32_t b0 = r.res.tstart[i], b1 = r.res.tstart[i + 1];
+    if (b0 == b1) continue;
+    const uint32_t g = A.a.cell[m];
+    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
+    int Sc[3];
+    decode_cell<D>(I, g, Sc);
+    real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      o[a] = A.a.off[(int64_t)a * A.mcap + m];
+      cdk[a] = (real)A.L.cd[k][a];
+      const real tt = rn_add(o[a], cdk[a]);
+      lo[a] = (int)floor(tt - A.R - A.tiny);
+      hi[a] = (int)floor(tt + A.R + A.tiny);
+    }
+    uint32_t pos = b0;
+#pragma unroll 1
+    for (int gz = lo[2]; gz <= hi[2]; ++gz)
+#pragma unroll 1
+      for (int gy = lo[1]; gy <= hi[1]; ++gy)
+#pragma unroll 1
+        for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+          const int dG[3] = {gx, gy, gz};
+          uint32_t Gg;
+          if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Gg)) continue;
+          const uint32_t c0 = A.b.start[Gg], c1 = A.b.start[Gg + 1];
+          for (uint32_t c = c0; c < c1; ++c) {
+            real cc[3] = {0, 0, 0}, e[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) cc[a] = canon_c<real>(-dG[a], cdk[a], A.b.off[(int64_t)a * A.ccap + c]);
+            if (canon_d2<D, real>(o, cc, e) <= A.R2) {
+              if (pos < b1) r.res.trec[pos] = make_rec<D, real>(c, i, e);
+              ++pos;
+            }
+          }
+        }
+    if (pos != b1) atomicOr(bad, 1u);
+  }
 }
 
-// start[c] = number of sorted keys < c, c in [0, items].
-__global__ void k_start_sorted(const uint32_t* __restrict__ keys, int64_t n, int64_t items, uint32_t* __restrict__ start) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= items; c += (int64_t)gridDim.x * blockDim.x) {
-    int64_t lo = 0, hi = n;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi) >> 1;
-      if (keys[mid] < (uint32_t)c) lo = mid + 1; else hi = mid;
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_tlist_refine(const __grid_constant__ Args<Q, D, P> A,
+                                                      StepRec<typename P::real, D> r,
+                                                      const uint32_t* __restrict__ cp_of_cell, uint32_t* __restrict__ bad) {
+  using real = typename P::real;
+  const int64_t M = r.M, QM = (int64_t)Q * M;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / M);
+    const uint32_t m = (uint32_t)(t - (int64_t)k * M);
+    const uint32_t i = m * (uint32_t)Q + (uint32_t)k;
+    const uint32_t b0 = r.ref.tstart[i], b1 = r.ref.tstart[i + 1];
+    if (b0 == b1) continue;
+    const uint32_t g = A.a.cell[m];
+    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
+    int Sc[3];
+    decode_cell<D>(I, g, Sc);
+    real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      o[a] = A.a.off[(int64_t)a * A.mcap + m];
+      cdk[a] = (real)A.L.cd[k][a];
+      const real tt = rn_add(o[a], cdk[a]);
+      lo[a] = (int)floor(tt - A.R - A.tiny);
+      hi[a] = (int)floor(tt + A.R + A.tiny);
     }
-    start[c] = (uint32_t)lo;
+    uint32_t pos = b0;
+#pragma unroll 1
+    for (int gz = lo[2]; gz <= hi[2]; ++gz)
+#pragma unroll 1
+      for (int gy = lo[1]; gy <= hi[1]; ++gy)
+#pragma unroll 1
+        for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+          const int dG[3] = {gx, gy, gz};
+          uint32_t Fg;
+          if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Fg)) continue;
+          const uint32_t j = cp_of_cell[Fg];
+          if (j == kNone || !r.cp_moved[j]) continue;
+          real c[3] = {0, 0, 0}, e[3];
+#pragma unroll
+          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(-dG[a], cdk[a], r.cp_cen[(int64_t)a * r.P + j]);
+          if (canon_d2<D, real>(o, c, e) <= A.R2) {
+            if (pos < b1) r.ref.trec[pos] = make_rec<D, real>(j, i, e);
+            ++pos;
+          }
+        }
+    if (pos != b1) atomicOr(bad, 1u);
+  }
+}
+
+// Transpose of a pair list (pairs grouped by item, ascending pair index inside each group): integer
+// atomics count and place the pairs, then each group is sorted, so the result does not depend on
+// the order the atomics ran in.
+template <class Rec>
+__global__ void k_item_count(const Rec* __restrict__ rec, int64_t n, uint32_t* __restrict__ cnt) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(cnt + rec[p].item, 1u);
+}
+template <class Rec>
+__global__ void k_item_place(const Rec* __restrict__ rec, int64_t n, const uint32_t* __restrict__ tstart,
+                             uint32_t* __restrict__ fill, Rec* __restrict__ trec) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    Rec q = rec[p];
+    const uint32_t i = q.item;
+    q.item = (uint32_t)p;
+    trec[tstart[i] + atomicAdd(fill + i, 1u)] = q;
+  }
+}
+template <class Rec>
+__global__ void k_item_sort(const uint32_t* __restrict__ tstart, int64_t items, Rec* __restrict__ trec) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < items; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t b0 = tstart[i], b1 = tstart[i + 1];
+    for (uint32_t a = b0 + 1; a < b1; ++a) {  // insertion sort by row-list index (groups hold a few pairs)
+      const Rec v = trec[a];
+      uint32_t c = a;
+      while (c > b0 && trec[c - 1].item > v.item) {
+        trec[c] = trec[c - 1];
+        --c;
+      }
+      trec[c] = v;
+    }
   }
 }
 
@@ -413,7 +544,7 @@ __global__ void __launch_bounds__(256) k_bwd_gap(const __grid_constant__ RecK<Q,
     for (int k = 0; k < Q; ++k) s[k] = 0;
     for (uint32_t p = p0; p < p1; ++p) {
       real u[3];
-      const real w = K.R - unit_of<D, real>(L.e, L.n, p, u);
+      const real w = K.R - unit_of<D, real>(L.rec[p], u);
       const uint32_t bits = L.bits[p];
 #pragma unroll
       for (int k = 0; k < Q; ++k)
@@ -432,7 +563,7 @@ __global__ void __launch_bounds__(256) k_bwd_gap(const __grid_constant__ RecK<Q,
     real xj[3] = {0, 0, 0};
     for (uint32_t p = p0; p < p1; ++p) {
       real u[3];
-      unit_of<D, real>(L.e, L.n, p, u);
+      unit_of<D, real>(L.rec[p], u);
       const uint32_t bits = L.bits[p];
       real c = 0;
 #pragma unroll
@@ -459,10 +590,10 @@ __global__ void __launch_bounds__(256) k_bwd_gap_t(const __grid_constant__ RecK<
     if (q0 == q1) continue;
     real xl[3] = {0, 0, 0};
     for (uint32_t q = q0; q < q1; ++q) {
-      const uint32_t p = L.tperm[q];
+      const auto pr = L.trec[q];
       real u[3];
-      unit_of<D, real>(L.e, L.n, p, u);
-      const real c = cpair[p];
+      unit_of<D, real>(pr, u);
+      const real c = cpair[pr.item];
 #pragma unroll
       for (int a = 0; a < D; ++a) xl[a] -= c * u[a];
     }
@@ -471,94 +602,123 @@ __global__ void __launch_bounds__(256) k_bwd_gap_t(const __grid_constant__ RecK<
   }
 }
 
-// Gather + weights, component side (one thread per input moment, all its directions):
-//   G_i = sum_j a_ij Fbar_jk,  a_ij = (r - d_ij)/sw_i           -> f*bar_i
+// Gather + weights, component side (one thread per component i = (m, k), m fastest):
+//   G_i = sum_j a_ij Fbar_jk,  a_ij = (r - d_ij)/sw_i                  -> f*bar_i
 //   wbar_ij = f*_i / sw_i (Fbar_jk - G_i)   (cotangent of r - d_ij through F and sw)
-//   ybar_i -= sum_j wbar_ij u_ij;  wbar is kept per pair for the CP side.
+//   ybar_i = -sum_j wbar_ij u_ij;  G_i is kept for the CP side
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK<Q, D, P> K,
                                                     const typename P::real* __restrict__ fbarG,
-                                                    typename P::real* __restrict__ fsbar, typename P::real* __restrict__ xbarM,
-                                                    typename P::real* __restrict__ wbar) {
+                                                    typename P::real* __restrict__ fsbar, typename P::real* __restrict__ ybar,
+                                                    typename P::real* __restrict__ Gc) {
   using real = typename P::real;
-  const int64_t M = K.r.M, Pn = K.r.P;
+  const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
   const auto& L = K.r.res;
-  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
-    real xm[3] = {0, 0, 0};
-#pragma unroll 1
-    for (int k = 0; k < Q; ++k) {
-      const int64_t i = m * Q + k;
-      const real inv = K.r.inv_sw[(int64_t)k * M + m];
-      const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
-      real G = 0;
-      if (inv > (real)0) {
-        for (uint32_t q = q0; q < q1; ++q) {
-          const uint32_t p = L.tperm[q];
-          real u[3];
-          const real d = unit_of<D, real>(L.e, L.n, p, u);
-          G += (K.R - d) * inv * fbarG[(int64_t)k * Pn + L.row[p]];
-        }
-      }
-      fsbar[(int64_t)k * M + m] = G;
-      const real fsi = rec_fstar<Q, D, P>(K, m, k) * inv;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / M);
+    const int64_t m = t - (int64_t)k * M;
+    const int64_t i = m * Q + k;
+    const real inv = K.r.inv_sw[t];
+    const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
+    real G = 0;
+    if (inv > (real)0) {
       for (uint32_t q = q0; q < q1; ++q) {
-        const uint32_t p = L.tperm[q];
+        const auto pr = L.trec[q];
         real u[3];
-        unit_of<D, real>(L.e, L.n, p, u);
-        const real wb = inv > (real)0 ? fsi * (fbarG[(int64_t)k * Pn + L.row[p]] - G) : (real)0;
-        wbar[p] = wb;
-#pragma unroll
-        for (int a = 0; a < D; ++a) xm[a] -= wb * u[a];
+        const real d = unit_of<D, real>(pr, u);
+        G += (K.R - d) * inv * fbarG[(int64_t)k * Pn + pr.row];
       }
     }
-#pragma unroll
-    for (int a = 0; a < D; ++a) xbarM[(int64_t)a * M + m] = xm[a];
-  }
-}
-
-// Gather + weights, CP side: p_j receives +wbar_ij u_ij from each of its pairs.
-template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_bwd_gather_cp(const __grid_constant__ RecK<Q, D, P> K,
-                                                       const typename P::real* __restrict__ wbar,
-                                                       typename P::real* __restrict__ xbarP) {
-  using real = typename P::real;
-  const int64_t Pn = K.r.P;
-  const auto& L = K.r.res;
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t p0 = L.start[j * Q], p1 = L.start[(j + 1) * Q];
-    real xj[3] = {0, 0, 0};
-    for (uint32_t p = p0; p < p1; ++p) {
+    fsbar[t] = G;
+    Gc[t] = G;
+    const real fsi = rec_fstar<Q, D, P>(K, m, k) * inv;
+    real y[3] = {0, 0, 0};
+    for (uint32_t q = q0; q < q1; ++q) {
+      const auto pr = L.trec[q];
       real u[3];
-      unit_of<D, real>(L.e, L.n, p, u);
-      const real wb = wbar[p];
+      unit_of<D, real>(pr, u);
+      const real wb = inv > (real)0 ? fsi * (fbarG[(int64_t)k * Pn + pr.row] - G) : (real)0;
 #pragma unroll
-      for (int a = 0; a < D; ++a) xj[a] += wb * u[a];
+      for (int a = 0; a < D; ++a) y[a] -= wb * u[a];
     }
 #pragma unroll
-    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] += xj[a];
+    for (int a = 0; a < D; ++a) ybar[(int64_t)a * QM + t] = y[a];
   }
 }
 
-// Refine, CP side.  A moved CP is p = sum w_i y_i / W (its centroid cancels): keep W and the move
-// s = sum w_i e_i / W for the component side.  An unmoved CP is its centroid: its cotangent goes to
-// the thin cell (already divided by the component count).
+// Per row (CP j, direction k): the CP's share of the resampling pairs (+wbar u, wbar from G of the
+// component side), and for a moved CP
+// the row's part of W = sum w and sum w e over its refine pairs (w = exp(f*)).
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_bwd_refine_cp(const __grid_constant__ RecK<Q, D, P> K,
-                                                       const typename P::real* __restrict__ xbarP,
-                                                       typename P::real* __restrict__ Wj, typename P::real* __restrict__ sj,
-                                                       typename P::real* __restrict__ cenbar, int64_t ncells) {
+__global__ void __launch_bounds__(256) k_bwd_rows(const __grid_constant__ RecK<Q, D, P> K,
+                                                  const typename P::real* __restrict__ Gc,
+                                                  const typename P::real* __restrict__ fbarG,
+                                                  typename P::real* __restrict__ xrow, typename P::real* __restrict__ Wrow,
+                                                  typename P::real* __restrict__ sxrow) {
   using real = typename P::real;
-  const int64_t Pn = K.r.P;
-  const auto& L = K.r.ref;
+  const int64_t M = K.r.M, Pn = K.r.P, PQ = Pn * Q;
+  for (int64_t rw = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; rw < PQ; rw += (int64_t)gridDim.x * blockDim.x) {
+    const auto& L = K.r.res;
+    const int64_t j = rw / Q;
+    const int k = (int)(rw - j * Q);
+    const real fb = fbarG[(int64_t)k * Pn + j];
+    real x[3] = {0, 0, 0};
+    for (uint32_t p = L.start[rw]; p < L.start[rw + 1]; ++p) {
+      const auto pr = L.rec[p];
+      real u[3];
+      unit_of<D, real>(pr, u);
+      const int64_t m = pr.item / Q;
+      const real inv = K.r.inv_sw[(int64_t)k * M + m];
+      const real wb = inv > (real)0 ? rec_fstar<Q, D, P>(K, m, k) * inv * (fb - Gc[(int64_t)k * M + m]) : (real)0;
+#pragma unroll
+      for (int a = 0; a < D; ++a) x[a] += wb * u[a];
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) xrow[(int64_t)a * PQ + rw] = x[a];
+    const auto& R = K.r.ref;
+    real W = 0, sx[3] = {0, 0, 0};
+    for (uint32_t p = R.start[rw]; p < R.start[rw + 1]; ++p) {
+      const auto pr = R.rec[p];
+      const uint32_t i = pr.item;
+      const real w = exp(rec_fstar<Q, D, P>(K, i / Q, (int)(i % Q)));
+      W += w;
+#pragma unroll
+      for (int a = 0; a < D; ++a) sx[a] += w * pr.e[a];
+    }
+    Wrow[rw] = W;
+#pragma unroll
+    for (int a = 0; a < D; ++a) sxrow[(int64_t)a * PQ + rw] = sx[a];
+  }
+}
+
+// Per CP: total cotangent of its position; a moved CP is p = sum w_i y_i / W (its centroid cancels),
+// so keep W and the move s = sum w_i e_i / W for the component side; an unmoved CP is its centroid,
+// whose cotangent goes to the thin cell (already divided by the component count).
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_cp(const __grid_constant__ RecK<Q, D, P> K,
+                                                const typename P::real* __restrict__ xrow, const typename P::real* __restrict__ Wrow,
+                                                const typename P::real* __restrict__ sxrow, typename P::real* __restrict__ xbarP,
+                                                typename P::real* __restrict__ Wj, typename P::real* __restrict__ sj,
+                                                typename P::real* __restrict__ cenbar, int64_t ncells) {
+  using real = typename P::real;
+  const int64_t Pn = K.r.P, PQ = Pn * Q;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
+    real x[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) x[a] = xbarP[(int64_t)a * Pn + j];
+#pragma unroll 1
+    for (int k = 0; k < Q; ++k)
+#pragma unroll
+      for (int a = 0; a < D; ++a) x[a] += xrow[(int64_t)a * PQ + j * Q + k];
+#pragma unroll
+    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] = x[a];
     if (K.r.cp_moved[j]) {
       real W = 0, sx[3] = {0, 0, 0};
-      for (uint32_t p = L.start[j]; p < L.start[j + 1]; ++p) {
-        const uint32_t i = L.item[p];
-        const real w = exp(rec_fstar<Q, D, P>(K, i / Q, (int)(i % Q)));
-        W += w;
+#pragma unroll 1
+      for (int k = 0; k < Q; ++k) {
+        W += Wrow[j * Q + k];
 #pragma unroll
-        for (int a = 0; a < D; ++a) sx[a] += w * L.e[(int64_t)a * L.n + p];
+        for (int a = 0; a < D; ++a) sx[a] += sxrow[(int64_t)a * PQ + j * Q + k];
       }
       Wj[j] = W;
 #pragma unroll
@@ -567,62 +727,78 @@ __global__ void __launch_bounds__(256) k_bwd_refine_cp(const __grid_constant__ R
       const uint32_t F = K.r.cp_thin[j];
       const real invn = (real)1 / (real)K.r.cp_n[j];
 #pragma unroll
-      for (int a = 0; a < D; ++a) cenbar[(int64_t)a * ncells + F] = xbarP[(int64_t)a * Pn + j] * invn;
+      for (int a = 0; a < D; ++a) cenbar[(int64_t)a * ncells + F] = x[a] * invn;
     }
   }
 }
 
-// Component side of refine and thinning, the dispersion sum over directions, and the collision:
+// Component side of refine and thinning (one thread per component, m fastest):
 //   ybar_i += w_i/W_j pbar_j,  f*bar_i += w_i ((e_i - s_j) . pbar_j)/W_j   (refine pairs of i)
 //   ybar_i += cenbar[thin cell of i]                                        (thinning)
-//   xbar_m  = sum_k ybar_(m,k)                                              (y = x + cd_k)
-//   fbar    = (1 - 1/tau) f*bar + (1/tau) J_feq^T f*bar,  taubar_m = -(1/tau^2) f*bar . (feq - f)
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_bwd_comp(const __grid_constant__ RecK<Q, D, P> K,
+                                                  const typename P::real* __restrict__ xbarP,
+                                                  const typename P::real* __restrict__ Wj, const typename P::real* __restrict__ sj,
+                                                  const typename P::real* __restrict__ cenbar, int64_t ncells,
+                                                  typename P::real* __restrict__ fsbar, typename P::real* __restrict__ ybar) {
+  using real = typename P::real;
+  const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
+  const auto& L = K.r.ref;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / M);
+    const int64_t m = t - (int64_t)k * M;
+    const int64_t i = m * Q + k;
+    real y[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) y[a] = ybar[(int64_t)a * QM + t];
+    real g = fsbar[t];
+    const uint32_t F = K.r.thin_cell[t];
+    if (F != kNone) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) y[a] += cenbar[(int64_t)a * ncells + F];
+    }
+    const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
+    if (q0 < q1) {
+      const real w = exp(rec_fstar<Q, D, P>(K, m, k));
+      for (uint32_t q = q0; q < q1; ++q) {
+        const auto pr = L.trec[q];
+        const uint32_t j = pr.row;
+        const real wW = w / Wj[j];
+        real dot = 0;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          const real pb = xbarP[(int64_t)a * Pn + j];
+          y[a] += wW * pb;
+          dot += (pr.e[a] - sj[(int64_t)a * Pn + j]) * pb;
+        }
+        g += wW * dot;
+      }
+    }
+    fsbar[t] = g;
+#pragma unroll
+    for (int a = 0; a < D; ++a) ybar[(int64_t)a * QM + t] = y[a];
+  }
+}
+
+// Per moment: the dispersion sum over directions (y = x + cd_k) and the collision:
+//   xbar_m = sum_k ybar_(m,k)
+//   fbar   = (1 - 1/tau) f*bar + (1/tau) J_feq^T f*bar,  taubar_m = -(1/tau^2) f*bar . (feq - f)
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_moment(const __grid_constant__ RecK<Q, D, P> K,
                                                     const typename P::real* __restrict__ fsbar,
-                                                    const typename P::real* __restrict__ xbarM,
-                                                    const typename P::real* __restrict__ xbarP,
-                                                    const typename P::real* __restrict__ Wj, const typename P::real* __restrict__ sj,
-                                                    const typename P::real* __restrict__ cenbar, int64_t ncells,
+                                                    const typename P::real* __restrict__ ybar,
                                                     double* __restrict__ goff_in, double* __restrict__ gf_in,
                                                     double* __restrict__ taupart) {
   using real = typename P::real;
-  const int64_t M = K.r.M, Pn = K.r.P;
-  const auto& L = K.r.ref;
+  const int64_t M = K.r.M, QM = (int64_t)Q * M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
-    real x[3] = {0, 0, 0};
+    real x[3] = {0, 0, 0}, g[Q];
 #pragma unroll
-    for (int a = 0; a < D; ++a) x[a] = xbarM[(int64_t)a * M + m];
-    real g[Q];
-#pragma unroll 1
     for (int k = 0; k < Q; ++k) {
-      const int64_t i = m * Q + k;
-      real gk = fsbar[(int64_t)k * M + m];
-      const uint32_t F = K.r.thin_cell[(int64_t)k * M + m];
-      if (F != kNone) {
+      g[k] = fsbar[(int64_t)k * M + m];
 #pragma unroll
-        for (int a = 0; a < D; ++a) x[a] += cenbar[(int64_t)a * ncells + F];
-      }
-      const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
-      if (q0 < q1) {
-        const real w = exp(rec_fstar<Q, D, P>(K, m, k));
-        for (uint32_t q = q0; q < q1; ++q) {
-          const uint32_t p = L.tperm[q];
-          const uint32_t j = L.row[p];
-          const real wW = w / Wj[j];
-          real dot = 0;
-#pragma unroll
-          for (int a = 0; a < D; ++a) {
-            const real pb = xbarP[(int64_t)a * Pn + j];
-            x[a] += wW * pb;
-            dot += (L.e[(int64_t)a * L.n + p] - sj[(int64_t)a * Pn + j]) * pb;
-          }
-          gk += wW * dot;
-        }
-      }
-      g[k] = gk;
+      for (int a = 0; a < D; ++a) x[a] += ybar[(int64_t)a * QM + (int64_t)k * M + m];
     }
-    // collision
     const InstK I = K.inst[find_instance(K.inst_base, K.n_inst, K.r.in_cell[m])];
     const real tau = (real)I.tau, itau = (real)1 / tau;
     const real inv = (real)K.L.inv_cs2;
@@ -699,24 +875,45 @@ __global__ void __launch_bounds__(256) k_bwd_moment(const __grid_constant__ RecK
   }
 }
 
-// Per-instance sum of the tau partials in a fixed order (strided per thread, then a tree).
+// Per-instance sum of the tau partials in a fixed order: kTauSplit blocks per instance each sum a
+// fixed strided subset (then a tree), and one thread per instance adds the block sums in order.
+constexpr int kTauSplit = 32;
 __global__ void __launch_bounds__(256) k_bwd_tau(const uint32_t* __restrict__ inst_start, const double* __restrict__ part,
-                                                 double* __restrict__ gtau) {
+                                                 double* __restrict__ blocksum) {
   __shared__ double sh[256];
-  const int b = blockIdx.x;
+  const int b = blockIdx.x / kTauSplit, sblk = blockIdx.x % kTauSplit;
   const uint32_t m0 = inst_start[b], m1 = inst_start[b + 1];
   double s = 0;
-  for (uint32_t m = m0 + threadIdx.x; m < m1; m += blockDim.x) s += part[m];
+  for (uint32_t m = m0 + sblk * 256 + threadIdx.x; m < m1; m += 256 * kTauSplit) s += part[m];
   sh[threadIdx.x] = s;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
     if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) gtau[b] += sh[0];
+  if (threadIdx.x == 0) blocksum[blockIdx.x] = sh[0];
+}
+__global__ void k_bwd_tau_sum(const double* __restrict__ blocksum, int n_inst, double* __restrict__ gtau) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n_inst; b += gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int i = 0; i < kTauSplit; ++i) s += blocksum[b * kTauSplit + i];
+    gtau[b] += s;
+  }
 }
 
-// Export helpers: real -> double, FP32DEV f -> rho*W + dev.
+// Export helpers: real -> double, FP32DEV f -> rho*W + dev, record fields -> arrays.
+template <class real, int D>
+__global__ void k_rec_fields(const PairRec<real, D>* __restrict__ rec, int64_t n, uint32_t* __restrict__ item,
+                             double* __restrict__ e) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const PairRec<real, D> q = rec[p];
+    if (item) item[p] = q.item;
+    if (e) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) e[(int64_t)a * n + p] = (double)q.e[a];
+    }
+  }
+}
 template <class real>
 __global__ void k_to_f64(const real* __restrict__ src, int64_t n, double* __restrict__ dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -751,25 +948,33 @@ template <int Q, int D, class P>
 struct TapeImpl : TapeBase, StepHook {
   using real = typename P::real;
   SimBase* sim;
-  std::vector<StepRec<real>> steps;
+  std::vector<StepRec<real, D>> steps;
   DevArena rec_mem, tmp_mem, bwd_mem;
-  StepRec<real> cur{};
+  StepRec<real, D> cur{};
   LatK<Q, D> L{};
   const InstK* inst = nullptr;
   const uint32_t* inst_base = nullptr;
   int n_inst = 0;
   real R = 0;
   int64_t ncells = 0;
-  double* wk = nullptr;  // W_k in FP64 (export of FP32DEV f)
+  double* wk = nullptr;       // W_k in FP64 (export of FP32DEV f)
+  uint32_t* hbuf = nullptr;   // pinned host words for the counts read back while recording
+  uint32_t* d_bad = nullptr;  // device flag: list orientations disagree
+  bool unchecked = false;
   cudaEvent_t done = nullptr;
 
   explicit TapeImpl(SimBase* s) : sim(s) {}
   ~TapeImpl() override {
     if (done) cudaEventDestroy(done);
+    if (hbuf) cudaFreeHost(hbuf);
+    if (d_bad) cudaFree(d_bad);
   }
 
   int init() {
     DBM_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    DBM_CUDA(cudaMallocHost(&hbuf, 64));
+    DBM_CUDA(cudaMalloc(&d_bad, 4));
+    DBM_CUDA(cudaMemset(d_bad, 0, 4));
     DBM_TRY(rec_mem.get(&wk, Q));
     return DBM_OK;
   }
@@ -790,22 +995,17 @@ struct TapeImpl : TapeBase, StepHook {
   }
 
   int step(cudaStream_t s) override {
-    cur = StepRec<real>{};
+    cur = StepRec<real, D>{};
     DBM_TRY(sim->step_hooked(this, s));
     steps.push_back(cur);
-    DBM_CUDA(cudaStreamSynchronize(s));
     return DBM_OK;
   }
 
-  static uint32_t read_u32(const uint32_t* d, cudaStream_t s, int* rc) {
-    uint32_t h = 0;
-    cudaError_t e = cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-      set_last_error("tape: %s", cudaGetErrorString(e));
-      *rc = DBM_ERR_CUDA;
-    }
-    return h;
+  // Copy n device words into hbuf[0..n) and wait for them.
+  int fetch(const uint32_t* const* src, int n, cudaStream_t s) {
+    for (int i = 0; i < n; ++i) DBM_CUDA(cudaMemcpyAsync(hbuf + i, src[i], 4, cudaMemcpyDeviceToHost, s));
+    DBM_CUDA(cudaStreamSynchronize(s));
+    return DBM_OK;
   }
 
   int before(const void* av, cudaStream_t s) override {
@@ -816,11 +1016,16 @@ struct TapeImpl : TapeBase, StepHook {
     n_inst = A.n_inst;
     R = A.R;
     ncells = A.ncells;
+    const uint32_t* src[2] = {A.a.count, d_bad};  // the previous step's list check rides along
+    DBM_TRY(fetch(src, 2, s));
+    const uint32_t M = hbuf[0];
+    unchecked = false;
+    if (hbuf[1]) {
+      set_last_error("tape: the two orientations of a neighbour list disagree");
+      return DBM_ERR_STATE;
+    }
     if (wk) DBM_CUDA(cudaMemcpyAsync(wk, L.w, sizeof(double) * Q, cudaMemcpyHostToDevice, s));
-    int rc = DBM_OK;
-    const uint32_t M = read_u32(A.a.count, s, &rc);
-    DBM_TRY(rc);
-    StepRec<real>& r = cur;
+    StepRec<real, D>& r = cur;
     r.M = M;
     DBM_TRY(rec_mem.get(&r.in_cell, M));
     DBM_TRY(rec_mem.get(&r.in_off, (int64_t)D * M));
@@ -845,69 +1050,65 @@ struct TapeImpl : TapeBase, StepHook {
     return DBM_OK;
   }
 
-  // Count, scan and fill one pair list, then build its transpose.
-  template <class Count, class Fill>
-  int build_list(PairCSR<real>& Lst, int64_t rows, int64_t items, bool with_bits, Count&& count, Fill&& fill,
-                 cudaStream_t s) {
+  // First half of a pair list: per-row counts (by `count`), scanned in place into start[].
+  template <class Count>
+  int list_count(PairCSR<real, D>& Lst, int64_t rows, int64_t items, bool with_bits, Count&& count, cudaStream_t s) {
     Lst.rows = rows;
     Lst.items = items;
+    (void)with_bits;
     DBM_TRY(rec_mem.get(&Lst.start, rows + 1));
     DBM_CUDA(cudaMemsetAsync(Lst.start + rows, 0, 4, s));
     DBM_TRY(count());
-    void* stmp;
-    DBM_TRY(tmp_mem.get((char**)&stmp, (int64_t)scan_tmp_bytes(rows + 1)));
+    char* stmp;
+    DBM_TRY(tmp_mem.get(&stmp, (int64_t)scan_tmp_bytes(rows + 1)));
     DBM_TRY(scan_exclusive_u32(Lst.start, Lst.start, rows + 1, nullptr, nullptr, stmp, s));
-    int rc = DBM_OK;
-    const uint32_t n = read_u32(Lst.start + rows, s, &rc);
-    DBM_TRY(rc);
-    Lst.n = n;
-    DBM_TRY(rec_mem.get(&Lst.row, n));
-    DBM_TRY(rec_mem.get(&Lst.item, n));
-    DBM_TRY(rec_mem.get(&Lst.e, (int64_t)D * n));
+    return DBM_OK;
+  }
+
+  // Second half, once Lst.n is known: fill the pairs (by `fill`), count the pairs of every item and
+  // build the transpose, by `tfill` when given (a component-side enumeration), else by placing the
+  // records with integer atomics and sorting each item's group.
+  template <class Fill, class TFill>
+  int list_fill(PairCSR<real, D>& Lst, bool with_bits, Fill&& fill, TFill&& tfill, bool have_tfill, cudaStream_t s) {
+    const int64_t n = Lst.n, items = Lst.items;
+    DBM_TRY(rec_mem.get(&Lst.rec, n));
     if (with_bits) DBM_TRY(rec_mem.get(&Lst.bits, n));
-    DBM_TRY(rec_mem.get(&Lst.tperm, n));
+    DBM_TRY(rec_mem.get(&Lst.trec, n));
     DBM_TRY(rec_mem.get(&Lst.tstart, items + 1));
-    if (n > 0) DBM_TRY(fill());
-    // transpose: stable sort of (item, pair index)
-    uint32_t *k0, *v0, *k1, *v1;
-    DBM_TRY(tmp_mem.get(&k0, n));
-    DBM_TRY(tmp_mem.get(&v0, n));
-    DBM_TRY(tmp_mem.get(&k1, n));
-    DBM_TRY(tmp_mem.get(&v1, n));
-    char* rtmp;
-    DBM_TRY(tmp_mem.get(&rtmp, (int64_t)radix_tmp_bytes(std::max<int64_t>(n, 1))));
-    const uint32_t* ks = k0;
-    const uint32_t* vs = v0;
+    uint32_t* cnt;
+    DBM_TRY(tmp_mem.get(&cnt, items + 1));
+    DBM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(items + 1) * 4, s));
     if (n > 0) {
-      DBM_CUDA(cudaMemcpyAsync(k0, Lst.item, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-      k_iota<<<grid_for(n), 256, 0, s>>>(v0, n);
+      DBM_TRY(fill());
+      k_item_count<<<grid_for(n), 256, 0, s>>>(Lst.rec, n, cnt);
       DBM_LAUNCH_CHECK();
-      int bits = 1;
-      while (bits < 32 && ((int64_t)1 << bits) <= items) ++bits;
-      bool alt = false;
-      DBM_TRY(radix_sort_pairs<uint32_t>(k0, v0, k1, v1, n, nullptr, bits, rtmp, s, &alt));
-      ks = alt ? k1 : k0;
-      vs = alt ? v1 : v0;
-      DBM_CUDA(cudaMemcpyAsync(Lst.tperm, vs, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     }
-    k_start_sorted<<<grid_for(items + 1), 256, 0, s>>>(ks, n, items, Lst.tstart);
+    char* stmp;
+    DBM_TRY(tmp_mem.get(&stmp, (int64_t)scan_tmp_bytes(items + 1)));
+    DBM_TRY(scan_exclusive_u32(cnt, Lst.tstart, items + 1, nullptr, nullptr, stmp, s));
+    if (n == 0) return DBM_OK;
+    if (have_tfill) return tfill();
+    DBM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)items * 4, s));
+    k_item_place<<<grid_for(n), 256, 0, s>>>(Lst.rec, n, Lst.tstart, cnt, Lst.trec);
+    DBM_LAUNCH_CHECK();
+    k_item_sort<<<grid_for(items), 256, 0, s>>>(Lst.tstart, items, Lst.trec);
     DBM_LAUNCH_CHECK();
     return DBM_OK;
   }
 
   int after(const void* av, cudaStream_t s) override {
     const Args<Q, D, P>& A = *(const Args<Q, D, P>*)av;
-    StepRec<real>& r = cur;
+    StepRec<real, D>& r = cur;
     tmp_mem.reset();
-    int rc = DBM_OK;
-    const uint32_t st = read_u32(A.status, s, &rc);
-    DBM_TRY(rc);
-    if (st & ST_NONFINITE) {
+    {
+      const uint32_t* src[2] = {A.status, A.d_P};
+      DBM_TRY(fetch(src, 2, s));
+    }
+    if (hbuf[0] & ST_NONFINITE) {
       set_last_error("tape: the step produced a non-finite refine move; it has no derivative");
       return DBM_ERR_INVALID;
     }
-    r.P = read_u32(A.d_P, s, &rc);
-    DBM_TRY(rc);
+    r.P = hbuf[1];
     const int64_t M = r.M, Pn = r.P;
     if (M > 0) {
       if constexpr (std::is_same<P, PF64>::value) {
@@ -931,53 +1132,78 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_TRY(rec_mem.get(&r.out_cell, Pn));
     DBM_TRY(rec_mem.get(&r.out_off, (int64_t)D * Pn));
     DBM_TRY(rec_mem.get(&r.emask, Pn));
+    uint32_t* cp_of_cell;
+    DBM_TRY(tmp_mem.get(&cp_of_cell, ncells));
+    DBM_CUDA(cudaMemsetAsync(cp_of_cell, 0xff, (size_t)ncells * 4, s));
     if (Pn > 0) {
-      k_rec_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(A, r);
+      k_rec_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(A, r, cp_of_cell);
       DBM_LAUNCH_CHECK();
     }
-    const unsigned gp = div_up(std::max<int64_t>(Pn, 1), 128);
-    // refine pairs (rows: CPs)
-    DBM_TRY(build_list(r.ref, Pn, (int64_t)Q * M, false,
-                       [&]() -> int {
-                         if (Pn > 0) { k_list_refine<Q, D, P, false><<<gp, 128, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
-                         return DBM_OK;
-                       },
-                       [&]() -> int {
-                         k_list_refine<Q, D, P, true><<<gp, 128, 0, s>>>(A, r);
-                         DBM_LAUNCH_CHECK();
-                         return DBM_OK;
-                       },
-                       s));
-    // resampling pairs (rows: CP x direction)
-    const dim3 gr(div_up(std::max<int64_t>(Pn, 1), 256), Q);
-    DBM_TRY(build_list(r.res, Pn * Q, (int64_t)Q * M, false,
-                       [&]() -> int {
-                         if (Pn > 0) { k_list_resample<Q, D, P, false><<<gr, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
-                         return DBM_OK;
-                       },
-                       [&]() -> int {
-                         k_list_resample<Q, D, P, true><<<gr, 256, 0, s>>>(A, r);
-                         DBM_LAUNCH_CHECK();
-                         return DBM_OK;
-                       },
-                       s));
-    // gap-fill pairs (rows: CPs, items: CPs)
-    const unsigned gg = div_up(std::max<int64_t>(Pn, 1), 256);
-    DBM_TRY(build_list(r.gap, Pn, Pn, true,
-                       [&]() -> int {
-                         if (Pn > 0) { k_list_gap<Q, D, P, false><<<gg, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
-                         return DBM_OK;
-                       },
-                       [&]() -> int {
-                         k_list_gap<Q, D, P, true><<<gg, 256, 0, s>>>(A, r);
-                         DBM_LAUNCH_CHECK();
-                         return DBM_OK;
-                       },
-                       s));
+    // the three lists: counts first (rows: CP x direction for refine and resampling, CP for gap fill)
+    const dim3 grq(div_up(std::max<int64_t>(Pn, 1), 256), Q);
+    const unsigned gp = div_up(std::max<int64_t>(Pn, 1), 256);
+    DBM_TRY(list_count(r.ref, Pn * Q, (int64_t)Q * M, false, [&]() -> int {
+      if (Pn > 0) { k_list_refine<Q, D, P, false><<<grq, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
+      return DBM_OK;
+    }, s));
+    DBM_TRY(list_count(r.res, Pn * Q, (int64_t)Q * M, false, [&]() -> int {
+      if (Pn > 0) { k_list_resample<Q, D, P, false><<<grq, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
+      return DBM_OK;
+    }, s));
+    DBM_TRY(list_count(r.gap, Pn, Pn, true, [&]() -> int {
+      if (Pn > 0) { k_list_gap<Q, D, P, false><<<gp, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
+      return DBM_OK;
+    }, s));
+    {
+      const uint32_t* src[3] = {r.ref.start + Pn * Q, r.res.start + Pn * Q, r.gap.start + Pn};
+      DBM_TRY(fetch(src, 3, s));
+    }
+    r.ref.n = hbuf[0];
+    r.res.n = hbuf[1];
+    r.gap.n = hbuf[2];
+    const auto none = []() -> int { return DBM_OK; };
+    DBM_TRY(list_fill(r.ref, false, [&]() -> int {
+      k_list_refine<Q, D, P, true><<<grq, 256, 0, s>>>(A, r);
+      DBM_LAUNCH_CHECK();
+      return DBM_OK;
+    }, [&]() -> int {
+      k_tlist_refine<Q, D, P><<<grid_for((int64_t)Q * M), 256, 0, s>>>(A, r, cp_of_cell, d_bad);
+      DBM_LAUNCH_CHECK();
+      return DBM_OK;
+    }, true, s));
+    DBM_TRY(list_fill(r.res, false, [&]() -> int {
+      k_list_resample<Q, D, P, true><<<grq, 256, 0, s>>>(A, r);
+      DBM_LAUNCH_CHECK();
+      return DBM_OK;
+    }, [&]() -> int {
+      k_tlist_resample<Q, D, P><<<grid_for((int64_t)Q * M), 256, 0, s>>>(A, r, d_bad);
+      DBM_LAUNCH_CHECK();
+      return DBM_OK;
+    }, true, s));
+    DBM_TRY(list_fill(r.gap, true, [&]() -> int {
+      k_list_gap<Q, D, P, true><<<gp, 256, 0, s>>>(A, r);
+      DBM_LAUNCH_CHECK();
+      return DBM_OK;
+    }, none, false, s));
+    unchecked = true;
     return DBM_OK;
   }
 
-  RecK<Q, D, P> reck(const StepRec<real>& r) const {
+  // The component-side enumerations flag a count that differs from the CP side's (a bug, never an
+  // input condition); read that flag.
+  int check_lists(cudaStream_t s) {
+    if (!unchecked) return DBM_OK;
+    const uint32_t* src[1] = {d_bad};
+    DBM_TRY(fetch(src, 1, s));
+    unchecked = false;
+    if (hbuf[0]) {
+      set_last_error("tape: the two orientations of a neighbour list disagree");
+      return DBM_ERR_STATE;
+    }
+    return DBM_OK;
+  }
+
+  RecK<Q, D, P> reck(const StepRec<real, D>& r) const {
     RecK<Q, D, P> K;
     K.L = L;
     K.inst = inst;
@@ -991,26 +1217,31 @@ struct TapeImpl : TapeBase, StepHook {
   int backward(int idx, const double* goff_out, const double* gf_out, double* goff_in, double* gf_in, double* gtau,
                cudaStream_t s) override {
     if (idx < 0 || idx >= (int)steps.size()) { set_last_error("tape: no step %d", idx); return DBM_ERR_INVALID; }
-    const StepRec<real>& r = steps[idx];
-    const int64_t M = r.M, Pn = r.P;
+    const StepRec<real, D>& r = steps[idx];
+    const int64_t M = r.M, Pn = r.P, QM = (int64_t)Q * M, PQ = Pn * Q;
     if ((Pn > 0 && (!goff_out || !gf_out)) || (M > 0 && (!goff_in || !gf_in)) || !gtau) {
       set_last_error("tape backward: null cotangent");
       return DBM_ERR_INVALID;
     }
+    DBM_TRY(check_lists(s));
     DBM_CUDA(cudaStreamWaitEvent(s, done, 0));  // the previous call's scratch is free
     bwd_mem.reset();
-    real *xbarP, *fbarG, *cpair, *fsbar, *xbarM, *wbar, *Wj, *sj, *cenbar;
-    double* taupart;
+    real *xbarP, *fbarG, *cpair, *fsbar, *ybar, *Gc, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
+    double *taupart, *blocksum;
     DBM_TRY(bwd_mem.get(&xbarP, (int64_t)D * Pn));
     DBM_TRY(bwd_mem.get(&fbarG, (int64_t)Q * Pn));
     DBM_TRY(bwd_mem.get(&cpair, r.gap.n));
-    DBM_TRY(bwd_mem.get(&fsbar, (int64_t)Q * M));
-    DBM_TRY(bwd_mem.get(&xbarM, (int64_t)D * M));
-    DBM_TRY(bwd_mem.get(&wbar, r.res.n));
+    DBM_TRY(bwd_mem.get(&fsbar, QM));
+    DBM_TRY(bwd_mem.get(&ybar, (int64_t)D * QM));
+    DBM_TRY(bwd_mem.get(&Gc, QM));
+    DBM_TRY(bwd_mem.get(&xrow, (int64_t)D * PQ));
+    DBM_TRY(bwd_mem.get(&Wrow, PQ));
+    DBM_TRY(bwd_mem.get(&sxrow, (int64_t)D * PQ));
     DBM_TRY(bwd_mem.get(&Wj, Pn));
     DBM_TRY(bwd_mem.get(&sj, (int64_t)D * Pn));
     DBM_TRY(bwd_mem.get(&cenbar, (int64_t)D * ncells));
     DBM_TRY(bwd_mem.get(&taupart, M));
+    DBM_TRY(bwd_mem.get(&blocksum, (int64_t)n_inst * kTauSplit));
     const RecK<Q, D, P> K = reck(r);
     DBM_CUDA(cudaMemsetAsync(cenbar, 0, sizeof(real) * (size_t)D * ncells, s));
     if (Pn > 0) {
@@ -1024,29 +1255,44 @@ struct TapeImpl : TapeBase, StepHook {
       }
     }
     if (M > 0) {
-      k_bwd_gather<Q, D, P><<<grid_for(M), 256, 0, s>>>(K, fbarG, fsbar, xbarM, wbar);
+      k_bwd_gather<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, fbarG, fsbar, ybar, Gc);
       DBM_LAUNCH_CHECK();
     }
     if (Pn > 0) {
-      k_bwd_gather_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, wbar, xbarP);
+      k_bwd_rows<Q, D, P><<<grid_for(PQ), 256, 0, s>>>(K, Gc, fbarG, xrow, Wrow, sxrow);
       DBM_LAUNCH_CHECK();
-      k_bwd_refine_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xbarP, Wj, sj, cenbar, ncells);
+      k_bwd_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xrow, Wrow, sxrow, xbarP, Wj, sj, cenbar, ncells);
       DBM_LAUNCH_CHECK();
     }
     if (M > 0) {
-      k_bwd_moment<Q, D, P><<<grid_for(M), 256, 0, s>>>(K, fsbar, xbarM, xbarP, Wj, sj, cenbar, ncells, goff_in, gf_in,
-                                                        taupart);
+      k_bwd_comp<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, xbarP, Wj, sj, cenbar, ncells, fsbar, ybar);
       DBM_LAUNCH_CHECK();
-      k_bwd_tau<<<n_inst, 256, 0, s>>>(r.inst_start, taupart, gtau);
+      k_bwd_moment<Q, D, P><<<grid_for(M), 256, 0, s>>>(K, fsbar, ybar, goff_in, gf_in, taupart);
+      DBM_LAUNCH_CHECK();
+      k_bwd_tau<<<n_inst * kTauSplit, 256, 0, s>>>(r.inst_start, taupart, blocksum);
+      DBM_LAUNCH_CHECK();
+      k_bwd_tau_sum<<<div_up(n_inst, 256), 256, 0, s>>>(blocksum, n_inst, gtau);
       DBM_LAUNCH_CHECK();
     }
     DBM_CUDA(cudaEventRecord(done, s));
     return DBM_OK;
   }
 
+  // The items (u32[n]) or the displacements (f64[D][n]) of a recorded list, in row order.
+  int export_list(const PairCSR<real, D>& Lst, bool disp, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) {
+    const int64_t sz = Lst.n * (disp ? 8 * D : 4);
+    if (needed) *needed = sz;
+    if (!dst || Lst.n == 0) return DBM_OK;
+    if (nbytes < sz) { set_last_error("tape export: destination too small"); return DBM_ERR_INVALID; }
+    k_rec_fields<real, D><<<grid_for(Lst.n), 256, 0, s>>>(Lst.rec, Lst.n, disp ? nullptr : (uint32_t*)dst,
+                                                        disp ? (double*)dst : nullptr);
+    DBM_LAUNCH_CHECK();
+    return DBM_OK;
+  }
+
   int export_(int idx, int what, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) override {
     if (idx < 0 || idx >= (int)steps.size()) { set_last_error("tape: no step %d", idx); return DBM_ERR_INVALID; }
-    const StepRec<real>& r = steps[idx];
+    const StepRec<real, D>& r = steps[idx];
     const void* src = nullptr;
     int64_t n = 0;
     bool conv = false;  // real -> f64
@@ -1064,16 +1310,16 @@ struct TapeImpl : TapeBase, StepHook {
       case DBM_TAPE_OUT_OFF: src = r.out_off; n = (int64_t)D * r.P; conv = true; break;
       case DBM_TAPE_EMPTY: src = r.emask; n = r.P; break;
       case DBM_TAPE_INV_SW: src = r.inv_sw; n = (int64_t)Q * r.M; conv = true; break;
-      case DBM_TAPE_REFINE_START: src = r.ref.start; n = r.P + 1; break;
-      case DBM_TAPE_REFINE_ITEM: src = r.ref.item; n = r.ref.n; break;
-      case DBM_TAPE_REFINE_E: src = r.ref.e; n = (int64_t)D * r.ref.n; conv = true; break;
+      case DBM_TAPE_REFINE_START: src = r.ref.start; n = r.P * Q + 1; break;
+      case DBM_TAPE_REFINE_ITEM: return export_list(r.ref, false, dst, nbytes, needed, s);
+      case DBM_TAPE_REFINE_E: return export_list(r.ref, true, dst, nbytes, needed, s);
       case DBM_TAPE_RES_START: src = r.res.start; n = r.P * Q + 1; break;
-      case DBM_TAPE_RES_ITEM: src = r.res.item; n = r.res.n; break;
-      case DBM_TAPE_RES_E: src = r.res.e; n = (int64_t)D * r.res.n; conv = true; break;
+      case DBM_TAPE_RES_ITEM: return export_list(r.res, false, dst, nbytes, needed, s);
+      case DBM_TAPE_RES_E: return export_list(r.res, true, dst, nbytes, needed, s);
       case DBM_TAPE_GAP_START: src = r.gap.start; n = r.P + 1; break;
-      case DBM_TAPE_GAP_ITEM: src = r.gap.item; n = r.gap.n; break;
+      case DBM_TAPE_GAP_ITEM: return export_list(r.gap, false, dst, nbytes, needed, s);
       case DBM_TAPE_GAP_BITS: src = r.gap.bits; n = r.gap.n; break;
-      case DBM_TAPE_GAP_E: src = r.gap.e; n = (int64_t)D * r.gap.n; conv = true; break;
+      case DBM_TAPE_GAP_E: return export_list(r.gap, true, dst, nbytes, needed, s);
       case DBM_TAPE_INST_START: src = r.inst_start; n = n_inst + 1; break;
       default: set_last_error("tape export: unknown array %d", what); return DBM_ERR_INVALID;
     }

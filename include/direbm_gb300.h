@@ -191,8 +191,8 @@ int dbm_sim_restore(dbm_sim* sim, const void* d_src, int64_t bytes, void* stream
  * reference, idea.md:250) ---------------------------------------------------------------------
  * A tape records steps of a simulator: the input moments, the collided f, each component's thin
  * cell, each control point's thin cell / count / centroid / refine decision, and three neighbour
- * lists -- refine (control point -> components within r of its centroid, moved points only),
- * resample (control point and direction -> components within r) and gap fill (control point ->
+ * lists -- refine (control point and direction -> components within r of its centroid, moved
+ * points only), resample (control point and direction -> components within r) and gap fill (control point ->
  * control points within r sharing an empty direction) -- with the displacement of every pair as
  * the forward step computed it.  dbm_tape_backward applies the transpose of the step's Jacobian
  * with those discrete decisions held fixed (a hand-written vector-Jacobian product of the
@@ -230,7 +230,7 @@ int dbm_tape_export(dbm_tape* tape, int32_t index, int32_t what, void* d_dst, in
 #define DBM_TAPE_OUT_OFF 11      /* f64[D][P] */
 #define DBM_TAPE_EMPTY 12        /* u32[P] gap-filled directions (bit k) */
 #define DBM_TAPE_INV_SW 13       /* f64[Q][M] 1/sw per component (0 if dropped) */
-#define DBM_TAPE_REFINE_START 14 /* u32[P+1] */
+#define DBM_TAPE_REFINE_START 14 /* u32[P*Q+1], row j*Q + k */
 #define DBM_TAPE_REFINE_ITEM 15  /* u32[n] component m*Q + k */
 #define DBM_TAPE_REFINE_E 16     /* f64[D][n] component minus centroid */
 #define DBM_TAPE_RES_START 17    /* u32[P*Q+1], row j*Q + k */

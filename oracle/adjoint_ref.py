@@ -54,8 +54,8 @@ def tape_from_oracle(spec: gs.GridSpec, st: gs.GridState) -> tuple[dict, gs.Grid
     sorted_of_thin = np.full(len(cells), -1, dtype=np.int64)
     sorted_of_thin[order] = np.arange(P)
     keep = (sorted_of_thin[pj] >= 0) & moved_thin[pj]
-    rows = sorted_of_thin[pj[keep]]
-    rstart, rord = _csr(rows, P)
+    rows = sorted_of_thin[pj[keep]] * Q + comps[1][ci[keep]]
+    rstart, rord = _csr(rows, P * Q)
     # resampling pairs
     cp_cell, cp_off = nxt.cell, nxt.off
     ci2, pj2, d2, e2, _ = gs._pairs_comp_cp(spec, st, cp_cell, cp_off, comps)
@@ -162,8 +162,8 @@ def step_fixed(T: dict, lattice, R: float, base, rho_rest, off_in, f_in, tau):
     jt = srt[loc[comp]]
     dcen = torch.zeros((P, D), dtype=torch.float64).index_add_(0, torch.as_tensor(jt), dX[torch.as_tensor(comp // Q)])
     dcen = dcen / torch.as_tensor(np.asarray(T["cp_count"]), dtype=torch.float64).clamp(min=1)[:, None]
-    # refine: p = cen + sum w e / sum w for the moved CPs
-    rrow = torch.as_tensor(_rows(T["ref_start"]))
+    # refine: p = cen + sum w e / sum w for the moved CPs (rows are CP x direction)
+    rrow = torch.as_tensor(_rows(T["ref_start"]) // Q)
     ritem = np.asarray(T["ref_item"])
     rm, rk = torch.as_tensor(ritem // Q), torch.as_tensor(ritem % Q)
     e_r = torch.as_tensor(T["ref_e"]) + dX[rm] - dcen[rrow]
