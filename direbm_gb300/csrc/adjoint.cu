@@ -17,8 +17,9 @@
 //   F_jk  = sum over resample pairs (i, j), k_i = k, of (r - |y_i - p_j|) / sw_i * f*_i
 //   F_jk  = r rho_rest W_k / sum over gap pairs (j, l) of (r - |p_l - p_j|)      (filled entries)
 // and the next state is (p_j, F_j).  dbm_tape_backward applies the transpose of its Jacobian,
-// pair by pair, in fixed order (no float atomics): every accumulation is owned by one thread,
-// scatters go through the lists' transposes (stable radix sort of each list by its item).
+// pair by pair, in fixed order (no float atomics): every accumulation is owned by one thread, and
+// every neighbour list is recorded in both orientations (by control point and by component), each
+// enumerated on its own side with the same canonical arithmetic, so scatters become gathers.
 // |y - p| has the subgradient 0 at zero distance.
 #include <algorithm>
 #include <vector>
@@ -67,8 +68,7 @@ struct DevArena {
 
 // One recorded pair: the reference point (row: a CP), the other end (item: a component m*Q + k, or
 // a neighbour CP in the gap fill) and the displacement e = other end - reference point exactly as
-// the step computed it.  One record is one aligned store / load (16 bytes for FP32 in 2D).  In a
-// transposed list `item` holds the pair's index in the row-ordered list instead.
+// the step computed it.  One record is one aligned store / load (16 bytes for FP32 in 2D).
 template <class real, int D>
 struct alignas((sizeof(real) * D + 8) <= 16 ? 16 : 8) PairRec {
   uint32_t row;
@@ -76,14 +76,23 @@ struct alignas((sizeof(real) * D + 8) <= 16 ? 16 : 8) PairRec {
   real e[D];
 };
 
+// A pair list: row r's pairs are rec[start[r] .. start[r] + cnt[r]).  Rows reserve their slots as
+// they are enumerated, so where a row sits in rec varies from run to run; what it holds does not.
+template <class real, int D>
+struct PairList {
+  int64_t rows = 0, n = 0, cap = 0;
+  uint32_t* start = nullptr;         // [rows]
+  uint32_t* cnt = nullptr;           // [rows]
+  PairRec<real, D>* rec = nullptr;   // [cap]
+  uint32_t* bits = nullptr;          // [cap] gap fill, CP side: directions empty in both CPs
+};
+
+// Both orientations of one neighbour relation: f by reference point (rows CP x direction; gap fill:
+// the filled CP), t by the other end (rows component k*M + m; gap fill: the neighbour CP, whose
+// records hold row = filled CP, item = the shared empty directions).
 template <class real, int D>
 struct PairCSR {
-  int64_t rows = 0, items = 0, n = 0;
-  uint32_t* start = nullptr;         // [rows + 1]
-  PairRec<real, D>* rec = nullptr;   // [n] grouped by row
-  uint32_t* bits = nullptr;          // [n] gap fill only: directions empty in both CPs
-  PairRec<real, D>* trec = nullptr;  // [n] grouped by item, ascending row-list index inside a group
-  uint32_t* tstart = nullptr;        // [items + 1]
+  PairList<real, D> f, t;
 };
 
 template <class real, int D>
@@ -174,7 +183,8 @@ __global__ void __launch_bounds__(256) k_rec_thin_cell(const __grid_constant__ A
 }
 
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_rec_cp(const __grid_constant__ Args<Q, D, P> A, StepRec<typename P::real, D> r,
+__global__ void __launch_bounds__(256) k_rec_cp(const __grid_constant__ Args<Q, D, P> A,
+                                                const __grid_constant__ StepRec<typename P::real, D> r,
                                                 uint32_t* __restrict__ cp_of_cell) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < r.P; j += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t F = A.svals[j];
@@ -197,22 +207,17 @@ __global__ void k_rec_inst_start(const __grid_constant__ Args<Q, D, P> A, uint32
   for (int b = threadIdx.x; b <= A.n_inst; b += blockDim.x) inst_start[b] = A.a.start[A.inst_base[b]];
 }
 
-// Refine pairs of moved CP j in direction k (row j*Q + k): the components of direction k within r of
-// its centroid, enumerated exactly as the forward refine decides them (thin cell window, canonical
-// displacement).  FILL = false writes the row's count into start[row]; FILL = true writes the pairs
-// at start[row]...
-template <int Q, int D, class P, bool FILL>
-__global__ void __launch_bounds__(256) k_list_refine(const __grid_constant__ Args<Q, D, P> A,
-                                                     StepRec<typename P::real, D> r) {
+// ---- neighbour lists ---------------------------------------------------------------------------
+// Each enumeration visits one row's pairs with exactly the arithmetic of the forward decision it
+// restates (canonical displacement, inclusive radius test) and calls emit(other end, e) per pair.
+
+// Refine, CP side, row (CP j, direction k): the components of direction k within r of the centroid
+// of moved CP j (the forward refine's window around the thin cell).
+template <int Q, int D, class P, class Emit>
+__device__ __forceinline__ uint32_t enum_refine_cp(const Args<Q, D, P>& A, const StepRec<typename P::real, D>& r,
+                                                   int64_t j, int k, Emit&& emit) {
   using real = typename P::real;
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
-  if (j >= r.P) return;
-  const int64_t rowid = j * Q + k;
-  if (!r.cp_moved[j]) {
-    if (!FILL) r.ref.start[rowid] = 0;
-    return;
-  }
+  if (!r.cp_moved[j]) return 0;
   const uint32_t F = r.cp_thin[j];
   const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, F)];
   int Fc[3];
@@ -227,7 +232,7 @@ __global__ void __launch_bounds__(256) k_list_refine(const __grid_constant__ Arg
     lo[a] = (int)floor(base - A.R - A.tiny);
     hi[a] = (int)floor(base + A.R + A.tiny);
   }
-  uint32_t cnt = 0, pos = FILL ? r.ref.start[rowid] : 0u;
+  uint32_t cnt = 0;
 #pragma unroll 1
   for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
@@ -247,26 +252,19 @@ __global__ void __launch_bounds__(256) k_list_refine(const __grid_constant__ Arg
 #pragma unroll
           for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
           if (canon_d2<D, real>(o, c, e) <= A.R2) {
-            if (FILL) {
-              r.ref.rec[pos++] = make_rec<D, real>((uint32_t)j, m * (uint32_t)Q + (uint32_t)k, e);
-            }
+            emit(m * (uint32_t)Q + (uint32_t)k, e);
             ++cnt;
           }
         }
       }
-  if (!FILL) r.ref.start[rowid] = cnt;
+  return cnt;
 }
 
-// Resampling pairs of (CP j, direction k), row j*Q + k: the components of direction k within r of
-// the CP, as the forward gather (and, with the same arithmetic, the weights pass) decides them.
-template <int Q, int D, class P, bool FILL>
-__global__ void __launch_bounds__(256) k_list_resample(const __grid_constant__ Args<Q, D, P> A,
-                                                       StepRec<typename P::real, D> r) {
+// Resampling, CP side, row (CP j, direction k): the components of direction k within r of the CP
+// (the forward gather's window).
+template <int Q, int D, class P, class Emit>
+__device__ __forceinline__ uint32_t enum_resample_cp(const Args<Q, D, P>& A, int64_t j, int k, Emit&& emit) {
   using real = typename P::real;
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
-  if (j >= r.P) return;
-  const int64_t rowid = j * Q + k;
   const uint32_t G = A.b.cell[j];
   const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
   int Gc[3];
@@ -281,7 +279,7 @@ __global__ void __launch_bounds__(256) k_list_resample(const __grid_constant__ A
     lo[a] = (int)floor(base - A.R - A.tiny);
     hi[a] = (int)floor(base + A.R + A.tiny);
   }
-  uint32_t cnt = 0, pos = FILL ? r.res.start[rowid] : 0u;
+  uint32_t cnt = 0;
 #pragma unroll 1
   for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
@@ -301,42 +299,93 @@ __global__ void __launch_bounds__(256) k_list_resample(const __grid_constant__ A
 #pragma unroll
           for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
           if (canon_d2<D, real>(o, c, e) <= A.R2) {
-            if (FILL) {
-              r.res.rec[pos++] = make_rec<D, real>((uint32_t)j, m * (uint32_t)Q + (uint32_t)k, e);
-            }
+            emit(m * (uint32_t)Q + (uint32_t)k, e);
             ++cnt;
           }
         }
       }
-  if (!FILL) r.res.start[rowid] = cnt;
+  return cnt;
 }
 
-// Gap-fill pairs of CP j: the CPs within r (from j's side, as the emit pass computes it) that share
-// an empty direction with j.
-template <int Q, int D, class P, bool FILL>
-__global__ void __launch_bounds__(256) k_list_gap(const __grid_constant__ Args<Q, D, P> A,
-                                                  StepRec<typename P::real, D> r) {
+// Component side of both lists, row = component (m, k): the window around the component's landing
+// point; CP candidates come from the output cells (resampling) or from the moved thin cells
+// (refine, through cp_of_cell).  The displacement is computed in the CP side's operation order, so
+// both sides decide the same pairs and record the same e.
+template <int Q, int D, class P, bool REFINE, class Emit>
+__device__ __forceinline__ uint32_t enum_comp(const Args<Q, D, P>& A, const StepRec<typename P::real, D>& r,
+                                              const uint32_t* __restrict__ cp_of_cell, uint32_t m, int k, Emit&& emit) {
   using real = typename P::real;
-  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (j >= r.P) return;
-  const uint32_t em = A.emask[j];
-  if (!em) {
-    if (!FILL) r.gap.start[j] = 0;
-    return;
-  }
-  const uint32_t G = A.b.cell[j];
-  const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
-  int Gc[3];
-  decode_cell<D>(I, G, Gc);
-  real p[3] = {0, 0, 0};
+  const uint32_t g = A.a.cell[m];
+  const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
+  int Sc[3];
+  decode_cell<D>(I, g, Sc);
+  real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
   for (int a = 0; a < D; ++a) {
-    p[a] = A.b.off[(int64_t)a * A.ccap + j];
-    lo[a] = (int)floor(p[a] - A.R - A.tiny);
-    hi[a] = (int)floor(p[a] + A.R + A.tiny);
+    o[a] = A.a.off[(int64_t)a * A.mcap + m];
+    cdk[a] = (real)A.L.cd[k][a];
+    const real tt = rn_add(o[a], cdk[a]);
+    lo[a] = (int)floor(tt - A.R - A.tiny);
+    hi[a] = (int)floor(tt + A.R + A.tiny);
   }
-  uint32_t cnt = 0, pos = FILL ? r.gap.start[j] : 0u;
+  uint32_t cnt = 0;
+#pragma unroll 1
+  for (int gz = lo[2]; gz <= hi[2]; ++gz)
+#pragma unroll 1
+    for (int gy = lo[1]; gy <= hi[1]; ++gy)
+#pragma unroll 1
+      for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+        const int dG[3] = {gx, gy, gz};
+        uint32_t Gg;
+        if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Gg)) continue;
+        if constexpr (REFINE) {
+          const uint32_t j = cp_of_cell[Gg];
+          if (j == kNone || !r.cp_moved[j]) continue;
+          real c[3] = {0, 0, 0}, e[3];
+#pragma unroll
+          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(-dG[a], cdk[a], r.cp_cen[(int64_t)a * r.P + j]);
+          if (canon_d2<D, real>(o, c, e) <= A.R2) {
+            emit(j, e);
+            ++cnt;
+          }
+        } else {
+          const uint32_t c0 = A.b.start[Gg], c1 = A.b.start[Gg + 1];
+          for (uint32_t c = c0; c < c1; ++c) {
+            real cc[3] = {0, 0, 0}, e[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) cc[a] = canon_c<real>(-dG[a], cdk[a], A.b.off[(int64_t)a * A.ccap + c]);
+            if (canon_d2<D, real>(o, cc, e) <= A.R2) {
+              emit(c, e);
+              ++cnt;
+            }
+          }
+        }
+      }
+  return cnt;
+}
+
+// Gap fill, row = CP j (T = false: the filled CP's side, emit(neighbour l, both, e)) or row = CP l
+// (T = true: the neighbour's side, emit(filled CP j, both, e)).  e = p_l - p_j is computed from j's
+// side in both cases, as the emit pass does.
+template <int Q, int D, class P, bool T, class Emit>
+__device__ __forceinline__ uint32_t enum_gap(const Args<Q, D, P>& A, int64_t x, Emit&& emit) {
+  using real = typename P::real;
+  const uint32_t em = A.emask[x];
+  if (!em) return 0;
+  const uint32_t G = A.b.cell[x];
+  const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
+  int Gc[3];
+  decode_cell<D>(I, G, Gc);
+  real px[3] = {0, 0, 0};
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    px[a] = A.b.off[(int64_t)a * A.ccap + x];
+    lo[a] = (int)floor(px[a] - A.R - A.tiny) - (T ? 1 : 0);
+    hi[a] = (int)floor(px[a] + A.R + A.tiny) + (T ? 1 : 0);
+  }
+  uint32_t cnt = 0;
 #pragma unroll 1
   for (int gz = lo[2]; gz <= hi[2]; ++gz)
 #pragma unroll 1
@@ -344,166 +393,110 @@ __global__ void __launch_bounds__(256) k_list_gap(const __grid_constant__ Args<Q
 #pragma unroll 1
       for (int gx = lo[0]; gx <= hi[0]; ++gx) {
         const int dS[3] = {gx, gy, gz};
-        real cc[3] = {0, 0, 0};
-#pragma unroll
-        for (int a = 0; a < D; ++a) cc[a] = canon_c<real>(dS[a], (real)0, p[a]);
-        if (cell_d2_lower<D, real>(cc) > A.R2) continue;
         uint32_t Hg;
         if (!cell_at<D>(I, Gc[0] + gx, Gc[1] + gy, Gc[2] + gz, &Hg)) continue;
         const uint32_t c0 = A.b.start[Hg], c1 = A.b.start[Hg + 1];
         for (uint32_t c = c0; c < c1; ++c) {
           const uint32_t both = A.emask[c] & em;
           if (!both) continue;
-          real o[3] = {0, 0, 0}, e[3];
+          real e[3], d2;
+          if constexpr (!T) {  // j = x, l = c, window offset dS from j to l
+            real cc[3] = {0, 0, 0}, o[3] = {0, 0, 0};
 #pragma unroll
-          for (int a = 0; a < D; ++a) o[a] = A.b.off[(int64_t)a * A.ccap + c];
-          if (canon_d2<D, real>(o, cc, e) <= A.R2) {
-            if (FILL) {
-              r.gap.bits[pos] = both;
-              r.gap.rec[pos++] = make_rec<D, real>((uint32_t)j, c, e);
+            for (int a = 0; a < D; ++a) {
+              cc[a] = canon_c<real>(dS[a], (real)0, px[a]);
+              o[a] = A.b.off[(int64_t)a * A.ccap + c];
             }
+            d2 = canon_d2<D, real>(o, cc, e);
+          } else {  // l = x, j = c: offset from j to l is -dS
+            real cc[3] = {0, 0, 0};
+#pragma unroll
+            for (int a = 0; a < D; ++a) cc[a] = canon_c<real>(-dS[a], (real)0, A.b.off[(int64_t)a * A.ccap + c]);
+            d2 = canon_d2<D, real>(px, cc, e);
+          }
+          if (d2 <= A.R2) {
+            emit(c, both, e);
             ++cnt;
           }
         }
       }
-  if (!FILL) r.gap.start[j] = cnt;
+  return cnt;
 }
 
-// Component-side copies of the resampling and refine lists (the transposes), enumerated from each
-// component's own window with the same canonical arithmetic as the CP side, so they hold exactly
-// the same pairs; each component's pairs land in its slot range [tstart[i], tstart[i+1]) (from the
-// CP-side counts) in window order.  A count mismatch would be a bug: it sets *bad and writes nothing
-// out of range.
-template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_tlist_resample(const __grid_constant__ Args<Q, D, P> A,
-                                                        StepRec<typename P::real, D> r, uint32_t* __restrict__ bad) {
+// Reserve cnt consecutive slots of a list for this lane: one atomicAdd per warp.  Every lane of the
+// warp calls it (lanes without a row pass 0).
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t cnt, uint32_t* counter) {
+  const int lane = threadIdx.x & 31;
+  uint32_t incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = atomicAdd(counter, total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  return base + incl - cnt;
+}
+
+// One pass per list: each row counts its pairs, reserves their slots and writes them (a second,
+// cache-warm enumeration).  A list whose capacity is too small writes nothing past it; the counter
+// then holds the size needed and the host runs the kernel again.
+enum ListKind { kRefineCP = 0, kRefineComp = 1, kResCP = 2, kResComp = 3, kGapCP = 4, kGapNb = 5 };
+
+template <int Q, int D, class P, int KIND>
+__global__ void __launch_bounds__(256) k_list(const __grid_constant__ Args<Q, D, P> A,
+                                              const __grid_constant__ StepRec<typename P::real, D> r,
+                                              const uint32_t* __restrict__ cp_of_cell, uint32_t* __restrict__ counter) {
   using real = typename P::real;
-  const int64_t M = r.M, QM = (int64_t)Q * M;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(t / M);
-    const uint32_t m = (uint32_t)(t - (int64_t)k * M);
-    const uint32_t i = m * (uint32_t)Q + (uint32_t)k;
-    const uint32_t b0 = r.res.tstart[i], b1 = r.res.tstart[i + 1];
-    if (b0 == b1) continue;
-    const uint32_t g = A.a.cell[m];
-    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
-    int Sc[3];
-    decode_cell<D>(I, g, Sc);
-    real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
-    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      o[a] = A.a.off[(int64_t)a * A.mcap + m];
-      cdk[a] = (real)A.L.cd[k][a];
-      const real tt = rn_add(o[a], cdk[a]);
-      lo[a] = (int)floor(tt - A.R - A.tiny);
-      hi[a] = (int)floor(tt + A.R + A.tiny);
-    }
-    uint32_t pos = b0;
-#pragma unroll 1
-    for (int gz = lo[2]; gz <= hi[2]; ++gz)
-#pragma unroll 1
-      for (int gy = lo[1]; gy <= hi[1]; ++gy)
-#pragma unroll 1
-        for (int gx = lo[0]; gx <= hi[0]; ++gx) {
-          const int dG[3] = {gx, gy, gz};
-          uint32_t Gg;
-          if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Gg)) continue;
-          const uint32_t c0 = A.b.start[Gg], c1 = A.b.start[Gg + 1];
-          for (uint32_t c = c0; c < c1; ++c) {
-            real cc[3] = {0, 0, 0}, e[3];
-#pragma unroll
-            for (int a = 0; a < D; ++a) cc[a] = canon_c<real>(-dG[a], cdk[a], A.b.off[(int64_t)a * A.ccap + c]);
-            if (canon_d2<D, real>(o, cc, e) <= A.R2) {
-              if (pos < b1) r.res.trec[pos] = make_rec<D, real>(c, i, e);
-              ++pos;
-            }
-          }
-        }
-    if (pos != b1) atomicOr(bad, 1u);
-  }
-}
-
-template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_tlist_refine(const __grid_constant__ Args<Q, D, P> A,
-                                                      StepRec<typename P::real, D> r,
-                                                      const uint32_t* __restrict__ cp_of_cell, uint32_t* __restrict__ bad) {
-  using real = typename P::real;
-  const int64_t M = r.M, QM = (int64_t)Q * M;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(t / M);
-    const uint32_t m = (uint32_t)(t - (int64_t)k * M);
-    const uint32_t i = m * (uint32_t)Q + (uint32_t)k;
-    const uint32_t b0 = r.ref.tstart[i], b1 = r.ref.tstart[i + 1];
-    if (b0 == b1) continue;
-    const uint32_t g = A.a.cell[m];
-    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
-    int Sc[3];
-    decode_cell<D>(I, g, Sc);
-    real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
-    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      o[a] = A.a.off[(int64_t)a * A.mcap + m];
-      cdk[a] = (real)A.L.cd[k][a];
-      const real tt = rn_add(o[a], cdk[a]);
-      lo[a] = (int)floor(tt - A.R - A.tiny);
-      hi[a] = (int)floor(tt + A.R + A.tiny);
-    }
-    uint32_t pos = b0;
-#pragma unroll 1
-    for (int gz = lo[2]; gz <= hi[2]; ++gz)
-#pragma unroll 1
-      for (int gy = lo[1]; gy <= hi[1]; ++gy)
-#pragma unroll 1
-        for (int gx = lo[0]; gx <= hi[0]; ++gx) {
-          const int dG[3] = {gx, gy, gz};
-          uint32_t Fg;
-          if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Fg)) continue;
-          const uint32_t j = cp_of_cell[Fg];
-          if (j == kNone || !r.cp_moved[j]) continue;
-          real c[3] = {0, 0, 0}, e[3];
-#pragma unroll
-          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(-dG[a], cdk[a], r.cp_cen[(int64_t)a * r.P + j]);
-          if (canon_d2<D, real>(o, c, e) <= A.R2) {
-            if (pos < b1) r.ref.trec[pos] = make_rec<D, real>(j, i, e);
-            ++pos;
-          }
-        }
-    if (pos != b1) atomicOr(bad, 1u);
-  }
-}
-
-// Transpose of a pair list (pairs grouped by item, ascending pair index inside each group): integer
-// atomics count and place the pairs, then each group is sorted, so the result does not depend on
-// the order the atomics ran in.
-template <class Rec>
-__global__ void k_item_count(const Rec* __restrict__ rec, int64_t n, uint32_t* __restrict__ cnt) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(cnt + rec[p].item, 1u);
-}
-template <class Rec>
-__global__ void k_item_place(const Rec* __restrict__ rec, int64_t n, const uint32_t* __restrict__ tstart,
-                             uint32_t* __restrict__ fill, Rec* __restrict__ trec) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-    Rec q = rec[p];
-    const uint32_t i = q.item;
-    q.item = (uint32_t)p;
-    trec[tstart[i] + atomicAdd(fill + i, 1u)] = q;
-  }
-}
-template <class Rec>
-__global__ void k_item_sort(const uint32_t* __restrict__ tstart, int64_t items, Rec* __restrict__ trec) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < items; i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t b0 = tstart[i], b1 = tstart[i + 1];
-    for (uint32_t a = b0 + 1; a < b1; ++a) {  // insertion sort by row-list index (groups hold a few pairs)
-      const Rec v = trec[a];
-      uint32_t c = a;
-      while (c > b0 && trec[c - 1].item > v.item) {
-        trec[c] = trec[c - 1];
-        --c;
+  const auto& Lst = KIND == kRefineCP ? r.ref.f : KIND == kRefineComp ? r.ref.t : KIND == kResCP ? r.res.f
+                  : KIND == kResComp ? r.res.t : KIND == kGapCP ? r.gap.f : r.gap.t;
+  const int64_t rows = Lst.rows;
+  for (int64_t t0 = blockIdx.x * (int64_t)blockDim.x; t0 < rows; t0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = t0 + threadIdx.x;
+    const bool act = row < rows;
+    const auto nop2 = [](uint32_t, const real(&)[3]) {};
+    const auto nop3 = [](uint32_t, uint32_t, const real(&)[3]) {};
+    uint32_t cnt = 0;
+    int64_t j = 0, m = 0;
+    int k = 0;
+    if (act) {
+      if constexpr (KIND == kRefineCP || KIND == kResCP) {
+        j = row / Q;
+        k = (int)(row - j * Q);
+        cnt = KIND == kRefineCP ? enum_refine_cp<Q, D, P>(A, r, j, k, nop2) : enum_resample_cp<Q, D, P>(A, j, k, nop2);
+      } else if constexpr (KIND == kRefineComp || KIND == kResComp) {
+        k = (int)(row / r.M);
+        m = row - (int64_t)k * r.M;
+        cnt = enum_comp<Q, D, P, KIND == kRefineComp>(A, r, cp_of_cell, (uint32_t)m, k, nop2);
+      } else {
+        cnt = enum_gap<Q, D, P, KIND == kGapNb>(A, row, nop3);
       }
-      trec[c] = v;
+    }
+    const uint32_t pos = warp_reserve(cnt, counter);
+    if (!act) continue;
+    Lst.start[row] = pos;
+    Lst.cnt[row] = cnt;
+    if (!cnt || (int64_t)pos + cnt > Lst.cap) continue;
+    uint32_t w = pos;
+    if constexpr (KIND == kRefineCP || KIND == kResCP) {
+      const auto put = [&](uint32_t item, const real(&e)[3]) { Lst.rec[w++] = make_rec<D, real>((uint32_t)j, item, e); };
+      if constexpr (KIND == kRefineCP) enum_refine_cp<Q, D, P>(A, r, j, k, put);
+      else enum_resample_cp<Q, D, P>(A, j, k, put);
+    } else if constexpr (KIND == kRefineComp || KIND == kResComp) {
+      const uint32_t i = (uint32_t)m * (uint32_t)Q + (uint32_t)k;
+      const auto put = [&](uint32_t cp, const real(&e)[3]) { Lst.rec[w++] = make_rec<D, real>(cp, i, e); };
+      enum_comp<Q, D, P, KIND == kRefineComp>(A, r, cp_of_cell, (uint32_t)m, k, put);
+    } else if constexpr (KIND == kGapCP) {
+      const auto put = [&](uint32_t l, uint32_t both, const real(&e)[3]) {
+        Lst.bits[w] = both;
+        Lst.rec[w++] = make_rec<D, real>((uint32_t)row, l, e);
+      };
+      enum_gap<Q, D, P, false>(A, row, put);
+    } else {
+      const auto put = [&](uint32_t jj, uint32_t both, const real(&e)[3]) { Lst.rec[w++] = make_rec<D, real>(jj, both, e); };
+      enum_gap<Q, D, P, true>(A, row, put);
     }
   }
 }
@@ -526,74 +519,81 @@ __global__ void __launch_bounds__(256) k_bwd_in(const __grid_constant__ RecK<Q, 
 }
 
 // Gap fill, CP side: F_jk = r rho_rest W_k / s_jk for the filled entries.  d s_jk / d p_j = sum of
-// unit vectors u_jl (e = p_l - p_j); the neighbour's share (-u_jl) is left in cpair for k_bwd_gap_t.
-// Filled entries do not depend on the gather, so their cotangent is cleared for it.
+// unit vectors u_jl (e = p_l - p_j); the neighbours' share (-u_jl) comes from sbar (kept per CP and
+// direction) in k_bwd_gap_t.  Filled entries do not depend on the gather: their cotangent is cleared.
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_gap(const __grid_constant__ RecK<Q, D, P> K, typename P::real* __restrict__ xbarP,
-                                                 typename P::real* __restrict__ fbarG, typename P::real* __restrict__ cpair) {
+                                                 typename P::real* __restrict__ fbarG, typename P::real* __restrict__ sbarG) {
   using real = typename P::real;
   const int64_t Pn = K.r.P;
-  const auto& L = K.r.gap;
+  const auto& L = K.r.gap.f;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t em = K.r.emask[j];
-    if (!em) continue;
-    const InstK I = K.inst[find_instance(K.inst_base, K.n_inst, K.r.out_cell[j])];
-    const uint32_t p0 = L.start[j], p1 = L.start[j + 1];
-    real s[Q];
-#pragma unroll
-    for (int k = 0; k < Q; ++k) s[k] = 0;
-    for (uint32_t p = p0; p < p1; ++p) {
-      real u[3];
-      const real w = K.R - unit_of<D, real>(L.rec[p], u);
-      const uint32_t bits = L.bits[p];
-#pragma unroll
-      for (int k = 0; k < Q; ++k)
-        if ((bits >> k) & 1u) s[k] += w;
-    }
     real sbar[Q];
 #pragma unroll
-    for (int k = 0; k < Q; ++k) {
-      sbar[k] = 0;
-      if (((em >> k) & 1u) && s[k] > (real)0) {
-        const real Fk = (K.R / s[k]) * (real)(I.rho_rest * K.L.w[k]);
-        sbar[k] = -fbarG[(int64_t)k * Pn + j] * Fk / s[k];
-        fbarG[(int64_t)k * Pn + j] = 0;
+    for (int k = 0; k < Q; ++k) sbar[k] = 0;
+    if (em) {
+      const InstK I = K.inst[find_instance(K.inst_base, K.n_inst, K.r.out_cell[j])];
+      const uint32_t p0 = L.start[j], p1 = p0 + L.cnt[j];
+      real s[Q];
+#pragma unroll
+      for (int k = 0; k < Q; ++k) s[k] = 0;
+      for (uint32_t p = p0; p < p1; ++p) {
+        real u[3];
+        const real w = K.R - unit_of<D, real>(L.rec[p], u);
+        const uint32_t bits = L.bits[p];
+#pragma unroll
+        for (int k = 0; k < Q; ++k)
+          if ((bits >> k) & 1u) s[k] += w;
       }
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        if (((em >> k) & 1u) && s[k] > (real)0) {
+          const real Fk = (K.R / s[k]) * (real)(I.rho_rest * K.L.w[k]);
+          sbar[k] = -fbarG[(int64_t)k * Pn + j] * Fk / s[k];
+          fbarG[(int64_t)k * Pn + j] = 0;
+        }
+      }
+      real xj[3] = {0, 0, 0};
+      for (uint32_t p = p0; p < p1; ++p) {
+        real u[3];
+        unit_of<D, real>(L.rec[p], u);
+        const uint32_t bits = L.bits[p];
+        real c = 0;
+#pragma unroll
+        for (int k = 0; k < Q; ++k)
+          if ((bits >> k) & 1u) c += sbar[k];
+#pragma unroll
+        for (int a = 0; a < D; ++a) xj[a] += c * u[a];
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] += xj[a];
     }
-    real xj[3] = {0, 0, 0};
-    for (uint32_t p = p0; p < p1; ++p) {
-      real u[3];
-      unit_of<D, real>(L.rec[p], u);
-      const uint32_t bits = L.bits[p];
-      real c = 0;
 #pragma unroll
-      for (int k = 0; k < Q; ++k)
-        if ((bits >> k) & 1u) c += sbar[k];
-      cpair[p] = c;
-#pragma unroll
-      for (int a = 0; a < D; ++a) xj[a] += c * u[a];
-    }
-#pragma unroll
-    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] += xj[a];
+    for (int k = 0; k < Q; ++k) sbarG[(int64_t)k * Pn + j] = sbar[k];
   }
 }
 
-// Gap fill, neighbour side: p_l receives -c u_jl from every pair (j, l).
+// Gap fill, neighbour side: p_l receives -(sum over shared empty k of sbar_jk) u_jl from every
+// filled CP j it is paired with.
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_bwd_gap_t(const __grid_constant__ RecK<Q, D, P> K, const typename P::real* __restrict__ cpair,
+__global__ void __launch_bounds__(256) k_bwd_gap_t(const __grid_constant__ RecK<Q, D, P> K, const typename P::real* __restrict__ sbarG,
                                                    typename P::real* __restrict__ xbarP) {
   using real = typename P::real;
   const int64_t Pn = K.r.P;
-  const auto& L = K.r.gap;
+  const auto& L = K.r.gap.t;
   for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < Pn; l += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t q0 = L.tstart[l], q1 = L.tstart[l + 1];
+    const uint32_t q0 = L.start[l], q1 = q0 + L.cnt[l];
     if (q0 == q1) continue;
     real xl[3] = {0, 0, 0};
     for (uint32_t q = q0; q < q1; ++q) {
-      const auto pr = L.trec[q];
+      const auto pr = L.rec[q];
       real u[3];
       unit_of<D, real>(pr, u);
-      const real c = cpair[pr.item];
+      real c = 0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k)
+        if ((pr.item >> k) & 1u) c += sbarG[(int64_t)k * Pn + pr.row];
 #pragma unroll
       for (int a = 0; a < D; ++a) xl[a] -= c * u[a];
     }
@@ -613,17 +613,16 @@ __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK
                                                     typename P::real* __restrict__ Gc) {
   using real = typename P::real;
   const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
-  const auto& L = K.r.res;
+  const auto& L = K.r.res.t;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(t / M);
     const int64_t m = t - (int64_t)k * M;
-    const int64_t i = m * Q + k;
     const real inv = K.r.inv_sw[t];
-    const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
+    const uint32_t q0 = L.start[t], q1 = q0 + L.cnt[t];
     real G = 0;
     if (inv > (real)0) {
       for (uint32_t q = q0; q < q1; ++q) {
-        const auto pr = L.trec[q];
+        const auto pr = L.rec[q];
         real u[3];
         const real d = unit_of<D, real>(pr, u);
         G += (K.R - d) * inv * fbarG[(int64_t)k * Pn + pr.row];
@@ -634,7 +633,7 @@ __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK
     const real fsi = rec_fstar<Q, D, P>(K, m, k) * inv;
     real y[3] = {0, 0, 0};
     for (uint32_t q = q0; q < q1; ++q) {
-      const auto pr = L.trec[q];
+      const auto pr = L.rec[q];
       real u[3];
       unit_of<D, real>(pr, u);
       const real wb = inv > (real)0 ? fsi * (fbarG[(int64_t)k * Pn + pr.row] - G) : (real)0;
@@ -658,12 +657,12 @@ __global__ void __launch_bounds__(256) k_bwd_rows(const __grid_constant__ RecK<Q
   using real = typename P::real;
   const int64_t M = K.r.M, Pn = K.r.P, PQ = Pn * Q;
   for (int64_t rw = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; rw < PQ; rw += (int64_t)gridDim.x * blockDim.x) {
-    const auto& L = K.r.res;
+    const auto& L = K.r.res.f;
     const int64_t j = rw / Q;
     const int k = (int)(rw - j * Q);
     const real fb = fbarG[(int64_t)k * Pn + j];
     real x[3] = {0, 0, 0};
-    for (uint32_t p = L.start[rw]; p < L.start[rw + 1]; ++p) {
+    for (uint32_t p = L.start[rw], pe = p + L.cnt[rw]; p < pe; ++p) {
       const auto pr = L.rec[p];
       real u[3];
       unit_of<D, real>(pr, u);
@@ -675,9 +674,9 @@ __global__ void __launch_bounds__(256) k_bwd_rows(const __grid_constant__ RecK<Q
     }
 #pragma unroll
     for (int a = 0; a < D; ++a) xrow[(int64_t)a * PQ + rw] = x[a];
-    const auto& R = K.r.ref;
+    const auto& R = K.r.ref.f;
     real W = 0, sx[3] = {0, 0, 0};
-    for (uint32_t p = R.start[rw]; p < R.start[rw + 1]; ++p) {
+    for (uint32_t p = R.start[rw], pe = p + R.cnt[rw]; p < pe; ++p) {
       const auto pr = R.rec[p];
       const uint32_t i = pr.item;
       const real w = exp(rec_fstar<Q, D, P>(K, i / Q, (int)(i % Q)));
@@ -743,11 +742,10 @@ __global__ void __launch_bounds__(256) k_bwd_comp(const __grid_constant__ RecK<Q
                                                   typename P::real* __restrict__ fsbar, typename P::real* __restrict__ ybar) {
   using real = typename P::real;
   const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
-  const auto& L = K.r.ref;
+  const auto& L = K.r.ref.t;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
     const int k = (int)(t / M);
     const int64_t m = t - (int64_t)k * M;
-    const int64_t i = m * Q + k;
     real y[3] = {0, 0, 0};
 #pragma unroll
     for (int a = 0; a < D; ++a) y[a] = ybar[(int64_t)a * QM + t];
@@ -757,11 +755,11 @@ __global__ void __launch_bounds__(256) k_bwd_comp(const __grid_constant__ RecK<Q
 #pragma unroll
       for (int a = 0; a < D; ++a) y[a] += cenbar[(int64_t)a * ncells + F];
     }
-    const uint32_t q0 = L.tstart[i], q1 = L.tstart[i + 1];
+    const uint32_t q0 = L.start[t], q1 = q0 + L.cnt[t];
     if (q0 < q1) {
       const real w = exp(rec_fstar<Q, D, P>(K, m, k));
       for (uint32_t q = q0; q < q1; ++q) {
-        const auto pr = L.trec[q];
+        const auto pr = L.rec[q];
         const uint32_t j = pr.row;
         const real wW = w / Wj[j];
         real dot = 0;
@@ -901,19 +899,7 @@ __global__ void k_bwd_tau_sum(const double* __restrict__ blocksum, int n_inst, d
   }
 }
 
-// Export helpers: real -> double, FP32DEV f -> rho*W + dev, record fields -> arrays.
-template <class real, int D>
-__global__ void k_rec_fields(const PairRec<real, D>* __restrict__ rec, int64_t n, uint32_t* __restrict__ item,
-                             double* __restrict__ e) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-    const PairRec<real, D> q = rec[p];
-    if (item) item[p] = q.item;
-    if (e) {
-#pragma unroll
-      for (int a = 0; a < D; ++a) e[(int64_t)a * n + p] = (double)q.e[a];
-    }
-  }
-}
+// Export helpers: real -> double, FP32DEV f -> rho*W + dev.
 template <class real>
 __global__ void k_to_f64(const real* __restrict__ src, int64_t n, double* __restrict__ dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -944,6 +930,24 @@ inline unsigned grid_for(int64_t n, int threads = 256) {
   return std::max(1u, std::min<unsigned>(div_up(std::max<int64_t>(n, 1), threads), (unsigned)sm_count() * 16));
 }
 
+// Canonical row-ordered copy of a list (export only): out[prefix[r] + q] = rec[start[r] + q].
+template <class real, int D>
+__global__ void k_rows_compact(PairList<real, D> L, const uint32_t* __restrict__ prefix, uint32_t* __restrict__ item,
+                               uint32_t* __restrict__ bits, double* __restrict__ e, int64_t n) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < L.rows; r += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t o = prefix[r], s0 = L.start[r], c = L.cnt[r];
+    for (uint32_t q = 0; q < c; ++q) {
+      const PairRec<real, D> pr = L.rec[s0 + q];
+      if (item) item[o + q] = pr.item;
+      if (bits) bits[o + q] = L.bits[s0 + q];
+      if (e) {
+#pragma unroll
+        for (int a = 0; a < D; ++a) e[(int64_t)a * n + o + q] = (double)pr.e[a];
+      }
+    }
+  }
+}
+
 template <int Q, int D, class P>
 struct TapeImpl : TapeBase, StepHook {
   using real = typename P::real;
@@ -957,24 +961,23 @@ struct TapeImpl : TapeBase, StepHook {
   int n_inst = 0;
   real R = 0;
   int64_t ncells = 0;
-  double* wk = nullptr;       // W_k in FP64 (export of FP32DEV f)
-  uint32_t* hbuf = nullptr;   // pinned host words for the counts read back while recording
-  uint32_t* d_bad = nullptr;  // device flag: list orientations disagree
-  bool unchecked = false;
+  double* wk = nullptr;        // W_k in FP64 (export of FP32DEV f)
+  uint32_t* hbuf = nullptr;    // pinned host words read back while recording
+  uint32_t* d_count = nullptr; // slot counters of the six lists
+  double per_row[6] = {16, 16, 16, 16, 4, 4};  // capacity estimate: pairs per row, grown as seen
   cudaEvent_t done = nullptr;
 
   explicit TapeImpl(SimBase* s) : sim(s) {}
   ~TapeImpl() override {
     if (done) cudaEventDestroy(done);
     if (hbuf) cudaFreeHost(hbuf);
-    if (d_bad) cudaFree(d_bad);
+    if (d_count) cudaFree(d_count);
   }
 
   int init() {
     DBM_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
     DBM_CUDA(cudaMallocHost(&hbuf, 64));
-    DBM_CUDA(cudaMalloc(&d_bad, 4));
-    DBM_CUDA(cudaMemset(d_bad, 0, 4));
+    DBM_CUDA(cudaMalloc(&d_count, 6 * 4));
     DBM_TRY(rec_mem.get(&wk, Q));
     return DBM_OK;
   }
@@ -990,7 +993,7 @@ struct TapeImpl : TapeBase, StepHook {
   int counts(int i, int64_t* c) const override {
     if (i < 0 || i >= (int)steps.size()) { set_last_error("tape: no step %d", i); return DBM_ERR_INVALID; }
     const auto& r = steps[i];
-    c[0] = r.M; c[1] = r.P; c[2] = r.ref.n; c[3] = r.res.n; c[4] = r.gap.n; c[5] = 0; c[6] = 0; c[7] = 0;
+    c[0] = r.M; c[1] = r.P; c[2] = r.ref.f.n; c[3] = r.res.f.n; c[4] = r.gap.f.n; c[5] = 0; c[6] = 0; c[7] = 0;
     return DBM_OK;
   }
 
@@ -1016,14 +1019,9 @@ struct TapeImpl : TapeBase, StepHook {
     n_inst = A.n_inst;
     R = A.R;
     ncells = A.ncells;
-    const uint32_t* src[2] = {A.a.count, d_bad};  // the previous step's list check rides along
-    DBM_TRY(fetch(src, 2, s));
+    const uint32_t* src[1] = {A.a.count};
+    DBM_TRY(fetch(src, 1, s));
     const uint32_t M = hbuf[0];
-    unchecked = false;
-    if (hbuf[1]) {
-      set_last_error("tape: the two orientations of a neighbour list disagree");
-      return DBM_ERR_STATE;
-    }
     if (wk) DBM_CUDA(cudaMemcpyAsync(wk, L.w, sizeof(double) * Q, cudaMemcpyHostToDevice, s));
     StepRec<real, D>& r = cur;
     r.M = M;
@@ -1050,48 +1048,41 @@ struct TapeImpl : TapeBase, StepHook {
     return DBM_OK;
   }
 
-  // First half of a pair list: per-row counts (by `count`), scanned in place into start[].
-  template <class Count>
-  int list_count(PairCSR<real, D>& Lst, int64_t rows, int64_t items, bool with_bits, Count&& count, cudaStream_t s) {
+  PairList<real, D>& list_of(StepRec<real, D>& r, int kind) {
+    switch (kind) {
+      case kRefineCP: return r.ref.f;
+      case kRefineComp: return r.ref.t;
+      case kResCP: return r.res.f;
+      case kResComp: return r.res.t;
+      case kGapCP: return r.gap.f;
+      default: return r.gap.t;
+    }
+  }
+
+  int alloc_list(PairList<real, D>& Lst, int64_t rows, int64_t cap, bool with_bits) {
     Lst.rows = rows;
-    Lst.items = items;
-    (void)with_bits;
-    DBM_TRY(rec_mem.get(&Lst.start, rows + 1));
-    DBM_CUDA(cudaMemsetAsync(Lst.start + rows, 0, 4, s));
-    DBM_TRY(count());
-    char* stmp;
-    DBM_TRY(tmp_mem.get(&stmp, (int64_t)scan_tmp_bytes(rows + 1)));
-    DBM_TRY(scan_exclusive_u32(Lst.start, Lst.start, rows + 1, nullptr, nullptr, stmp, s));
+    Lst.cap = cap;
+    DBM_TRY(rec_mem.get(&Lst.start, rows));
+    DBM_TRY(rec_mem.get(&Lst.cnt, rows));
+    DBM_TRY(rec_mem.get(&Lst.rec, cap));
+    if (with_bits) DBM_TRY(rec_mem.get(&Lst.bits, cap));
     return DBM_OK;
   }
 
-  // Second half, once Lst.n is known: fill the pairs (by `fill`), count the pairs of every item and
-  // build the transpose, by `tfill` when given (a component-side enumeration), else by placing the
-  // records with integer atomics and sorting each item's group.
-  template <class Fill, class TFill>
-  int list_fill(PairCSR<real, D>& Lst, bool with_bits, Fill&& fill, TFill&& tfill, bool have_tfill, cudaStream_t s) {
-    const int64_t n = Lst.n, items = Lst.items;
-    DBM_TRY(rec_mem.get(&Lst.rec, n));
-    if (with_bits) DBM_TRY(rec_mem.get(&Lst.bits, n));
-    DBM_TRY(rec_mem.get(&Lst.trec, n));
-    DBM_TRY(rec_mem.get(&Lst.tstart, items + 1));
-    uint32_t* cnt;
-    DBM_TRY(tmp_mem.get(&cnt, items + 1));
-    DBM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(items + 1) * 4, s));
-    if (n > 0) {
-      DBM_TRY(fill());
-      k_item_count<<<grid_for(n), 256, 0, s>>>(Lst.rec, n, cnt);
-      DBM_LAUNCH_CHECK();
+  int launch_list(const Args<Q, D, P>& A, const StepRec<real, D>& r, int kind, const uint32_t* cp_of_cell,
+                  cudaStream_t s) {
+    const PairList<real, D>& Lst = list_of(const_cast<StepRec<real, D>&>(r), kind);
+    DBM_CUDA(cudaMemsetAsync(d_count + kind, 0, 4, s));
+    if (Lst.rows == 0) return DBM_OK;
+    const unsigned g = grid_for(Lst.rows);
+    switch (kind) {
+      case kRefineCP: k_list<Q, D, P, kRefineCP><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
+      case kRefineComp: k_list<Q, D, P, kRefineComp><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
+      case kResCP: k_list<Q, D, P, kResCP><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
+      case kResComp: k_list<Q, D, P, kResComp><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
+      case kGapCP: k_list<Q, D, P, kGapCP><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
+      default: k_list<Q, D, P, kGapNb><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
     }
-    char* stmp;
-    DBM_TRY(tmp_mem.get(&stmp, (int64_t)scan_tmp_bytes(items + 1)));
-    DBM_TRY(scan_exclusive_u32(cnt, Lst.tstart, items + 1, nullptr, nullptr, stmp, s));
-    if (n == 0) return DBM_OK;
-    if (have_tfill) return tfill();
-    DBM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)items * 4, s));
-    k_item_place<<<grid_for(n), 256, 0, s>>>(Lst.rec, n, Lst.tstart, cnt, Lst.trec);
-    DBM_LAUNCH_CHECK();
-    k_item_sort<<<grid_for(items), 256, 0, s>>>(Lst.tstart, items, Lst.trec);
     DBM_LAUNCH_CHECK();
     return DBM_OK;
   }
@@ -1139,65 +1130,29 @@ struct TapeImpl : TapeBase, StepHook {
       k_rec_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(A, r, cp_of_cell);
       DBM_LAUNCH_CHECK();
     }
-    // the three lists: counts first (rows: CP x direction for refine and resampling, CP for gap fill)
-    const dim3 grq(div_up(std::max<int64_t>(Pn, 1), 256), Q);
-    const unsigned gp = div_up(std::max<int64_t>(Pn, 1), 256);
-    DBM_TRY(list_count(r.ref, Pn * Q, (int64_t)Q * M, false, [&]() -> int {
-      if (Pn > 0) { k_list_refine<Q, D, P, false><<<grq, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
-      return DBM_OK;
-    }, s));
-    DBM_TRY(list_count(r.res, Pn * Q, (int64_t)Q * M, false, [&]() -> int {
-      if (Pn > 0) { k_list_resample<Q, D, P, false><<<grq, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
-      return DBM_OK;
-    }, s));
-    DBM_TRY(list_count(r.gap, Pn, Pn, true, [&]() -> int {
-      if (Pn > 0) { k_list_gap<Q, D, P, false><<<gp, 256, 0, s>>>(A, r); DBM_LAUNCH_CHECK(); }
-      return DBM_OK;
-    }, s));
-    {
-      const uint32_t* src[3] = {r.ref.start + Pn * Q, r.res.start + Pn * Q, r.gap.start + Pn};
-      DBM_TRY(fetch(src, 3, s));
+    // the six lists, in one pass each
+    const int64_t rows[6] = {Pn * Q, (int64_t)Q * M, Pn * Q, (int64_t)Q * M, Pn, Pn};
+    for (int kind = 0; kind < 6; ++kind) {
+      const int64_t cap = (int64_t)(per_row[kind] * 1.25 * (double)rows[kind]) + 1024;
+      DBM_TRY(alloc_list(list_of(r, kind), rows[kind], cap, kind == kGapCP));
     }
-    r.ref.n = hbuf[0];
-    r.res.n = hbuf[1];
-    r.gap.n = hbuf[2];
-    const auto none = []() -> int { return DBM_OK; };
-    DBM_TRY(list_fill(r.ref, false, [&]() -> int {
-      k_list_refine<Q, D, P, true><<<grq, 256, 0, s>>>(A, r);
-      DBM_LAUNCH_CHECK();
-      return DBM_OK;
-    }, [&]() -> int {
-      k_tlist_refine<Q, D, P><<<grid_for((int64_t)Q * M), 256, 0, s>>>(A, r, cp_of_cell, d_bad);
-      DBM_LAUNCH_CHECK();
-      return DBM_OK;
-    }, true, s));
-    DBM_TRY(list_fill(r.res, false, [&]() -> int {
-      k_list_resample<Q, D, P, true><<<grq, 256, 0, s>>>(A, r);
-      DBM_LAUNCH_CHECK();
-      return DBM_OK;
-    }, [&]() -> int {
-      k_tlist_resample<Q, D, P><<<grid_for((int64_t)Q * M), 256, 0, s>>>(A, r, d_bad);
-      DBM_LAUNCH_CHECK();
-      return DBM_OK;
-    }, true, s));
-    DBM_TRY(list_fill(r.gap, true, [&]() -> int {
-      k_list_gap<Q, D, P, true><<<gp, 256, 0, s>>>(A, r);
-      DBM_LAUNCH_CHECK();
-      return DBM_OK;
-    }, none, false, s));
-    unchecked = true;
-    return DBM_OK;
-  }
-
-  // The component-side enumerations flag a count that differs from the CP side's (a bug, never an
-  // input condition); read that flag.
-  int check_lists(cudaStream_t s) {
-    if (!unchecked) return DBM_OK;
-    const uint32_t* src[1] = {d_bad};
-    DBM_TRY(fetch(src, 1, s));
-    unchecked = false;
-    if (hbuf[0]) {
-      set_last_error("tape: the two orientations of a neighbour list disagree");
+    for (int kind = 0; kind < 6; ++kind) DBM_TRY(launch_list(A, r, kind, cp_of_cell, s));
+    const uint32_t* src[6] = {d_count, d_count + 1, d_count + 2, d_count + 3, d_count + 4, d_count + 5};
+    DBM_TRY(fetch(src, 6, s));
+    uint32_t need[6];
+    for (int kind = 0; kind < 6; ++kind) need[kind] = hbuf[kind];
+    for (int kind = 0; kind < 6; ++kind) {
+      PairList<real, D>& Lst = list_of(r, kind);
+      Lst.n = need[kind];
+      if (rows[kind] > 0) per_row[kind] = std::max(per_row[kind], (double)need[kind] / (double)rows[kind]);
+      if ((int64_t)need[kind] > Lst.cap) {  // too small: allocate the exact size and run it again
+        DBM_TRY(alloc_list(Lst, rows[kind], (int64_t)need[kind], kind == kGapCP));
+        DBM_TRY(launch_list(A, r, kind, cp_of_cell, s));
+      }
+    }
+    if (need[kRefineCP] != need[kRefineComp] || need[kResCP] != need[kResComp] || need[kGapCP] != need[kGapNb]) {
+      set_last_error("tape: the two orientations of a neighbour list disagree (%u/%u, %u/%u, %u/%u)",
+                     need[0], need[1], need[2], need[3], need[4], need[5]);
       return DBM_ERR_STATE;
     }
     return DBM_OK;
@@ -1223,14 +1178,13 @@ struct TapeImpl : TapeBase, StepHook {
       set_last_error("tape backward: null cotangent");
       return DBM_ERR_INVALID;
     }
-    DBM_TRY(check_lists(s));
     DBM_CUDA(cudaStreamWaitEvent(s, done, 0));  // the previous call's scratch is free
     bwd_mem.reset();
-    real *xbarP, *fbarG, *cpair, *fsbar, *ybar, *Gc, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
+    real *xbarP, *fbarG, *sbarG, *fsbar, *ybar, *Gc, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
     double *taupart, *blocksum;
     DBM_TRY(bwd_mem.get(&xbarP, (int64_t)D * Pn));
     DBM_TRY(bwd_mem.get(&fbarG, (int64_t)Q * Pn));
-    DBM_TRY(bwd_mem.get(&cpair, r.gap.n));
+    DBM_TRY(bwd_mem.get(&sbarG, (int64_t)Q * Pn));
     DBM_TRY(bwd_mem.get(&fsbar, QM));
     DBM_TRY(bwd_mem.get(&ybar, (int64_t)D * QM));
     DBM_TRY(bwd_mem.get(&Gc, QM));
@@ -1247,10 +1201,10 @@ struct TapeImpl : TapeBase, StepHook {
     if (Pn > 0) {
       k_bwd_in<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, goff_out, gf_out, xbarP, fbarG);
       DBM_LAUNCH_CHECK();
-      if (r.gap.n > 0) {
-        k_bwd_gap<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xbarP, fbarG, cpair);
+      if (r.gap.f.n > 0) {
+        k_bwd_gap<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xbarP, fbarG, sbarG);
         DBM_LAUNCH_CHECK();
-        k_bwd_gap_t<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, cpair, xbarP);
+        k_bwd_gap_t<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, sbarG, xbarP);
         DBM_LAUNCH_CHECK();
       }
     }
@@ -1278,15 +1232,30 @@ struct TapeImpl : TapeBase, StepHook {
     return DBM_OK;
   }
 
-  // The items (u32[n]) or the displacements (f64[D][n]) of a recorded list, in row order.
-  int export_list(const PairCSR<real, D>& Lst, bool disp, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) {
-    const int64_t sz = Lst.n * (disp ? 8 * D : 4);
+  // A list in canonical CSR form (rows ascending, each row's pairs in enumeration order):
+  // what = 0 start u32[rows + 1], 1 items u32[n], 2 displacements f64[D][n], 3 bits u32[n].
+  int export_list(const PairList<real, D>& Lst, int what, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) {
+    const int64_t n = Lst.n;
+    const int64_t sz = what == 0 ? (Lst.rows + 1) * 4 : what == 2 ? n * 8 * D : n * 4;
     if (needed) *needed = sz;
-    if (!dst || Lst.n == 0) return DBM_OK;
+    if (!dst) return DBM_OK;
     if (nbytes < sz) { set_last_error("tape export: destination too small"); return DBM_ERR_INVALID; }
-    k_rec_fields<real, D><<<grid_for(Lst.n), 256, 0, s>>>(Lst.rec, Lst.n, disp ? nullptr : (uint32_t*)dst,
-                                                        disp ? (double*)dst : nullptr);
-    DBM_LAUNCH_CHECK();
+    uint32_t* prefix;
+    DBM_TRY(tmp_mem.get(&prefix, Lst.rows + 1));
+    DBM_CUDA(cudaMemsetAsync(prefix + Lst.rows, 0, 4, s));
+    if (Lst.rows > 0) DBM_CUDA(cudaMemcpyAsync(prefix, Lst.cnt, (size_t)Lst.rows * 4, cudaMemcpyDeviceToDevice, s));
+    char* stmp;
+    DBM_TRY(tmp_mem.get(&stmp, (int64_t)scan_tmp_bytes(Lst.rows + 1)));
+    DBM_TRY(scan_exclusive_u32(prefix, prefix, Lst.rows + 1, nullptr, nullptr, stmp, s));
+    if (what == 0) {
+      DBM_CUDA(cudaMemcpyAsync(dst, prefix, (size_t)sz, cudaMemcpyDeviceToDevice, s));
+    } else if (n > 0 && Lst.rows > 0) {
+      k_rows_compact<real, D><<<grid_for(Lst.rows), 256, 0, s>>>(Lst, prefix, what == 1 ? (uint32_t*)dst : nullptr,
+                                                                  what == 3 ? (uint32_t*)dst : nullptr,
+                                                                  what == 2 ? (double*)dst : nullptr, n);
+      DBM_LAUNCH_CHECK();
+    }
+    DBM_CUDA(cudaStreamSynchronize(s));  // tmp_mem may be reused by the next call
     return DBM_OK;
   }
 
@@ -1310,16 +1279,16 @@ struct TapeImpl : TapeBase, StepHook {
       case DBM_TAPE_OUT_OFF: src = r.out_off; n = (int64_t)D * r.P; conv = true; break;
       case DBM_TAPE_EMPTY: src = r.emask; n = r.P; break;
       case DBM_TAPE_INV_SW: src = r.inv_sw; n = (int64_t)Q * r.M; conv = true; break;
-      case DBM_TAPE_REFINE_START: src = r.ref.start; n = r.P * Q + 1; break;
-      case DBM_TAPE_REFINE_ITEM: return export_list(r.ref, false, dst, nbytes, needed, s);
-      case DBM_TAPE_REFINE_E: return export_list(r.ref, true, dst, nbytes, needed, s);
-      case DBM_TAPE_RES_START: src = r.res.start; n = r.P * Q + 1; break;
-      case DBM_TAPE_RES_ITEM: return export_list(r.res, false, dst, nbytes, needed, s);
-      case DBM_TAPE_RES_E: return export_list(r.res, true, dst, nbytes, needed, s);
-      case DBM_TAPE_GAP_START: src = r.gap.start; n = r.P + 1; break;
-      case DBM_TAPE_GAP_ITEM: return export_list(r.gap, false, dst, nbytes, needed, s);
-      case DBM_TAPE_GAP_BITS: src = r.gap.bits; n = r.gap.n; break;
-      case DBM_TAPE_GAP_E: return export_list(r.gap, true, dst, nbytes, needed, s);
+      case DBM_TAPE_REFINE_START: return export_list(r.ref.f, 0, dst, nbytes, needed, s);
+      case DBM_TAPE_REFINE_ITEM: return export_list(r.ref.f, 1, dst, nbytes, needed, s);
+      case DBM_TAPE_REFINE_E: return export_list(r.ref.f, 2, dst, nbytes, needed, s);
+      case DBM_TAPE_RES_START: return export_list(r.res.f, 0, dst, nbytes, needed, s);
+      case DBM_TAPE_RES_ITEM: return export_list(r.res.f, 1, dst, nbytes, needed, s);
+      case DBM_TAPE_RES_E: return export_list(r.res.f, 2, dst, nbytes, needed, s);
+      case DBM_TAPE_GAP_START: return export_list(r.gap.f, 0, dst, nbytes, needed, s);
+      case DBM_TAPE_GAP_ITEM: return export_list(r.gap.f, 1, dst, nbytes, needed, s);
+      case DBM_TAPE_GAP_BITS: return export_list(r.gap.f, 3, dst, nbytes, needed, s);
+      case DBM_TAPE_GAP_E: return export_list(r.gap.f, 2, dst, nbytes, needed, s);
       case DBM_TAPE_INST_START: src = r.inst_start; n = n_inst + 1; break;
       default: set_last_error("tape export: unknown array %d", what); return DBM_ERR_INVALID;
     }

@@ -676,7 +676,8 @@ struct SimImpl : SimBase {
   cudaStream_t own = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  unsigned long long graph_kernels = 0;
+  cudaGraphExec_t graph_tr[2] = {nullptr, nullptr};  // the same step writing every intermediate
+  unsigned long long graph_kernels = 0, graph_tr_kernels = 0;
   int trace_on = 0;
   // shared-memory tiling (2D)
   bool tiled = false;
@@ -687,6 +688,8 @@ struct SimImpl : SimBase {
 
   ~SimImpl() override {
     for (auto& g : graph)
+      if (g) cudaGraphExecDestroy(g);
+    for (auto& g : graph_tr)
       if (g) cudaGraphExecDestroy(g);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
@@ -914,11 +917,12 @@ struct SimImpl : SimBase {
   }
 
   void invalidate_graphs() override {
-    for (auto& g : graph)
-      if (g) {
-        cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
+    for (auto* set : {graph, graph_tr})
+      for (int i = 0; i < 2; ++i)
+        if (set[i]) {
+          cudaGraphExecDestroy(set[i]);
+          set[i] = nullptr;
+        }
   }
 
   void bind() {
@@ -1101,7 +1105,27 @@ struct SimImpl : SimBase {
     DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
     bind();
     int rc = h->before(&args, own);
-    if (rc == DBM_OK) rc = launch_step(own, 99);
+    if (rc == DBM_OK) {
+      if (use_graphs) {  // the step with every intermediate kept, captured once per buffer parity
+        if (!graph_tr[cur]) {
+          const unsigned long long before = g_launches;
+          cudaGraph_t gr;
+          DBM_CUDA(cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal));
+          rc = launch_step(own, 99);
+          cudaError_t e = cudaStreamEndCapture(own, &gr);
+          if (rc != DBM_OK) { trace_on = keep; return rc; }
+          if (e != cudaSuccess) { trace_on = keep; set_last_error("graph capture failed: %s", cudaGetErrorString(e)); return DBM_ERR_CUDA; }
+          graph_tr_kernels = g_launches - before;
+          g_launches = before;
+          DBM_CUDA(cudaGraphInstantiate(&graph_tr[cur], gr, 0));
+          cudaGraphDestroy(gr);
+        }
+        DBM_CUDA(cudaGraphLaunch(graph_tr[cur], own));
+        count_launch(graph_tr_kernels);
+      } else {
+        rc = launch_step(own, 99);
+      }
+    }
     if (rc == DBM_OK) rc = h->after(&args, own);
     trace_on = keep;
     if (rc != DBM_OK) return rc;
