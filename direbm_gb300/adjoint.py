@@ -35,6 +35,7 @@ class Tape:
         with torch.cuda.device(sim.device):
             _lib.check(self.lib.dbm_tape_create(sim.handle, ctypes.byref(h)), "dbm_tape_create")
         self._h = h
+        self._counts = []
 
     def close(self):
         if getattr(self, "_h", None):
@@ -49,20 +50,28 @@ class Tape:
 
     def clear(self):
         _lib.check(self.lib.dbm_tape_clear(self._h), "dbm_tape_clear")
+        self._counts = []
 
     def step(self):
         """Advance the simulator one step and record it."""
         with torch.cuda.device(self.sim.device):
             _lib.check(self.lib.dbm_tape_step(self._h, _stream()), "dbm_tape_step")
         self.sim.iteration += 1
+        self._counts.append(self._query_counts(len(self._counts)))
 
     def __len__(self) -> int:
         return int(self.lib.dbm_tape_length(self._h))
 
-    def counts(self, i: int) -> dict:
+    def _query_counts(self, i: int) -> dict:
         c = (ctypes.c_int64 * 8)()
         _lib.check(self.lib.dbm_tape_counts(self._h, int(i), c), "dbm_tape_counts")
         return {"M": c[0], "P": c[1], "refine": c[2], "resample": c[3], "gapfill": c[4]}
+
+    def counts(self, i: int) -> dict:
+        """Moments in (M), control points out (P) and the pair counts of recorded step i."""
+        if 0 <= i < len(self._counts):
+            return self._counts[i]
+        return self._query_counts(i)
 
     def backward(self, i: int, g_off_out: torch.Tensor, g_f_out: torch.Tensor, g_tau: torch.Tensor):
         """Cotangents of step i's output (offsets (P, D) in cell units, f (P, Q)) -> those of its
@@ -71,8 +80,10 @@ class Tape:
         sim = self.sim
         D, Q = sim.lattice.D, sim.lattice.Q
         dev = sim.device
-        g_off_out = g_off_out.to(device=dev, dtype=torch.float64).contiguous()
-        g_f_out = g_f_out.to(device=dev, dtype=torch.float64).contiguous()
+        if g_off_out.dtype != torch.float64 or not g_off_out.is_contiguous() or g_off_out.device != dev:
+            g_off_out = g_off_out.to(device=dev, dtype=torch.float64).contiguous()
+        if g_f_out.dtype != torch.float64 or not g_f_out.is_contiguous() or g_f_out.device != dev:
+            g_f_out = g_f_out.to(device=dev, dtype=torch.float64).contiguous()
         if g_off_out.shape != (c["P"], D) or g_f_out.shape != (c["P"], Q):
             raise ValueError(f"tape backward {i}: expected cotangents ({c['P']}, {D}) and ({c['P']}, {Q})")
         if g_tau.dtype != torch.float64 or not g_tau.is_contiguous() or g_tau.device != dev:

@@ -503,31 +503,23 @@ __global__ void __launch_bounds__(256) k_list(const __grid_constant__ Args<Q, D,
 
 // ---- backward kernels ---------------------------------------------------------------------------
 
-// Output cotangents (row-major FP64) -> working layout [D][P], [Q][P].
-template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_bwd_in(const __grid_constant__ RecK<Q, D, P> K, const double* __restrict__ goff,
-                                                const double* __restrict__ gf, typename P::real* __restrict__ xbarP,
-                                                typename P::real* __restrict__ fbarG) {
-  using real = typename P::real;
-  const int64_t Pn = K.r.P;
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
-#pragma unroll
-    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] = (real)goff[j * D + a];
-#pragma unroll
-    for (int k = 0; k < Q; ++k) fbarG[(int64_t)k * Pn + j] = (real)gf[j * Q + k];
-  }
-}
-
-// Gap fill, CP side: F_jk = r rho_rest W_k / s_jk for the filled entries.  d s_jk / d p_j = sum of
+// Output cotangents into the working layout, then the gap fill, CP side: F_jk = r rho_rest W_k / s_jk
+// for the filled entries.  d s_jk / d p_j = sum of
 // unit vectors u_jl (e = p_l - p_j); the neighbours' share (-u_jl) comes from sbar (kept per CP and
 // direction) in k_bwd_gap_t.  Filled entries do not depend on the gather: their cotangent is cleared.
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_bwd_gap(const __grid_constant__ RecK<Q, D, P> K, typename P::real* __restrict__ xbarP,
+__global__ void __launch_bounds__(256) k_bwd_gap(const __grid_constant__ RecK<Q, D, P> K, const double* __restrict__ goff,
+                                                 const double* __restrict__ gf, typename P::real* __restrict__ xbarP,
                                                  typename P::real* __restrict__ fbarG, typename P::real* __restrict__ sbarG) {
   using real = typename P::real;
   const int64_t Pn = K.r.P;
   const auto& L = K.r.gap.f;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < Pn; j += (int64_t)gridDim.x * blockDim.x) {
+    // the output cotangents (row-major FP64) into the working layout [D][P], [Q][P]
+#pragma unroll
+    for (int a = 0; a < D; ++a) xbarP[(int64_t)a * Pn + j] = (real)goff[j * D + a];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) fbarG[(int64_t)k * Pn + j] = (real)gf[j * Q + k];
     const uint32_t em = K.r.emask[j];
     real sbar[Q];
 #pragma unroll
@@ -610,7 +602,7 @@ template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK<Q, D, P> K,
                                                     const typename P::real* __restrict__ fbarG,
                                                     typename P::real* __restrict__ fsbar, typename P::real* __restrict__ ybar,
-                                                    typename P::real* __restrict__ Gc) {
+                                                    typename P::real* __restrict__ Gc, typename P::real* __restrict__ wexp) {
   using real = typename P::real;
   const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
   const auto& L = K.r.res.t;
@@ -630,7 +622,9 @@ __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK
     }
     fsbar[t] = G;
     Gc[t] = G;
-    const real fsi = rec_fstar<Q, D, P>(K, m, k) * inv;
+    const real fst = rec_fstar<Q, D, P>(K, m, k);
+    wexp[t] = exp(fst);  // the refine weight, kept for the refine kernels
+    const real fsi = fst * inv;
     real y[3] = {0, 0, 0};
     for (uint32_t q = q0; q < q1; ++q) {
       const auto pr = L.rec[q];
@@ -651,6 +645,7 @@ __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_rows(const __grid_constant__ RecK<Q, D, P> K,
                                                   const typename P::real* __restrict__ Gc,
+                                                  const typename P::real* __restrict__ wexp,
                                                   const typename P::real* __restrict__ fbarG,
                                                   typename P::real* __restrict__ xrow, typename P::real* __restrict__ Wrow,
                                                   typename P::real* __restrict__ sxrow) {
@@ -679,7 +674,7 @@ __global__ void __launch_bounds__(256) k_bwd_rows(const __grid_constant__ RecK<Q
     for (uint32_t p = R.start[rw], pe = p + R.cnt[rw]; p < pe; ++p) {
       const auto pr = R.rec[p];
       const uint32_t i = pr.item;
-      const real w = exp(rec_fstar<Q, D, P>(K, i / Q, (int)(i % Q)));
+      const real w = wexp[(int64_t)(i % Q) * M + i / Q];
       W += w;
 #pragma unroll
       for (int a = 0; a < D; ++a) sx[a] += w * pr.e[a];
@@ -739,6 +734,7 @@ __global__ void __launch_bounds__(256) k_bwd_comp(const __grid_constant__ RecK<Q
                                                   const typename P::real* __restrict__ xbarP,
                                                   const typename P::real* __restrict__ Wj, const typename P::real* __restrict__ sj,
                                                   const typename P::real* __restrict__ cenbar, int64_t ncells,
+                                                  const typename P::real* __restrict__ wexp,
                                                   typename P::real* __restrict__ fsbar, typename P::real* __restrict__ ybar) {
   using real = typename P::real;
   const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
@@ -757,7 +753,7 @@ __global__ void __launch_bounds__(256) k_bwd_comp(const __grid_constant__ RecK<Q
     }
     const uint32_t q0 = L.start[t], q1 = q0 + L.cnt[t];
     if (q0 < q1) {
-      const real w = exp(rec_fstar<Q, D, P>(K, m, k));
+      const real w = wexp[t];
       for (uint32_t q = q0; q < q1; ++q) {
         const auto pr = L.rec[q];
         const uint32_t j = pr.row;
@@ -965,6 +961,8 @@ struct TapeImpl : TapeBase, StepHook {
   uint32_t* hbuf = nullptr;    // pinned host words read back while recording
   uint32_t* d_count = nullptr; // slot counters of the six lists
   double per_row[6] = {16, 16, 16, 16, 4, 4};  // capacity estimate: pairs per row, grown as seen
+  uint64_t known_version = ~0ull - 1;  // simulator state version right after this tape's last step
+  uint32_t known_P = 0;                // and its moment count
   cudaEvent_t done = nullptr;
 
   explicit TapeImpl(SimBase* s) : sim(s) {}
@@ -999,8 +997,11 @@ struct TapeImpl : TapeBase, StepHook {
 
   int step(cudaStream_t s) override {
     cur = StepRec<real, D>{};
+    known_version = ~0ull - 1;
     DBM_TRY(sim->step_hooked(this, s));
     steps.push_back(cur);
+    known_version = sim->version;
+    known_P = (uint32_t)cur.P;
     return DBM_OK;
   }
 
@@ -1019,9 +1020,14 @@ struct TapeImpl : TapeBase, StepHook {
     n_inst = A.n_inst;
     R = A.R;
     ncells = A.ncells;
-    const uint32_t* src[1] = {A.a.count};
-    DBM_TRY(fetch(src, 1, s));
-    const uint32_t M = hbuf[0];
+    uint32_t M;
+    if (sim->version == known_version + 1) {  // the state is the output of this tape's last step
+      M = known_P;
+    } else {
+      const uint32_t* src[1] = {A.a.count};
+      DBM_TRY(fetch(src, 1, s));
+      M = hbuf[0];
+    }
     if (wk) DBM_CUDA(cudaMemcpyAsync(wk, L.w, sizeof(double) * Q, cudaMemcpyHostToDevice, s));
     StepRec<real, D>& r = cur;
     r.M = M;
@@ -1180,7 +1186,7 @@ struct TapeImpl : TapeBase, StepHook {
     }
     DBM_CUDA(cudaStreamWaitEvent(s, done, 0));  // the previous call's scratch is free
     bwd_mem.reset();
-    real *xbarP, *fbarG, *sbarG, *fsbar, *ybar, *Gc, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
+    real *xbarP, *fbarG, *sbarG, *fsbar, *ybar, *Gc, *wexp, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
     double *taupart, *blocksum;
     DBM_TRY(bwd_mem.get(&xbarP, (int64_t)D * Pn));
     DBM_TRY(bwd_mem.get(&fbarG, (int64_t)Q * Pn));
@@ -1188,6 +1194,7 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_TRY(bwd_mem.get(&fsbar, QM));
     DBM_TRY(bwd_mem.get(&ybar, (int64_t)D * QM));
     DBM_TRY(bwd_mem.get(&Gc, QM));
+    DBM_TRY(bwd_mem.get(&wexp, QM));
     DBM_TRY(bwd_mem.get(&xrow, (int64_t)D * PQ));
     DBM_TRY(bwd_mem.get(&Wrow, PQ));
     DBM_TRY(bwd_mem.get(&sxrow, (int64_t)D * PQ));
@@ -1199,27 +1206,25 @@ struct TapeImpl : TapeBase, StepHook {
     const RecK<Q, D, P> K = reck(r);
     DBM_CUDA(cudaMemsetAsync(cenbar, 0, sizeof(real) * (size_t)D * ncells, s));
     if (Pn > 0) {
-      k_bwd_in<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, goff_out, gf_out, xbarP, fbarG);
+      k_bwd_gap<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, goff_out, gf_out, xbarP, fbarG, sbarG);
       DBM_LAUNCH_CHECK();
       if (r.gap.f.n > 0) {
-        k_bwd_gap<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xbarP, fbarG, sbarG);
-        DBM_LAUNCH_CHECK();
         k_bwd_gap_t<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, sbarG, xbarP);
         DBM_LAUNCH_CHECK();
       }
     }
     if (M > 0) {
-      k_bwd_gather<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, fbarG, fsbar, ybar, Gc);
+      k_bwd_gather<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, fbarG, fsbar, ybar, Gc, wexp);
       DBM_LAUNCH_CHECK();
     }
     if (Pn > 0) {
-      k_bwd_rows<Q, D, P><<<grid_for(PQ), 256, 0, s>>>(K, Gc, fbarG, xrow, Wrow, sxrow);
+      k_bwd_rows<Q, D, P><<<grid_for(PQ), 256, 0, s>>>(K, Gc, wexp, fbarG, xrow, Wrow, sxrow);
       DBM_LAUNCH_CHECK();
       k_bwd_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xrow, Wrow, sxrow, xbarP, Wj, sj, cenbar, ncells);
       DBM_LAUNCH_CHECK();
     }
     if (M > 0) {
-      k_bwd_comp<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, xbarP, Wj, sj, cenbar, ncells, fsbar, ybar);
+      k_bwd_comp<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, xbarP, Wj, sj, cenbar, ncells, wexp, fsbar, ybar);
       DBM_LAUNCH_CHECK();
       k_bwd_moment<Q, D, P><<<grid_for(M), 256, 0, s>>>(K, fsbar, ybar, goff_in, gf_in, taupart);
       DBM_LAUNCH_CHECK();

@@ -962,6 +962,7 @@ struct SimImpl : SimBase {
     if (m < 0 || m > mcap) { set_last_error("set_state: %lld moments exceed capacity %lld", (long long)m, (long long)mcap); return DBM_ERR_CAPACITY; }
     if (m > 0 && (!inst_of || !pos || !fin)) { set_last_error("set_state: null input"); return DBM_ERR_INVALID; }
     cur = 0;
+    ++version;
     return import_sorted_states(m, s, inst_of, pos, fin);
   }
 
@@ -1030,6 +1031,7 @@ struct SimImpl : SimBase {
 
   int step(int n, cudaStream_t s) override {
     if (n <= 0) return DBM_OK;
+    ++version;
     DBM_CUDA(cudaEventRecord(ev_in, s));
     DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
     for (int i = 0; i < n; ++i) {
@@ -1064,6 +1066,7 @@ struct SimImpl : SimBase {
   // receives the 6 stage durations (collide, thin+refine, compaction+sort+finalize, weights,
   // gather, emit) measured on the stream the kernels run on.
   int profile_step(float* stage_ms, cudaStream_t s) override {
+    ++version;
     cudaEvent_t ev[7];
     for (auto& e : ev) DBM_CUDA(cudaEventCreate(&e));
     DBM_CUDA(cudaEventRecord(ev_in, s));
@@ -1085,6 +1088,7 @@ struct SimImpl : SimBase {
 
   int step_partial(int upto, cudaStream_t s) override {
     trace_on = 1;
+    ++version;
     DBM_CUDA(cudaEventRecord(ev_in, s));
     DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
     int rc = launch_step(own, upto);
@@ -1100,6 +1104,7 @@ struct SimImpl : SimBase {
   // collision and after the emit (the adjoint records its tape there).
   int step_hooked(StepHook* h, cudaStream_t s) override {
     const int keep = trace_on;
+    ++version;
     trace_on = 1;
     DBM_CUDA(cudaEventRecord(ev_in, s));
     DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
@@ -1202,6 +1207,7 @@ struct SimImpl : SimBase {
     DBM_CUDA(cudaEventRecord(ev_in, s));
     DBM_CUDA(cudaStreamWaitEvent(own, ev_in, 0));
     cur = 0;
+    ++version;
     bind();
     StateP<P>& S = st[0];
     const char* p = (const char*)src + snap_align(sizeof(SnapHeader));

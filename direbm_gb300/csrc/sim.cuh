@@ -195,6 +195,7 @@ struct SimBase {
   virtual void invalidate_graphs() = 0;
   int use_graphs = 1;
   int use_tiles = 1;
+  uint64_t version = 0;  // bumped by every change of the state (load, step, restore)
   int lattice = 0;
   int precision = 0;
   int n_inst = 0;
