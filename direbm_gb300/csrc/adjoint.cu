@@ -964,9 +964,14 @@ struct TapeImpl : TapeBase, StepHook {
   uint64_t known_version = ~0ull - 1;  // simulator state version right after this tape's last step
   uint32_t known_P = 0;                // and its moment count
   cudaEvent_t done = nullptr;
+  cudaStream_t side = nullptr;   // second stream for the recording kernels
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   explicit TapeImpl(SimBase* s) : sim(s) {}
   ~TapeImpl() override {
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     if (done) cudaEventDestroy(done);
     if (hbuf) cudaFreeHost(hbuf);
     if (d_count) cudaFree(d_count);
@@ -974,6 +979,9 @@ struct TapeImpl : TapeBase, StepHook {
 
   int init() {
     DBM_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    DBM_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    DBM_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    DBM_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     DBM_CUDA(cudaMallocHost(&hbuf, 64));
     DBM_CUDA(cudaMalloc(&d_count, 6 * 4));
     DBM_TRY(rec_mem.get(&wk, Q));
@@ -1142,7 +1150,13 @@ struct TapeImpl : TapeBase, StepHook {
       const int64_t cap = (int64_t)(per_row[kind] * 1.25 * (double)rows[kind]) + 1024;
       DBM_TRY(alloc_list(list_of(r, kind), rows[kind], cap, kind == kGapCP));
     }
-    for (int kind = 0; kind < 6; ++kind) DBM_TRY(launch_list(A, r, kind, cp_of_cell, s));
+    // CP-side lists on s, component-side and gap lists on a second stream: they are independent
+    DBM_CUDA(cudaEventRecord(ev_fork, s));
+    DBM_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+    for (int kind : {kRefineCP, kResCP}) DBM_TRY(launch_list(A, r, kind, cp_of_cell, s));
+    for (int kind : {kRefineComp, kResComp, kGapCP, kGapNb}) DBM_TRY(launch_list(A, r, kind, cp_of_cell, side));
+    DBM_CUDA(cudaEventRecord(ev_join, side));
+    DBM_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
     const uint32_t* src[6] = {d_count, d_count + 1, d_count + 2, d_count + 3, d_count + 4, d_count + 5};
     DBM_TRY(fetch(src, 6, s));
     uint32_t need[6];
