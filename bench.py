@@ -454,6 +454,25 @@ def run_reference(args):
 
 # ---- main ----------------------------------------------------------------------------------------
 
+def max_over_ranks(ms: float, dist=None) -> float:
+    """The slowest rank's time (every rank gets it); a plain float without a process group.  The
+    tensor lives where the group's backend wants it (CUDA for NCCL, host for gloo)."""
+    if dist is None or not dist.is_initialized():
+        return float(ms)
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(moments_per_rank: int, world: int, steps: int, ms: float) -> float:
+    """Point-steps/s of the whole job: every rank advances its own replica of the ensemble
+    (weak scaling), so the work is world x moments x steps over the slowest rank's time."""
+    return world * moments_per_rank * steps / (ms * 1e-3)
+
+
 def run_ours(args):
     import torch
 
@@ -484,13 +503,10 @@ def run_ours(args):
     clk.start()
     ms, launches = timed_steps(sim, args.steps, args.warmup)
     clocks = clk.stop()
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     P = sim.count()
     sim.check_status()
-    value = world * M * args.steps / (ms * 1e-3)
+    value = whole_job_rate(M, world, args.steps, ms)
 
     if rank != 0:
         if dist:
