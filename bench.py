@@ -62,6 +62,11 @@ KERNEL_BYTES = {
     "sort": ("cp", 0, 3 * 20 + 8 + 24),
 }
 
+# DRAM bytes per input moment measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
+# one launch on a 4.18 M-moment case of this workload (profiles/gather_t_full_ensemble64.md);
+# traffic grows with the moments, so a full launch's traffic is this times M.
+KERNEL_TRAFFIC_PER_MOMENT = {"gather": 169.5}
+
 # Per point-step byte model of the method (components materialised as 12-byte sort records):
 # B = M(Qs+b_p) + Nc k_b + 2 Nc k_b + 3(Nc k_b + M(Qs+b_p)) + 3 P b_p + P(Qs+b_p), with P ~ M,
 # s = 4, b_p = 8D (int cell + FP32 offset per axis), k_b = 12 -> 956 B for D2Q9 FP32.
@@ -208,9 +213,13 @@ def roofline_from_profile(sim, M, P, peak):
     unit, per_m, per_c = KERNEL_BYTES[dom]
     nbytes = per_m * M + per_c * (P if unit != "moment+cell" else sim.ncells)
     achieved = nbytes / (avg[dom] * 1e-3) / 1e9
+    per_m = KERNEL_TRAFFIC_PER_MOMENT.get(dom)
+    traffic = int(per_m * M) if per_m else None
     return dom, avg, {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                      "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": int(nbytes),
-                      "ms_per_launch": avg[dom], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}
+                      "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
+                      "ms_per_launch": avg[dom], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                      "traffic_source": ("ncu DRAM bytes of a 4.18 M-moment launch, scaled by moments "
+                                         "(profiles/gather_t_full_ensemble64.md)") if per_m else None}
 
 
 def velocity_l2(f, lat):
@@ -332,7 +341,7 @@ def e2e_leg(sim, ib, x, f, steps=2):
             "path": "Simulation.set_state/step/state (C ABI dbm_sim_*) with pinned host buffers"}
 
 
-def adjoint_leg(n=256, steps=100, every=10, tau=0.6):
+def adjoint_leg(n=256, steps=100, every=10, tau=0.6, precisions=("fp32dev", "fp64")):
     """Inverse problem: one periodic D2Q9 run of n x n = 64k jittered points, unit density, initial
     velocity from 8 Fourier modes (16 coefficients, seed 21, RMS 0.02); loss = mean |u(f_T) - u*(x_T)|^2
     against a target 8-mode field (seed 1000); gradient w.r.t. the 16 coefficients and tau through
@@ -351,7 +360,7 @@ def adjoint_leg(n=256, steps=100, every=10, tau=0.6):
     out = {"config": f"{n}x{n} jittered points, periodic D2Q9, tau {tau}, r 1.5h, cell h, {steps} steps, "
                      f"checkpoint every {every}; 16 mode coefficients + tau", "steps": steps, "checkpoint_every": every}
     grads = {}
-    for prec in ("fp32dev", "fp64"):
+    for prec in precisions:
         sim = make_sim([n], [tau], prec, 4 * len(x))
         # plain forward step (captured graphs), the reference cost of one step
         f0 = eq_np(np.ones(len(x)), field(torch.as_tensor(x), torch.as_tensor(field.coeffs)).numpy(), D2Q9)
@@ -384,8 +393,10 @@ def adjoint_leg(n=256, steps=100, every=10, tau=0.6):
         }
         tape.close()
         sim.close()
-    out["fp32dev_grad_rel_err_vs_fp64"] = float(np.linalg.norm(grads["fp32dev"] - grads["fp64"]) /
-                                                 np.linalg.norm(grads["fp64"]))
+    if "fp32dev" in grads and "fp64" in grads:
+        out["fp32dev_grad_rel_err_vs_fp64"] = float(np.linalg.norm(grads["fp32dev"] - grads["fp64"]) /
+                                                     np.linalg.norm(grads["fp64"]))
+        out["fp32dev_loss_rel_err_vs_fp64"] = abs(out["fp32dev"]["loss"] / out["fp64"]["loss"] - 1.0)
     return out
 
 
@@ -569,6 +580,10 @@ def main():
     ap.add_argument("--instances", type=int, default=N_INST, help="first N ensemble members (profiling runs)")
     ap.add_argument("--legs", default="all", choices=["all", "main", "adjoint"],
                     help="main = timed step only; adjoint = the inverse-problem leg only")
+    ap.add_argument("--adjoint-n", type=int, default=256, help="adjoint leg: points per side")
+    ap.add_argument("--adjoint-steps", type=int, default=100, help="adjoint leg: rollout steps")
+    ap.add_argument("--adjoint-every", type=int, default=10, help="adjoint leg: checkpoint interval")
+    ap.add_argument("--adjoint-precisions", default="fp32dev,fp64", help="adjoint leg: stores to run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -576,7 +591,8 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"adjoint": adjoint_leg()}), flush=True)
+        print(json.dumps({"adjoint": adjoint_leg(args.adjoint_n, args.adjoint_steps, args.adjoint_every,
+                                                 precisions=tuple(args.adjoint_precisions.split(",")))}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)
