@@ -835,6 +835,13 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
     for (int k = 0; k < Q; ++k) {
       const real* ginv = A.sw + (int64_t)k * A.mcap;
       const real* gfk = F64 ? (const real*)(A.a.f64 + (int64_t)k * A.mcap) : (const real*)(A.a.dev + (int64_t)k * A.mcap);
+      // stage (1/sw, f_k) of every region item for this direction
+      __syncthreads();
+      for (int l = threadIdx.x; l < nstaged; l += blockDim.x) {
+        const int gm = s_gi[l];
+        s_kv[l] = Pair<real>{ginv[gm], gfk[gm]};
+      }
+      __syncthreads();
       const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
       for (int i = threadIdx.x; i < nc; i += blockDim.x) {
         const int bx = s_bx[i], by = s_by[i];
@@ -859,8 +866,7 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
             const real ex = rn_add(it.ox, cx), ey = rn_add(it.oy, cy);
             const real d2 = rn_add(rn_mul(ex, ex), rn_mul(ey, ey));
             if (d2 <= A.R2) {
-              const int gm = s_gi[m];
-              const Pair<real> kv{__ldg(ginv + gm), __ldg(gfk + gm)};
+              const Pair<real> kv = s_kv[m];
               if (kv.x > (real)0) {
                 const real wgt = (A.R - rn_sqrt(d2)) * kv.x;
                 if constexpr (F64) {
