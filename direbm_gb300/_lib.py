@@ -108,6 +108,7 @@ _SIGS = {
     "dbm_sim_set_option": (ctypes.c_int, [_vp, _i32, _i32]),
     "dbm_sim_trace": (ctypes.c_int, [_vp, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp]),
     "dbm_sim_device_bytes": (_i64, [_vp]),
+    "dbm_sim_get_tiling": (ctypes.c_int, [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
     "dbm_sim_set_tau": (ctypes.c_int, [_vp, _vp, _i32]),
     "dbm_sim_snapshot": (ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp]),
     "dbm_sim_restore": (ctypes.c_int, [_vp, _vp, _i64, _vp]),

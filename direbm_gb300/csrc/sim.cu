@@ -683,6 +683,8 @@ struct SimImpl : SimBase {
   bool tiled = false;
   Tile2* d_tiles = nullptr;
   int ntiles = 0;
+  int pgrid[3] = {1, 1, 1};  // persistent grids: thin+refine, weights, gather
+  int use_persistent = 0;
   TileGeo geo{};
   size_t sm_refine = 0, sm_weights = 0, sm_gather = 0;
 
@@ -861,9 +863,13 @@ struct SimImpl : SimBase {
     return cap;
   }
 
-  int init_tiles(const LatHost& LH, double R) {
-    geo.tx = 32;
-    geo.ty = 8;
+  // Tile geometry for tiles of tx x (256 / tx) cells: halos from the lattice and R, staging
+  // capacities from the shared-memory budget, the tile list, and the resident blocks per SM of the
+  // three tiled kernels (the grid of their persistent launch).
+  int init_tiles(const LatHost& LH, double R, int tx = 32) {
+    if (tx < 8 || tx > 128 || 256 % tx) { set_last_error("tile width %d: must divide 256, 8..128", tx); return DBM_ERR_INVALID; }
+    geo.tx = tx;
+    geo.ty = 256 / tx;
     const double tiny = 2e-4;
     Halo m{0, 0, 0, 0}, c{0, 0, 0, 0};
     for (int k = 0; k < Q; ++k) {
@@ -902,6 +908,11 @@ struct SimImpl : SimBase {
       for (int y0 = 0; y0 < inst_h[i].dims[1]; y0 += geo.ty)
         for (int x0 = 0; x0 < inst_h[i].dims[0]; x0 += geo.tx) tiles.push_back({i, x0, y0});
     ntiles = (int)tiles.size();
+    if (d_tiles) {  // re-tiling: release the previous list
+      cudaFree(d_tiles);
+      allocs.erase(std::remove(allocs.begin(), allocs.end(), (void*)d_tiles), allocs.end());
+      d_tiles = nullptr;
+    }
     DBM_TRY(alloc(&d_tiles, ntiles));
     DBM_CUDA(cudaMemcpy(d_tiles, tiles.data(), sizeof(Tile2) * ntiles, cudaMemcpyHostToDevice));
     if constexpr (D == 2) {
@@ -911,10 +922,35 @@ struct SimImpl : SimBase {
                                     (int)sm_weights));
       DBM_CUDA(cudaFuncSetAttribute((const void*)k_gather_t<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)sm_gather));
+      int nb[3] = {1, 1, 1};
+      DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[0], k_thin_refine_t<Q, P>, 256, sm_refine));
+      DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], k_weights_t<Q, P>, 256, sm_weights));
+      DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], k_gather_t<Q, P>, 256, sm_gather));
+      for (int i = 0; i < 3; ++i) pgrid[i] = std::max(1, std::min(ntiles, std::max(nb[i], 1) * sm_count()));
     }
     tiled = true;
     return DBM_OK;
   }
+
+  // Tile width (height 256 / width) and persistent launches of the tiled kernels; results do not
+  // depend on either (each tile is one block with the same per-thread loop order).
+  int set_tiling(int tx, int persistent) {
+    if constexpr (D == 2) {
+      if (tx != geo.tx) DBM_TRY(init_tiles(*lat_host(desc.lattice), desc.r_res / desc.cell, tx));
+      use_persistent = persistent ? 1 : 0;
+      invalidate_graphs();
+      return DBM_OK;
+    } else {
+      set_last_error("tiling options apply to 2D lattices only");
+      return DBM_ERR_INVALID;
+    }
+  }
+  int tiling(int* tx, int* persistent) const override {
+    *tx = geo.tx;
+    *persistent = use_persistent;
+    return DBM_OK;
+  }
+  int set_tiling_v(int tx, int persistent) override { return set_tiling(tx, persistent); }
 
   void invalidate_graphs() override {
     for (auto* set : {graph, graph_tr})
@@ -982,7 +1018,8 @@ struct SimImpl : SimBase {
     mark(1, s);
     if (upto <= 1) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled && use_tiles) k_thin_refine_t<Q, P><<<ntiles, 256, sm_refine, s>>>(A, d_tiles, geo);
+      if (tiled && use_tiles)
+        k_thin_refine_t<Q, P><<<use_persistent ? pgrid[0] : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo, ntiles);
       else k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
     } else {
       k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
@@ -1005,7 +1042,8 @@ struct SimImpl : SimBase {
     mark(3, s);
     if (upto <= 3) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled && use_tiles) k_weights_t<Q, P><<<ntiles, 256, sm_weights, s>>>(A, d_tiles, geo);
+      if (tiled && use_tiles)
+        k_weights_t<Q, P><<<use_persistent ? pgrid[1] : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo, ntiles);
       else k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
     } else {
       k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
@@ -1015,7 +1053,8 @@ struct SimImpl : SimBase {
     if (upto <= 4) return DBM_OK;
     DBM_CUDA(cudaMemsetAsync(A.emask, 0, (size_t)ccap * 4, s));
     if constexpr (D == 2) {
-      if (tiled && use_tiles) k_gather_t<Q, P><<<ntiles, 256, sm_gather, s>>>(A, d_tiles, geo);
+      if (tiled && use_tiles)
+        k_gather_t<Q, P><<<use_persistent ? pgrid[2] : ntiles, 256, sm_gather, s>>>(A, d_tiles, geo, ntiles);
       else k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
     } else {
       k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
@@ -1426,7 +1465,12 @@ int dbm_sim_set_option(dbm_sim* s, int32_t option, int32_t value) {
   SIM_CHECK(s);
   if (option == DBM_OPT_GRAPHS) s->impl->use_graphs = value ? 1 : 0;
   else if (option == DBM_OPT_TILES) s->impl->use_tiles = value ? 1 : 0;
-  else {
+  else if (option == DBM_OPT_TILE_WIDTH || option == DBM_OPT_PERSISTENT) {
+    int tx = 0, pers = 0;
+    s->impl->tiling(&tx, &pers);
+    if (option == DBM_OPT_TILE_WIDTH) tx = value; else pers = value;
+    return s->impl->set_tiling_v(tx, pers);
+  } else {
     set_last_error("dbm_sim_set_option: unknown option %d", option);
     return DBM_ERR_INVALID;
   }
@@ -1445,6 +1489,15 @@ int dbm_sim_trace(dbm_sim* s, int32_t what, void* dst, int64_t bytes, int64_t* n
 int64_t dbm_sim_device_bytes(dbm_sim* s) {
   if (!s || !s->impl) return -1;
   return s->impl->device_bytes();
+}
+int dbm_sim_get_tiling(dbm_sim* s, int32_t* tile_width, int32_t* persistent) {
+  SIM_CHECK(s);
+  if (!tile_width || !persistent) return DBM_ERR_INVALID;
+  int tx = 0, pers = 0;
+  DBM_TRY(s->impl->tiling(&tx, &pers));
+  *tile_width = tx;
+  *persistent = pers;
+  return DBM_OK;
 }
 int dbm_sim_set_tau(dbm_sim* s, const double* tau, int32_t n) {
   SIM_CHECK(s);

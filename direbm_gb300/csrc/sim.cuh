@@ -193,6 +193,8 @@ struct SimBase {
   virtual int restore(const void*, int64_t, cudaStream_t) = 0;
   virtual int64_t device_bytes() const = 0;
   virtual void invalidate_graphs() = 0;
+  virtual int tiling(int* tx, int* persistent) const = 0;
+  virtual int set_tiling_v(int tx, int persistent) = 0;
   int use_graphs = 1;
   int use_tiles = 1;
   uint64_t version = 0;  // bumped by every change of the state (load, step, restore)

@@ -488,12 +488,17 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
   }
 }
 
+// The three tiled kernels take a tile list and loop over it with a fixed stride (tile blockIdx.x,
+// blockIdx.x + gridDim.x, ...): launched with one block per tile they are ordinary kernels;
+// launched with fewer blocks (a few per SM) they are persistent.  Either way each tile is processed
+// by one block with the same per-thread loop order, so results do not depend on the launch.
 template <int Q, class P>
 __global__ void __launch_bounds__(256) k_thin_refine_t(const __grid_constant__ Args<Q, 2, P> A,
-                                                      const Tile2* __restrict__ tiles, const TileGeo G) {
+                                                      const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
   using real = typename P::real;
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tile2 T = tiles[blockIdx.x];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+  const Tile2 T = tiles[tb];
   const InstK I = A.inst[T.inst];
   const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
   const int cap = G.cap_refine;
@@ -513,6 +518,8 @@ __global__ void __launch_bounds__(256) k_thin_refine_t(const __grid_constant__ A
     thin_refine_rows<Q, P>(A, I, T, G, rw, rh, s_beg, s_end, s_it, s_w, cap);
   } else {
     thin_refine_body<Q, P, false>(A, I, T, G, rw, rh, s_beg, s_end, nullptr, nullptr, nullptr, 0);
+  }
+  __syncthreads();  // shared memory is restaged for the next tile
   }
 }
 
@@ -690,10 +697,11 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
 
 template <int Q, class P>
 __global__ void __launch_bounds__(256) k_weights_t(const __grid_constant__ Args<Q, 2, P> A,
-                                                  const Tile2* __restrict__ tiles, const TileGeo G) {
+                                                  const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
   using real = typename P::real;
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tile2 T = tiles[blockIdx.x];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+  const Tile2 T = tiles[tb];
   const InstK I = A.inst[T.inst];
   const int rw = G.tx + G.cp.xh - G.cp.xl, rh = G.ty + G.cp.yh - G.cp.yl;
   const int cap = G.cap_weights, cap_t = G.cap_tile;
@@ -713,6 +721,8 @@ __global__ void __launch_bounds__(256) k_weights_t(const __grid_constant__ Args<
                });
   if (s_row[rh + 1]) weights_rows<Q, P>(A, I, T, G, rw, rh, s_beg, s_end, s_cit, s_tr, s_ij, s_bx, s_by, s_mpos);
   else weights_body<Q, P, false>(A, I, T, G, rw, rh, s_beg, s_end, nullptr, s_tr, s_ij, s_bx, s_by, s_mpos);
+  __syncthreads();
+  }
 }
 
 // ---- gather: per control point and direction ------------------------------------------------------
@@ -902,11 +912,12 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
 
 template <int Q, class P>
 __global__ void __launch_bounds__(256) k_gather_t(const __grid_constant__ Args<Q, 2, P> A,
-                                                 const Tile2* __restrict__ tiles, const TileGeo G) {
+                                                 const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
   using real = typename P::real;
   constexpr bool F64 = std::is_same<P, PF64>::value;
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tile2 T = tiles[blockIdx.x];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+  const Tile2 T = tiles[tb];
   const InstK I = A.inst[T.inst];
   const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
   const int cap = G.cap_gather, cap_t = G.cap_tile;
@@ -935,6 +946,8 @@ __global__ void __launch_bounds__(256) k_gather_t(const __grid_constant__ Args<Q
   else
     gather_body<Q, P, false>(A, I, T, G, rw, rh, s_beg, s_end, s_gi, nullptr, s_rho, s_kv, 0, s_tr, s_ij, s_bx, s_by,
                              s_cpos);
+  __syncthreads();
+  }
 }
 
 }  // namespace dbm

@@ -220,6 +220,25 @@ class Simulation:
                        "dbm_sim_trace")
         return buf
 
+    # ---- launch configuration -------------------------------------------------------------------
+    OPT_TILE_WIDTH, OPT_PERSISTENT = 3, 4
+
+    def tiling(self) -> tuple:
+        """(tile width in cells, persistent launches) of the 2D tiled kernels."""
+        w, p = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(self.lib.dbm_sim_get_tiling(self._h, ctypes.byref(w), ctypes.byref(p)), "dbm_sim_get_tiling")
+        return int(w.value), bool(p.value)
+
+    def set_tiling(self, tile_width: int | None = None, persistent: bool | None = None):
+        """Tiles of tile_width x 256/tile_width cells and/or persistent launches (2D only).  Results
+        are bit-identical for every setting; only the speed changes."""
+        with torch.cuda.device(self.device):
+            if tile_width is not None:
+                _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_TILE_WIDTH, int(tile_width)), "set tile width")
+            if persistent is not None:
+                _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_PERSISTENT, 1 if persistent else 0),
+                           "set persistent")
+
     # ---- parameters, checkpoints ----------------------------------------------------------------
     def set_tau(self, tau):
         """Replace every instance's tau (one value per instance, each > 1/2)."""

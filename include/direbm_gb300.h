@@ -165,7 +165,14 @@ int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
  * (2D: shared-memory tiled window kernels, default 1; results are bit-identical either way). */
 #define DBM_OPT_GRAPHS 1
 #define DBM_OPT_TILES 2
+/* DBM_OPT_TILE_WIDTH (2D): tiles of w x 256/w cells, w in {8, 16, 32, 64, 128} (default 32);
+ * DBM_OPT_PERSISTENT (2D): launch the tiled kernels with a few resident blocks per SM that loop
+ * over the tile list (default 0).  Neither changes any result bit; direbm_gb300.autotune picks them
+ * by timing. */
+#define DBM_OPT_TILE_WIDTH 3
+#define DBM_OPT_PERSISTENT 4
 int dbm_sim_set_option(dbm_sim* sim, int32_t option, int32_t value);
+int dbm_sim_get_tiling(dbm_sim* sim, int32_t* tile_width, int32_t* persistent);
 /* Run one step but stop after `stage` (1 collide, 2 thin+refine, 3 sort, 4 weights, 5 gather,
  * 6 emit) so intermediates can be exported with dbm_sim_trace. */
 int dbm_sim_step_partial(dbm_sim* sim, int32_t stage, void* stream);
