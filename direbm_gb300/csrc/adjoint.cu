@@ -1022,6 +1022,10 @@ struct TapeImpl : TapeBase, StepHook {
 
   int before(const void* av, cudaStream_t s) override {
     const Args<Q, D, P>& A = *(const Args<Q, D, P>*)av;
+    if (A.any_obstacle) {
+      set_last_error("tape: the adjoint does not cover obstacles (bounced components)");
+      return DBM_ERR_INVALID;
+    }
     L = A.L;
     inst = A.inst;
     inst_base = A.inst_base;

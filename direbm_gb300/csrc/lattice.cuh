@@ -5,6 +5,8 @@
 // second-order form with the lattice's cs^2 (direbm/physics.py:29-45, warp/physics.py:31-42).
 #pragma once
 
+#include <cmath>
+
 #include "common.cuh"
 
 namespace dbm {
@@ -40,6 +42,7 @@ struct LatK {
   double cd[Q][D]; // c * dx / cell (cell units)
   float cdf[Q][D]; // float(c * dx / cell)
   double inv_cs2;
+  int opp[Q];      // index of -c_k
 };
 
 template <int Q, int D>
@@ -58,6 +61,14 @@ LatK<Q, D> make_latk(const LatHost& h, double dx, double cell) {
     }
   }
   k.inv_cs2 = 1.0 / h.cs2;
+  for (int q = 0; q < Q; ++q) {
+    k.opp[q] = q;
+    for (int r = 0; r < Q; ++r) {
+      bool neg = true;
+      for (int a = 0; a < D; ++a) neg = neg && std::fabs(h.c[r][a] + h.c[q][a]) < 1e-12;
+      if (neg) { k.opp[q] = r; break; }
+    }
+  }
   return k;
 }
 

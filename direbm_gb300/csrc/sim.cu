@@ -38,27 +38,56 @@ __global__ void __launch_bounds__(256) k_collide(const __grid_constant__ Args<Q,
     const uint32_t g = A.a.cell[m];
     const int b = find_instance(A.inst_base, A.n_inst, g);
     const InstK I = A.inst[b];
+    int c[3] = {0, 0, 0};
+    if (!I.periodic || I.has_obs || I.inflow_w > 0) decode_cell<D>(I, g, c);
+    const bool inflow = I.inflow_w > 0 && c[0] < I.inflow_w;  // reset to the inflow equilibrium
     if constexpr (std::is_same<P, PF64>::value) {
       double f[Q];
 #pragma unroll
       for (int k = 0; k < Q; ++k) f[k] = A.a.f64[(int64_t)k * A.mcap + m];
-      collide_moment<Q, D, double>(f, I.tau, A.L);
+      if (inflow) {
+        double rho = 0, u[D];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) rho += f[k];
+#pragma unroll
+        for (int a = 0; a < D; ++a) u[a] = I.u_in[a];
+        equilibrium_all<Q, D, double>(rho, u, A.L, f);
+      } else {
+        collide_moment<Q, D, double>(f, I.tau, A.L);
+      }
 #pragma unroll
       for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + m] = f[k];
     } else {
       float dv[Q];
 #pragma unroll
       for (int k = 0; k < Q; ++k) dv[k] = A.a.dev[(int64_t)k * A.mcap + m];
-      collide_moment_dev<Q, D>(A.a.rho[m], dv, (float)I.tau, A.L);
+      if (inflow) {
+        float u[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) u[a] = (float)I.u_in[a];
+        eq_deviation_f32<Q, D>(A.a.rho[m], u, A.L, dv);
+      } else {
+        collide_moment_dev<Q, D>(A.a.rho[m], dv, (float)I.tau, A.L);
+      }
 #pragma unroll
       for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + m] = dv[k];
     }
-    if (!I.periodic) {  // every component must land inside a bounded box
-      int c[3];
-      decode_cell<D>(I, g, c);
+    uint32_t bm = 0;
+    if (I.has_obs) {  // bounce-back: a direction whose end point lies inside the solid is blocked
+#pragma unroll 1
+      for (int k = 1; k < Q; ++k) {
+        double o[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a) o[a] = __dadd_rn((double)A.a.off[(int64_t)a * A.mcap + m], A.L.cd[k][a]);
+        if (inside_sphere<D>(I, c, o)) bm |= 1u << k;
+      }
+    }
+    if (A.any_obstacle) A.bmask[m] = bm;
+    if (!I.periodic) {  // every component must land inside a bounded box (bounced ones stay put)
       bool out = false;
 #pragma unroll
       for (int k = 0; k < Q; ++k) {
+        if ((bm >> k) & 1u) continue;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
           real t = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
@@ -110,6 +139,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
           if (!cell_at<D>(I, Fc[0] + so[0], Fc[1] + so[1], Fc[2] + so[2], &Sg)) continue;
           const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
           for (uint32_t m = m0; m < m1; ++m) {
+            if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: stays in its cell
             real t[3];
             bool land = true;
 #pragma unroll
@@ -127,6 +157,21 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
             }
           }
         }
+  }
+  if (A.any_obstacle) {  // bounced components land in their own cell, at their moment's offset
+    for (uint32_t m = A.a.start[F], m1 = A.a.start[F + 1]; m < m1; ++m) {
+      const uint32_t bits = A.bmask[m];
+#pragma unroll 1
+      for (int k = 1; k < Q; ++k) {
+        if (!((bits >> k) & 1u)) continue;
+        ++cnt;
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          const real rel = A.a.off[(int64_t)a * A.mcap + m];
+          if constexpr (std::is_same<P, PF64>::value) sum[a] += rel; else csum[a].add(rel);
+        }
+      }
+    }
   }
   if (cnt == 0) {
     A.occ[F] = 0u;
@@ -172,6 +217,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
           if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
           const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
           for (uint32_t m = m0; m < m1; ++m) {
+            if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: visited below
             real o[3] = {0, 0, 0}, e[3];
 #pragma unroll
             for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
@@ -181,6 +227,52 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
               if constexpr (std::is_same<P, PF64>::value) {
                 // separate rounding of product and sum (no FMA), in loop order: the oracle
                 // reproduces this sum bit for bit
+                swd = __dadd_rn(swd, w);
+#pragma unroll
+                for (int a = 0; a < D; ++a) sxd[a] = __dadd_rn(sxd[a], __dmul_rn(w, e[a]));
+              } else {
+                swf += w;
+#pragma unroll
+                for (int a = 0; a < D; ++a) sxf[a] = fmaf(w, e[a], sxf[a]);
+              }
+            }
+          }
+        }
+  }
+  if (A.any_obstacle) {
+    // bounced components (displacement 0, opposite label): window order, then moment, then slot
+    int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      lo[a] = (int)floor(cen[a] - A.R - A.tiny);
+      hi[a] = (int)floor(cen[a] + A.R + A.tiny);
+    }
+#pragma unroll 1
+    for (int sz = lo[2]; sz <= hi[2]; ++sz)
+#pragma unroll 1
+      for (int sy = lo[1]; sy <= hi[1]; ++sy)
+#pragma unroll 1
+        for (int sx = lo[0]; sx <= hi[0]; ++sx) {
+          const int dS[3] = {sx, sy, sz};
+          real c[3] = {0, 0, 0};
+#pragma unroll
+          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], (real)0, cen[a]);
+          if (cell_d2_lower<D, real>(c) > A.R2) continue;
+          uint32_t Sg;
+          if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
+          for (uint32_t m = A.a.start[Sg], m1 = A.a.start[Sg + 1]; m < m1; ++m) {
+            const uint32_t bits = A.bmask[m];
+            if (!bits) continue;
+            real o[3] = {0, 0, 0}, e[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+            if (canon_d2<D, real>(o, c, e) > A.R2) continue;
+#pragma unroll 1
+            for (int k = 1; k < Q; ++k) {
+              if (!((bits >> k) & 1u)) continue;
+              mask |= 1u << A.L.opp[k];
+              const real w = exp(fstar_at<Q, D, P>(A, m, k));
+              if constexpr (std::is_same<P, PF64>::value) {
                 swd = __dadd_rn(swd, w);
 #pragma unroll
                 for (int a = 0; a < D; ++a) sxd[a] = __dadd_rn(sxd[a], __dmul_rn(w, e[a]));
@@ -226,8 +318,16 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
     }
   }
   uint32_t G;
-  const bool inside = cell_at<D>(I, Fc[0] + sh[0], Fc[1] + sh[1], Fc[2] + sh[2], &G);
+  bool inside = cell_at<D>(I, Fc[0] + sh[0], Fc[1] + sh[1], Fc[2] + sh[2], &G);
   if (!inside) atomicOr(A.status, ST_OUT_OF_BOX);
+  if (inside && I.has_obs) {  // a point inside the solid is removed
+    int Gc[3];
+    decode_cell<D>(I, G, Gc);
+    double o[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) o[a] = (double)off[a];
+    if (inside_sphere<D>(I, Gc, o)) inside = false;
+  }
   A.occ[F] = inside ? 1u : 0u;
   A.fkey[F] = inside ? G : 0xffffffffu;
 #pragma unroll
@@ -281,10 +381,11 @@ __global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q,
   decode_cell<D>(I, g, Sc);
   real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  const bool bounced = A.any_obstacle && ((A.bmask[m] >> k) & 1u);  // stays at the moment
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     o[a] = A.a.off[(int64_t)a * A.mcap + m];
-    cdk[a] = (real)A.L.cd[k][a];
+    cdk[a] = bounced ? (real)0 : (real)A.L.cd[k][a];
     const real t = rn_add(o[a], cdk[a]);
     lo[a] = (int)floor(t - A.R - A.tiny);
     hi[a] = (int)floor(t + A.R + A.tiny);
@@ -369,6 +470,7 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
         if (!cell_at<D>(I, Gc[0] + sx, Gc[1] + sy, Gc[2] + sz, &Sg)) continue;
         const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
         for (uint32_t m = m0; m < m1; ++m) {
+          if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: label opp[k]
           real o[3] = {0, 0, 0}, e[3];
 #pragma unroll
           for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
@@ -387,6 +489,48 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
           }
         }
       }
+  if (A.any_obstacle && k > 0) {
+    // components of slot kb = opp[k] that bounced carry label k and sit at their moment's offset
+    const int kb = A.L.opp[k];
+    int blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      blo[a] = (int)floor(p[a] - A.R - A.tiny);
+      bhi[a] = (int)floor(p[a] + A.R + A.tiny);
+    }
+#pragma unroll 1
+    for (int sz = blo[2]; sz <= bhi[2]; ++sz)
+#pragma unroll 1
+      for (int sy = blo[1]; sy <= bhi[1]; ++sy)
+#pragma unroll 1
+        for (int sx = blo[0]; sx <= bhi[0]; ++sx) {
+          const int dS[3] = {sx, sy, sz};
+          real c[3] = {0, 0, 0};
+#pragma unroll
+          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], (real)0, p[a]);
+          if (cell_d2_lower<D, real>(c) > A.R2) continue;
+          uint32_t Sg;
+          if (!cell_at<D>(I, Gc[0] + sx, Gc[1] + sy, Gc[2] + sz, &Sg)) continue;
+          for (uint32_t m = A.a.start[Sg], m1 = A.a.start[Sg + 1]; m < m1; ++m) {
+            if (!((A.bmask[m] >> kb) & 1u)) continue;
+            real o[3] = {0, 0, 0}, e[3];
+#pragma unroll
+            for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+            const real d2 = canon_d2<D, real>(o, c, e);
+            if (d2 > A.R2) continue;
+            const real inv = A.sw[(int64_t)kb * A.mcap + m];
+            if (inv > (real)0) {
+              const real wgt = (A.R - rn_sqrt(d2)) * inv;
+              if constexpr (std::is_same<P, PF64>::value) {
+                acc += wgt * A.a.f64[(int64_t)kb * A.mcap + m];
+              } else {
+                sa.add_prod(wgt, A.a.rho[m]);
+                sb.add_prod(wgt, A.a.dev[(int64_t)kb * A.mcap + m]);
+              }
+            }
+          }
+        }
+  }
   bool empty;
   if constexpr (std::is_same<P, PF64>::value) {
     A.cpf64[(int64_t)k * A.ccap + j] = acc;
@@ -820,6 +964,8 @@ struct SimImpl : SimBase {
       DBM_TRY(alloc(&A.cpflo, (int64_t)Q * ccap));
     }
     DBM_TRY(alloc(&A.emask, ccap));
+    DBM_TRY(alloc(&A.bmask, mcap));
+    A.any_obstacle = 0;
     DBM_TRY(alloc(&A.status, 1));
     DBM_TRY(alloc(&A.d_P, 1));
     DBM_CUDA(cudaMemset(A.status, 0, 4));
@@ -1018,7 +1164,7 @@ struct SimImpl : SimBase {
     mark(1, s);
     if (upto <= 1) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled && use_tiles)
+      if (tiled && use_tiles && !A.any_obstacle)
         k_thin_refine_t<Q, P><<<use_persistent ? pgrid[0] : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo, ntiles);
       else k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
     } else {
@@ -1042,7 +1188,7 @@ struct SimImpl : SimBase {
     mark(3, s);
     if (upto <= 3) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled && use_tiles)
+      if (tiled && use_tiles && !A.any_obstacle)
         k_weights_t<Q, P><<<use_persistent ? pgrid[1] : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo, ntiles);
       else k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
     } else {
@@ -1053,7 +1199,7 @@ struct SimImpl : SimBase {
     if (upto <= 4) return DBM_OK;
     DBM_CUDA(cudaMemsetAsync(A.emask, 0, (size_t)ccap * 4, s));
     if constexpr (D == 2) {
-      if (tiled && use_tiles)
+      if (tiled && use_tiles && !A.any_obstacle)
         k_gather_t<Q, P><<<use_persistent ? pgrid[2] : ntiles, 256, sm_gather, s>>>(A, d_tiles, geo, ntiles);
       else k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
     } else {
@@ -1187,6 +1333,60 @@ struct SimImpl : SimBase {
     DBM_CUDA(cudaStreamSynchronize(own));  // no step may still read the table
     for (int i = 0; i < n; ++i) inst_h[i].tau = tau[i];
     DBM_CUDA(cudaMemcpy(dinst, inst_h.data(), sizeof(InstK) * n, cudaMemcpyHostToDevice));
+    return DBM_OK;
+  }
+
+  // A solid sphere (disc in 2D) with bounce-back in instance `b`: center in world units (D values),
+  // radius in world units; radius <= 0 removes it.  A sphere in a periodic box must keep a margin
+  // of one window from the box faces (the blocked test uses the box's own coordinates, no image).
+  int set_obstacle(int b, const double* center, double radius) override {
+    if (b < 0 || b >= (int)inst_h.size() || (radius > 0 && !center)) { set_last_error("set_obstacle: bad arguments"); return DBM_ERR_INVALID; }
+    InstK& I = inst_h[b];
+    if (radius > 0) {
+      const double r = radius / desc.cell;
+      double cmax = 0;
+      const LatHost& LH = *lat_host(desc.lattice);
+      for (int k = 0; k < Q; ++k) {
+        double s2 = 0;
+        for (int a = 0; a < D; ++a) s2 += LH.c[k][a] * LH.c[k][a];
+        cmax = std::max(cmax, std::sqrt(s2) * desc.dx / desc.cell);
+      }
+      const double margin = desc.r_res / desc.cell + cmax + 2;
+      for (int a = 0; a < D; ++a) {
+        const double c = center[a] / desc.cell - I.origin[a];
+        if (I.periodic && (c - r - margin < 0 || c + r + margin > I.dims[a])) {
+          set_last_error("set_obstacle: the sphere must stay %.1f cells away from the faces of a periodic box", margin);
+          return DBM_ERR_INVALID;
+        }
+        I.obs_c[a] = c;
+      }
+      I.obs_r2 = r * r;
+      I.has_obs = 1;
+    } else {
+      I.has_obs = 0;
+    }
+    return push_instances();
+  }
+
+  // An inflow layer in instance `b`: moments in the first `width` cell columns (x) are set to the
+  // equilibrium at velocity u (D values) with their own density instead of colliding.
+  int set_inflow(int b, const double* u, int width) override {
+    if (b < 0 || b >= (int)inst_h.size() || width < 0 || (width > 0 && !u)) { set_last_error("set_inflow: bad arguments"); return DBM_ERR_INVALID; }
+    InstK& I = inst_h[b];
+    I.inflow_w = width;
+    for (int a = 0; a < 3; ++a) I.u_in[a] = (width > 0 && a < D) ? u[a] : 0.0;
+    return push_instances();
+  }
+
+  int push_instances() {
+    DBM_CUDA(cudaStreamSynchronize(own));  // no step may still read the table
+    DBM_CUDA(cudaMemcpy(dinst, inst_h.data(), sizeof(InstK) * inst_h.size(), cudaMemcpyHostToDevice));
+    int any = 0;
+    for (auto& I : inst_h) any |= I.has_obs;
+    if (any != args.any_obstacle) {
+      args.any_obstacle = any;
+      invalidate_graphs();  // captured launches hold the flag
+    }
     return DBM_OK;
   }
 
@@ -1503,6 +1703,14 @@ int dbm_sim_set_tau(dbm_sim* s, const double* tau, int32_t n) {
   SIM_CHECK(s);
   if (!tau) { set_last_error("dbm_sim_set_tau: null tau"); return DBM_ERR_INVALID; }
   return s->impl->set_tau(tau, n);
+}
+int dbm_sim_set_obstacle(dbm_sim* s, int32_t inst, const double* center, double radius) {
+  SIM_CHECK(s);
+  return s->impl->set_obstacle(inst, center, radius);
+}
+int dbm_sim_set_inflow(dbm_sim* s, int32_t inst, const double* u, int32_t width) {
+  SIM_CHECK(s);
+  return s->impl->set_inflow(inst, u, width);
 }
 int dbm_sim_snapshot(dbm_sim* s, void* dst, int64_t bytes, int64_t* needed, void* stream) {
   SIM_CHECK(s);

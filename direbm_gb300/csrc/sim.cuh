@@ -23,6 +23,11 @@ struct InstK {
   int32_t periodic;
   double tau;
   double rho_rest;
+  int32_t has_obs;   // a solid sphere (disc in 2D) with bounce-back
+  int32_t inflow_w;  // inflow layer: moments in local cell columns x < inflow_w are set to feq(rho, u_in)
+  double obs_c[3];   // sphere center, instance-local cell units
+  double obs_r2;     // squared radius, cell units
+  double u_in[3];
 };
 
 struct PF64 {
@@ -79,6 +84,8 @@ struct Args {
   float* cpfhi;    // FP32DEV: [Q][ccap]
   float* cpflo;    // FP32DEV: [Q][ccap]
   uint32_t* emask; // [ccap]
+  uint32_t* bmask; // [mcap] blocked (bounced) directions of each input moment, bit k (obstacles only)
+  int any_obstacle;
   uint32_t* status;
   uint32_t* d_P;
   int write_trace;
@@ -165,6 +172,21 @@ __device__ __forceinline__ T cell_d2_lower(const T (&c)[3]) {
 template <class P>
 __device__ __forceinline__ typename P::real floor_r(typename P::real x) { return floor(x); }
 
+// Whether the point (local integer cell S) + o (cell units, FP64) lies inside the instance's
+// sphere: end_a = ((double)S_a - ctr_a) + o_a, inside <=> sum end_a^2 < r^2, each operation rounded
+// in FP64 in this order (the oracle's order, oracle/grid_step.py: inside_obstacle).
+template <int D>
+__device__ __forceinline__ bool inside_sphere(const InstK& I, const int (&S)[3], const double (&o)[3]) {
+  double d2 = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double e = __dadd_rn(__dsub_rn((double)S[a], I.obs_c[a]), o[a]);
+    const double e2 = __dmul_rn(e, e);
+    d2 = a == 0 ? e2 : __dadd_rn(d2, e2);
+  }
+  return d2 < I.obs_r2;
+}
+
 // Called around one step by SimBase::step_hooked.  `before` sees the input state (args->a, not
 // yet collided); `after` sees every buffer of the step (a = the collided input moments, b = the
 // output moments, the per-cell thinning/refine scratch, the sorted pairs, 1/sw, the gathered f
@@ -189,6 +211,8 @@ struct SimBase {
   virtual int conservation(double*, cudaStream_t) = 0;
   virtual int trace(int, void*, int64_t, int64_t*, cudaStream_t) = 0;
   virtual int set_tau(const double*, int) = 0;
+  virtual int set_obstacle(int, const double*, double) = 0;
+  virtual int set_inflow(int, const double*, int) = 0;
   virtual int snapshot(void*, int64_t, int64_t*, cudaStream_t) = 0;
   virtual int restore(const void*, int64_t, cudaStream_t) = 0;
   virtual int64_t device_bytes() const = 0;

@@ -32,6 +32,8 @@ class Instance:
     periodic: bool = True
     tau: float = 0.6
     rho_rest: float = 1.0
+    obstacle: tuple | None = None  # (center (D,) world, radius world): solid sphere/disc, bounce-back
+    inflow: tuple | None = None  # (u (D,), width in cells): inflow layer at the low-x face
 
 
 _PREC = {"fp64": _lib.FP64, "fp32dev": _lib.FP32DEV, "fp32": _lib.FP32DEV}
@@ -105,6 +107,11 @@ class Simulation:
         _lib.check(self.lib.dbm_sim_set_option(self._h, 1, 1 if graphs else 0), "dbm_sim_set_option")
         _lib.check(self.lib.dbm_sim_set_option(self._h, 2, 1 if tiles else 0), "dbm_sim_set_option")
         self.iteration = 0
+        for i, inst in enumerate(self.instances):
+            if inst.obstacle is not None:
+                self.set_obstacle(i, *inst.obstacle)
+            if inst.inflow is not None:
+                self.set_inflow(i, *inst.inflow)
 
     # ---- lifecycle ------------------------------------------------------------------------------
     def close(self):
@@ -219,6 +226,28 @@ class Simulation:
             _lib.check(self.lib.dbm_sim_trace(self._h, what, buf.data_ptr(), buf.numel(), ctypes.byref(need), _stream()),
                        "dbm_sim_trace")
         return buf
+
+    # ---- obstacles and inflow --------------------------------------------------------------------
+    def set_obstacle(self, inst: int, center, radius: float):
+        """Solid sphere (disc in 2D) with bounce-back in instance `inst` (world units); radius <= 0
+        removes it."""
+        c = np.ascontiguousarray(np.asarray(center, dtype=np.float64).reshape(-1))
+        if c.shape[0] != self.lattice.D:
+            raise ValueError(f"center needs {self.lattice.D} coordinates")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_set_obstacle(self._h, int(inst), c.ctypes.data, float(radius)),
+                       "dbm_sim_set_obstacle")
+        self.instances[inst].obstacle = (tuple(c), float(radius)) if radius > 0 else None
+
+    def set_inflow(self, inst: int, u, width: int):
+        """Inflow layer: moments in the first `width` cell columns of instance `inst` are set to the
+        equilibrium at velocity u with their own density; width 0 removes it."""
+        v = np.ascontiguousarray(np.asarray(u, dtype=np.float64).reshape(-1))
+        if v.shape[0] != self.lattice.D:
+            raise ValueError(f"u needs {self.lattice.D} components")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_set_inflow(self._h, int(inst), v.ctypes.data, int(width)), "dbm_sim_set_inflow")
+        self.instances[inst].inflow = (tuple(v), int(width)) if width > 0 else None
 
     # ---- launch configuration -------------------------------------------------------------------
     OPT_TILE_WIDTH, OPT_PERSISTENT = 3, 4

@@ -188,6 +188,16 @@ int64_t dbm_sim_device_bytes(dbm_sim* sim);
  * reference fixes tau at construction (warp/simulator.py:25-44); a new tau is what a gradient
  * step on tau needs. */
 int dbm_sim_set_tau(dbm_sim* sim, const double* h_tau, int32_t n);
+/* Obstacles and inflow (config 3; the reference's obstacles are CPU-only, reference/boundary.py and
+ * reference/simulator.py:105-117, with a specular bounce and a direction split).  A solid sphere
+ * (disc in 2D) of `radius` (world units) at `center` (D world coordinates) in instance `inst`;
+ * radius <= 0 removes it.  A component whose dispersion end point lies inside it bounces back: it
+ * stays at its moment's position and carries the opposite direction.  Points that end a step
+ * inside the solid are removed, as in the reference.  The inflow layer sets moments of the first
+ * `width` cell columns to the equilibrium at velocity u (their own density).  Both take effect at
+ * the next step; with an obstacle the 2D window kernels run untiled.  Synchronise. */
+int dbm_sim_set_obstacle(dbm_sim* sim, int32_t inst, const double* h_center, double radius);
+int dbm_sim_set_inflow(dbm_sim* sim, int32_t inst, const double* h_u, int32_t width);
 /* Checkpoint / resume (the reference has none): copy the current state into a device blob of
  * *needed bytes (call with d_dst = NULL to size it; synchronises), and make such a blob the
  * current state again, bit for bit. */

@@ -50,7 +50,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from .lattices import Lattice
-from .physics import collide_unguarded
+from .physics import collide_unguarded, equilibrium
 
 
 @dataclass
@@ -60,6 +60,9 @@ class Instance:
     periodic: bool = True
     tau: float = 0.6
     rho_rest: float = 1.0
+    obstacle: tuple = None  # (center (D,) world units, radius world units): a solid sphere / disc
+    inflow: tuple = None  # (u (D,), width in cells): moments in the first `width` cell columns
+    #                       are reset to the equilibrium at velocity u (their own density)
 
 
 @dataclass
@@ -202,21 +205,87 @@ def _offsets(D, lo, hi):
     return np.stack([gr.ravel() for gr in grids], axis=1)
 
 
+def opposite(lattice):
+    """Index of -c_k for every direction k."""
+    C = lattice.C
+    return np.array([int(np.flatnonzero(np.all(np.abs(C + C[k]) < 1e-12, axis=1))[0]) for k in range(len(C))])
+
+
+def _obstacle_local(spec: GridSpec, b):
+    """Sphere center in instance-local cell units and squared radius in cell units (FP64)."""
+    inst = spec.instances[b]
+    ctr = np.asarray(inst.obstacle[0], dtype=np.float64) / np.float64(spec.cell) - np.asarray(inst.origin, np.float64)
+    r = np.float64(inst.obstacle[1]) / np.float64(spec.cell)
+    return ctr, r * r
+
+
+def inside_obstacle(spec: GridSpec, b, coords, off, shift=None):
+    """Whether points (instance b, local integer cell coords, offsets [+ FP64 shift]) lie inside
+    their instance's obstacle: end_a = ((double)S_a - ctr_a) + ((double)off_a [+ shift_a]),
+    inside <=> sum_a end_a^2 < r^2, every operation in FP64 in this order (the kernels' order)."""
+    b = np.asarray(b)
+    out = np.zeros(len(b), dtype=bool)
+    for bi in np.unique(b):
+        if spec.instances[bi].obstacle is None:
+            continue
+        sel = b == bi
+        ctr, r2 = _obstacle_local(spec, bi)
+        o = np.asarray(off, dtype=np.float64)[sel]
+        if shift is not None:
+            o = o + np.asarray(shift, dtype=np.float64)[sel]
+        rel = np.asarray(coords, dtype=np.float64)[sel] - ctr[None, :]
+        end = rel + o
+        d2 = end[:, 0] * end[:, 0]
+        for a in range(1, spec.D):
+            d2 = d2 + end[:, a] * end[:, a]
+        out[sel] = d2 < r2
+    return out
+
+
+def blocked(spec: GridSpec, st: GridState):
+    """(M, Q) bool: slot k of moment m is blocked when its dispersion end point (moment position +
+    c_k dx) lies inside the instance's obstacle (bounce-back; the rest direction never is)."""
+    M, Q = len(st.cell), spec.Q
+    out = np.zeros((M, Q), dtype=bool)
+    if all(inst.obstacle is None for inst in spec.instances) or M == 0:
+        return out
+    b, S = decode(spec, st.cell)
+    cd64 = spec.lattice.C * np.float64(spec.dx) / np.float64(spec.cell)
+    for k in range(1, Q):
+        out[:, k] = inside_obstacle(spec, b, S, st.off.astype(np.float64), np.broadcast_to(cd64[k], (M, spec.D)))
+    return out
+
+
 def components(spec: GridSpec, st: GridState):
-    """All (m, k) components: moment index, direction, source coords, t = off + cd (working dtype)."""
+    """All (m, k) components (slots): moment index, slot direction, instance, source coords and
+    t = off + displacement (working dtype), plus the label (the direction the component carries)
+    and whether the slot is blocked.  An unblocked slot k sits at off + cd_k with label k; a blocked
+    slot bounces back: it stays at off (displacement 0) with the opposite label, carrying f*_k."""
     M, Q = len(st.cell), spec.Q
     b, S = decode(spec, st.cell)
     m = np.repeat(np.arange(M), Q)
     k = np.tile(np.arange(Q), M)
-    t = (st.off[m].astype(spec.dtype) + spec.cd[k]).astype(spec.dtype)
-    return m, k, b[m], S[m], t
+    blk = blocked(spec, st).reshape(-1)
+    cdv = np.where(blk[:, None], spec.dtype(0), spec.cd[k]).astype(spec.dtype)
+    t = (st.off[m].astype(spec.dtype) + cdv).astype(spec.dtype)
+    lab = np.where(blk, opposite(spec.lattice)[k], k)
+    return m, k, b[m], S[m], t, lab, blk, cdv
 
 
 # ---- the stages --------------------------------------------------------------------------------
 
 def collide_state(spec: GridSpec, st: GridState):
-    b, _ = decode(spec, st.cell)
-    return collide_unguarded(st.f, spec.tau_arr()[b], spec.lattice)
+    b, S = decode(spec, st.cell)
+    fs = collide_unguarded(st.f, spec.tau_arr()[b], spec.lattice)
+    for bi, inst in enumerate(spec.instances):
+        if inst.inflow is None:
+            continue
+        sel = (b == bi) & (S[:, 0] < int(inst.inflow[1]))
+        if sel.any():
+            rho = st.f[sel].sum(1)
+            u = np.broadcast_to(np.asarray(inst.inflow[0], dtype=np.float64), (int(sel.sum()), spec.D))
+            fs[sel] = equilibrium(rho, u, spec.lattice)
+    return fs
 
 
 def ordered_sums(group, order_keys, vals, ngroups):
@@ -253,7 +322,7 @@ def thin(spec: GridSpec, st: GridState):
     """Stage 2.  Returns (occupied global cells sorted, count per CP, centroid rel (P,D),
     component landing cell per (m,k) (or -1 outside a non-periodic box)).  The centroid sum runs
     in the kernel's order: direction, then source-cell offset, then moment."""
-    m, k, b, S, t = components(spec, st)
+    m, k, b, S, t, lab, blk, _ = components(spec, st)
     fl = np.floor(t).astype(np.int64)
     C = encode(spec, b, S + fl)
     rel = ((-fl).astype(spec.dtype) + t).astype(spec.dtype)
@@ -261,7 +330,11 @@ def thin(spec: GridSpec, st: GridState):
     cells, inv = np.unique(C[ok], return_inverse=True)
     cnt = np.bincount(inv, minlength=len(cells))
     so = -fl[ok]
-    sums = ordered_sums(inv, [k[ok]] + _so_keys(so, spec.D) + [m[ok]], rel[ok].astype(np.float64), len(cells))
+    bo = blk[ok]
+    # kernel order: regular components by (direction, source offset, moment), then the bounced ones
+    # (which land in their own cell) by (moment, direction)
+    keys = [bo.astype(np.int64), np.where(bo, 0, k[ok])] + _so_keys(so, spec.D) + [m[ok], np.where(bo, k[ok], 0)]
+    sums = ordered_sums(inv, keys, rel[ok].astype(np.float64), len(cells))
     cen = (sums / cnt[:, None]).astype(spec.dtype)
     return cells, cnt, cen, C
 
@@ -272,7 +345,7 @@ def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
     the CP (canonical order, see disp) and the integer cell difference dS = S - G."""
     if comps is None:
         comps = components(spec, st)
-    m, k, b, S, t = comps
+    m, k, b, S, t, lab, blk, cdv = comps
     fl = np.floor(t).astype(np.int64)
     order = np.argsort(cp_cell, kind="stable")
     cs = cp_cell[order]
@@ -289,7 +362,7 @@ def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
         within = np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt)
         pj = order[np.repeat(lo, cnt) + within]
         dS = -(fl[ci] + o)
-        e = disp(spec, dS, spec.cd[k[ci]], cp_off[pj], st.off[m[ci]])
+        e = disp(spec, dS, cdv[ci], cp_off[pj], st.off[m[ci]])
         d = norm(spec, e)
         keep = d <= spec.R
         ci_all.append(ci[keep])
@@ -307,15 +380,17 @@ def _pairs_comp_cp(spec, st, cp_cell, cp_off, comps=None):
 def refine(spec: GridSpec, st: GridState, fstar, cells, cen):
     """Stage 3.  Returns (mask, kappa, final global cell, final offset) per CP (thinning order)."""
     comps = components(spec, st)
-    m, k, b, S, t = comps
+    m, k, b, S, t, lab, blk, _ = comps
     ci, pj, d, e, dS = _pairs_comp_cp(spec, st, cells, cen, comps)
     P = len(cells)
     mask = np.zeros(P, dtype=np.int64)
-    np.bitwise_or.at(mask, pj, np.left_shift(1, k[ci]))
+    np.bitwise_or.at(mask, pj, np.left_shift(1, lab[ci]))
     kappa = np.array([bin(int(x)).count("1") for x in mask], dtype=np.int64)
     w = np.exp(fstar[m[ci], k[ci]])
-    # sums in the kernel's order: direction, window offset (z, y, x), moment
-    keys = [k[ci]] + _so_keys(dS, spec.D) + [m[ci]]
+    # sums in the kernel's order: regular components by direction, window offset (z, y, x),
+    # moment; then bounced ones by window offset, moment, direction
+    bc = blk[ci]
+    keys = [bc.astype(np.int64), np.where(bc, 0, k[ci])] + _so_keys(dS, spec.D) + [m[ci], np.where(bc, k[ci], 0)]
     sw = ordered_sums(pj, keys, w, P)
     sx = ordered_sums(pj, keys, w[:, None] * e.astype(np.float64), P)
     move = kappa > spec.kappa_hard
@@ -352,14 +427,15 @@ def weights(spec: GridSpec, st: GridState, cp_cell, cp_off, comps=None):
 def gather(spec: GridSpec, st: GridState, fstar, cp_cell, cp_off):
     """Stages 5+6.  Returns cp_f (P,Q) before gap fill and sw per component."""
     comps = components(spec, st)
-    m, k = comps[0], comps[1]
+    m, k, lab = comps[0], comps[1], comps[5]
     sw, ci, pj, wv = weights(spec, st, cp_cell, cp_off, comps)
     live = sw[ci] > 0.0
     P = len(cp_cell)
     cp_f = np.zeros((P, spec.Q))
     inv = np.zeros_like(sw)
     np.divide(1.0, sw, out=inv, where=sw > 0.0)
-    np.add.at(cp_f, (pj[live], k[ci[live]]), (wv[live] * inv[ci[live]]) * fstar[m[ci[live]], k[ci[live]]])
+    # a component lands in the control point's f at its label (the opposite direction if it bounced)
+    np.add.at(cp_f, (pj[live], lab[ci[live]]), (wv[live] * inv[ci[live]]) * fstar[m[ci[live]], k[ci[live]]])
     return cp_f, sw.reshape(-1, spec.Q)
 
 
@@ -407,6 +483,9 @@ def step(spec: GridSpec, st: GridState, trace: dict | None = None) -> GridState:
     cells, cnt, cen, comp_cell = thin(spec, st)
     mask, kappa, G, off = refine(spec, st, fstar, cells, cen)
     keep = G >= 0
+    if keep.any() and any(inst.obstacle is not None for inst in spec.instances):
+        bq, Fq = decode(spec, np.where(keep, G, 0))
+        keep &= ~inside_obstacle(spec, bq, Fq, off.astype(np.float64))  # solid: the point is removed
     order = sort_cps(np.where(keep, G, np.iinfo(np.int64).max))
     order = order[keep[order]]
     cp_cell = G[order]

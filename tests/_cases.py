@@ -48,7 +48,8 @@ def rest_pulse(half, lattice="D2Q7", pulse=1.5):
 def oracle_spec(lattice, instances, dx, r_res, cell, kappa_hard=4, dtype=np.float64):
     insts = [grid_step.Instance(dims=tuple(i["dims"]), origin=tuple(i.get("origin", (0,) * len(i["dims"]))),
                                 periodic=i.get("periodic", True), tau=i.get("tau", 0.6),
-                                rho_rest=i.get("rho_rest", 1.0)) for i in instances]
+                                rho_rest=i.get("rho_rest", 1.0), obstacle=i.get("obstacle"),
+                                inflow=i.get("inflow")) for i in instances]
     return grid_step.GridSpec(lattice=BY_NAME[lattice], dx=dx, r_res=r_res, cell=cell, kappa_hard=kappa_hard,
                               instances=insts, dtype=dtype)
 
@@ -57,3 +58,15 @@ def bounded_box(pos, cell, margin):
     lo = np.floor((pos.min(0) - margin) / cell).astype(int)
     hi = np.ceil((pos.max(0) + margin) / cell).astype(int)
     return tuple(int(v) for v in hi - lo), tuple(int(v) for v in lo)
+
+
+def around_obstacle(n, D, center, radius, seed=0, u0=0.04, lattice="D2Q9", jitter=0.25):
+    """Jittered points on an n^D periodic box outside a sphere, uniform flow u0 along x."""
+    lat = BY_NAME[lattice]
+    x = np.mod(jittered_grid(n, D, seed, jitter), n)
+    keep = ((x - np.asarray(center)) ** 2).sum(1) >= (radius + 0.5) ** 2
+    x = x[keep]
+    u = np.zeros_like(x)
+    u[:, 0] = u0
+    f = equilibrium(np.ones(len(x)), u, lat)
+    return x, f
