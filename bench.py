@@ -16,6 +16,7 @@ Keys beyond the base contract:
   lbm           hexagonal D2Q7 shear wave 1024x1024 (FP32DEV and FP64), node-steps/s
   adjoint       inverse problem on 64k points, 100 steps, checkpoint every 10: adjoint steps/s, its
                 cost relative to the forward step, FP32DEV gradient error vs FP64
+  sphere        3D flow past a bounce-back sphere (D3Q19, ~2 M points, inflow), FP32DEV and FP64
   cpu_baseline  the CPU oracle (numpy restatement of the reference step) on the host cores
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -400,6 +401,81 @@ def adjoint_leg(n=256, steps=100, every=10, tau=0.6, precisions=("fp32dev", "fp6
     return out
 
 
+def sphere_leg(steps=20, steps64=4):
+    """Flow past a sphere (the 3D obstacle configuration): D3Q19, periodic box of 160 x 112 x 112
+    cells (h = dx = 1) with one jittered point per cell outside a bounce-back sphere of radius 16h
+    at (40, 56, 56) (~2.0 M points), uniform initial and inflow velocity 0.04 along x (inflow layer
+    of 2 cell columns), tau 0.56, r 1.5h.  Uniform point density: cell thinning at cell h keeps at
+    most one point per cell, so a 4x denser seeding near the sphere would be thinned back to this
+    density in the first step.  FP32DEV and FP64 point-steps/s and their velocity difference."""
+    import torch
+
+    from direbm_gb300.lattices import D3Q19, equilibrium
+    from direbm_gb300.sim import Instance, Simulation
+
+    dims = (160, 112, 112)
+    center, radius, u0 = (40.0, 56.0, 56.0), 16.0, 0.04
+    rng = np.random.default_rng(3)
+    x = (np.indices(dims).reshape(3, -1).T + 0.5).astype(np.float64)
+    x += rng.uniform(-0.25, 0.25, size=x.shape)
+    x = np.mod(x, np.asarray(dims, dtype=np.float64))
+    x = x[((x - np.asarray(center)) ** 2).sum(1) >= (radius + 0.5) ** 2]
+    u = np.zeros_like(x)
+    u[:, 0] = u0
+    f = equilibrium(np.ones(len(x)), u, D3Q19)
+    out = {"config": "D3Q19 sphere r=16h in 160x112x112 periodic box, inflow 0.04 (2 columns), tau 0.56, "
+                     "uniform 1 point/cell outside the sphere", "points": int(len(x))}
+    states = {}
+    for prec, n in (("fp32dev", steps), ("fp64", steps64)):
+        inst = Instance(dims=dims, periodic=True, tau=0.56, obstacle=(center, radius), inflow=((u0, 0.0, 0.0), 2))
+        sim = Simulation([inst], lattice="D3Q19", precision=prec, dx=DX, r_res=R_RES, cell=CELL,
+                         moment_capacity=int(1.2 * len(x)))
+        sim.set_state(None, x, f)
+        m0 = float(sim.conservation()[0, 0])
+        sim.step(1)  # warm-up (graph capture)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sim.step(n)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        sim.check_status()
+        pts = sim.count()
+        out[prec] = {"point_steps_per_s": pts * n / (ms * 1e-3), "ms_per_step": ms / n, "steps": n,
+                     "mass_drift": float(sim.conservation()[0, 0]) / m0 - 1.0}
+        sim.close()
+        # the same 1 + steps64 steps again for the FP32DEV vs FP64 comparison
+        sim = Simulation([inst], lattice="D3Q19", precision=prec, dx=DX, r_res=R_RES, cell=CELL,
+                         moment_capacity=int(1.2 * len(x)))
+        sim.set_state(None, x, f)
+        sim.step(1 + steps64)
+        states[prec] = sim.state_numpy()
+        sim.close()
+    # FP32 and FP64 take a few near-tie decisions differently on 2 M points, so the point sets can
+    # differ slightly: compare velocities cell by cell where each run has exactly one point
+    (_, xa, fa), (_, xb, fb) = states["fp32dev"], states["fp64"]
+
+    def by_cell(xp):
+        c = np.floor(xp).astype(np.int64)
+        key = (c[:, 2] * dims[1] + c[:, 1]) * dims[0] + c[:, 0]
+        uk, idx, cnt = np.unique(key, return_index=True, return_counts=True)
+        return dict(zip(uk[cnt == 1].tolist(), idx[cnt == 1].tolist()))
+
+    ca, cb = by_cell(xa), by_cell(xb)
+    common = sorted(set(ca) & set(cb))
+    ia = np.array([ca[k] for k in common], dtype=np.int64)
+    ib = np.array([cb[k] for k in common], dtype=np.int64)
+    ua, ub = velocity_l2(fa[ia], D3Q19), velocity_l2(fb[ib], D3Q19)
+    out["fp32dev_vs_fp64_after_steps"] = 1 + steps64
+    out["fp32dev_velocity_l2_rel_vs_fp64"] = float(np.sqrt(((ua - ub) ** 2).sum() / (ub ** 2).sum()))
+    out["fp32dev_vs_fp64_points"] = [int(len(xa)), int(len(xb))]
+    out["matched_cells_frac"] = len(common) / max(len(xb), 1)
+    out["max_pos_err_matched"] = float(np.abs(xa[ia] - xb[ib]).max())
+    out["speedup_fp32dev_vs_fp64"] = out["fp32dev"]["point_steps_per_s"] / out["fp64"]["point_steps_per_s"]
+    return out
+
+
 # ---- CPU oracle legs -----------------------------------------------------------------------------
 
 def _oracle_instance_steps(args):
@@ -555,6 +631,7 @@ def run_ours(args):
     acc = accuracy_leg()
     lbm = lbm_leg()
     adj = adjoint_leg()
+    sph = sphere_leg()
     cpu = cpu_baseline_leg()
     line = {
         "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
@@ -569,7 +646,7 @@ def run_ours(args):
         "roofline": roof, "stage_ms": stage_ms, "step_roofline": step_roof,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
         "fp64": fp64, "speedup_fp32dev_vs_fp64": value / world / fp64["value"], "accuracy": acc, "lbm": lbm,
-        "adjoint": adj,
+        "adjoint": adj, "sphere": sph,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -584,8 +661,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=N_INST, help="first N ensemble members (profiling runs)")
-    ap.add_argument("--legs", default="all", choices=["all", "main", "adjoint"],
-                    help="main = timed step only; adjoint = the inverse-problem leg only")
+    ap.add_argument("--legs", default="all", choices=["all", "main", "adjoint", "sphere"],
+                    help="main = timed step only; adjoint / sphere = that leg only")
     ap.add_argument("--adjoint-n", type=int, default=256, help="adjoint leg: points per side")
     ap.add_argument("--adjoint-steps", type=int, default=100, help="adjoint leg: rollout steps")
     ap.add_argument("--adjoint-every", type=int, default=10, help="adjoint leg: checkpoint interval")
@@ -593,6 +670,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.legs == "sphere" and args.impl == "ours":
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"sphere": sphere_leg()}), flush=True)
+        return
     if args.legs == "adjoint" and args.impl == "ours":
         import torch
 
