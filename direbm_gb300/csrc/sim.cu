@@ -73,7 +73,13 @@ __global__ void __launch_bounds__(256) k_collide(const __grid_constant__ Args<Q,
       for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + m] = dv[k];
     }
     uint32_t bm = 0;
-    if (I.has_obs) {  // bounce-back: a direction whose end point lies inside the solid is blocked
+    real om[3] = {0, 0, 0};
+    if (I.has_obs) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) om[a] = A.a.off[(int64_t)a * A.mcap + m];
+    }
+    if (I.has_obs && sphere_dist2<D, real>(I, c, om) < I.near2) {
+      // bounce-back: a direction whose end point lies inside the solid is blocked
 #pragma unroll 1
       for (int k = 1; k < Q; ++k) {
         double o[3] = {0, 0, 0};
@@ -239,7 +245,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
           }
         }
   }
-  if (A.any_obstacle) {
+  if (A.any_obstacle && I.has_obs && sphere_dist2<D, real>(I, Fc, cen) < I.reach2) {
     // bounced components (displacement 0, opposite label): window order, then moment, then slot
     int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
@@ -489,7 +495,7 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
           }
         }
       }
-  if (A.any_obstacle && k > 0) {
+  if (A.any_obstacle && k > 0 && I.has_obs && sphere_dist2<D, real>(I, Gc, p) < I.reach2) {
     // components of slot kb = opp[k] that bounced carry label k and sit at their moment's offset
     const int kb = A.L.opp[k];
     int blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0};
@@ -1362,6 +1368,12 @@ struct SimImpl : SimBase {
       }
       I.obs_r2 = r * r;
       I.has_obs = 1;
+      // margins (cell units, generous against FP32 rounding): a blocked direction ends inside the
+      // sphere, so its moment lies within r + |cd| of the center; a bounced component within the
+      // resampling radius of a point puts that point within r + |cd| + R
+      const double near = r + cmax + 1.0, reach = r + cmax + desc.r_res / desc.cell + 2.0;
+      I.near2 = (float)(near * near);
+      I.reach2 = (float)(reach * reach);
     } else {
       I.has_obs = 0;
     }

@@ -28,6 +28,8 @@ struct InstK {
   double obs_c[3];   // sphere center, instance-local cell units
   double obs_r2;     // squared radius, cell units
   double u_in[3];
+  float near2;       // squared distance from the center beyond which no direction of a moment can be blocked
+  float reach2;      // squared distance beyond which no bounced component lies within r of a point
 };
 
 struct PF64 {
@@ -171,6 +173,19 @@ __device__ __forceinline__ T cell_d2_lower(const T (&c)[3]) {
 
 template <class P>
 __device__ __forceinline__ typename P::real floor_r(typename P::real x) { return floor(x); }
+
+// Squared distance (FP32, approximate) from the instance's sphere center to local cell S + o; used
+// only against margins that are wider than its error, to skip exact tests far from the solid.
+template <int D, class T>
+__device__ __forceinline__ float sphere_dist2(const InstK& I, const int (&S)[3], const T (&o)[3]) {
+  float d2 = 0.f;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const float e = (float)S[a] - (float)I.obs_c[a] + (float)o[a];
+    d2 += e * e;
+  }
+  return d2;
+}
 
 // Whether the point (local integer cell S) + o (cell units, FP64) lies inside the instance's
 // sphere: end_a = ((double)S_a - ctr_a) + o_a, inside <=> sum end_a^2 < r^2, each operation rounded

@@ -649,10 +649,12 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
     const int n = tile_items<real>(I, T, G, G.cp, A.a.start, A.a.cell, A.a.off, A.mcap, c0, cap_t, s_tr, s_ij, s_bx,
                                    s_by, s_mpos);
     const int nc = min(cap_t, n - c0);
-#pragma unroll 1
-    for (int k = 0; k < Q; ++k) {
+    // one work unit per (item, direction), direction-major: finer than one item's nine directions,
+    // so the threads of a block finish together; each unit's sum is still one thread's loop
+    for (int wu = threadIdx.x; wu < nc * Q; wu += blockDim.x) {
+      const int k = wu / nc, i = wu - k * nc;
       const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
-      for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+      {
         const int bx = s_bx[i], by = s_by[i];
         const real bxf = (real)bx;
         const Pair<real> o = s_mpos[i];
