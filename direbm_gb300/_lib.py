@@ -121,6 +121,9 @@ _SIGS = {
     "dbm_tape_length": (_i32, [_vp]),
     "dbm_tape_counts": (ctypes.c_int, [_vp, _i32, _vp]),
     "dbm_tape_backward": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "dbm_tape_record": (ctypes.c_int, [_vp, _i32, _vp]),
+    "dbm_tape_set_estimate": (ctypes.c_int, [_vp, _f64]),
+    "dbm_tape_backward_all": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "dbm_tape_export": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp]),
 }
 

@@ -25,6 +25,18 @@ from . import _lib
 from .sim import Simulation, _stream
 
 
+class TapeOverflow(_lib.DbmError):
+    """A neighbour list outgrew the tape's estimate: restore the state of the first recorded step,
+    clear the tape and record again (the estimate has grown, so the next recording fits)."""
+
+
+def _check_tape(rc: int, what: str):
+    if rc == 3:  # DBM_ERR_CAPACITY
+        msg = _lib.load().dbm_last_error().decode()
+        raise TapeOverflow(f"{what}: {msg}")
+    _lib.check(rc, what)
+
+
 class Tape:
     """Recorded steps of one ``Simulation`` (``dbm_tape``)."""
 
@@ -55,21 +67,57 @@ class Tape:
     def step(self):
         """Advance the simulator one step and record it."""
         with torch.cuda.device(self.sim.device):
-            _lib.check(self.lib.dbm_tape_step(self._h, _stream()), "dbm_tape_step")
+            _check_tape(self.lib.dbm_tape_step(self._h, _stream()), "dbm_tape_step")
         self.sim.iteration += 1
-        self._counts.append(self._query_counts(len(self._counts)))
+        self._counts.append(None)
+
+    def set_estimate(self, pairs_per_row: float):
+        """Initial list-size estimate (pairs per row; grown as steps are recorded)."""
+        _lib.check(self.lib.dbm_tape_set_estimate(self._h, float(pairs_per_row)), "dbm_tape_set_estimate")
+
+    def record(self, n: int):
+        """Advance the simulator n steps, recording each."""
+        with torch.cuda.device(self.sim.device):
+            _check_tape(self.lib.dbm_tape_record(self._h, int(n), _stream()), "dbm_tape_record")
+        self.sim.iteration += int(n)
+        self._counts.extend([None] * int(n))  # read on first use (reading settles the tape)
+
+    def backward_all(self, g_off_out: torch.Tensor, g_f_out: torch.Tensor, g_tau: torch.Tensor):
+        """Every recorded step in reverse: cotangents of the last step's output -> those of the first
+        step's input; d loss / d tau added into g_tau."""
+        n = len(self._counts)
+        if n == 0:
+            raise ValueError("nothing recorded")
+        sim = self.sim
+        D, Q, dev = sim.lattice.D, sim.lattice.Q, sim.device
+        last, first = self.counts(n - 1), self.counts(0)
+        g_off_out = g_off_out.to(device=dev, dtype=torch.float64).contiguous()
+        g_f_out = g_f_out.to(device=dev, dtype=torch.float64).contiguous()
+        if g_off_out.shape != (last["P"], D) or g_f_out.shape != (last["P"], Q):
+            raise ValueError(f"expected cotangents ({last['P']}, {D}) and ({last['P']}, {Q})")
+        if g_tau.dtype != torch.float64 or not g_tau.is_contiguous() or g_tau.device != dev:
+            raise ValueError("g_tau must be a contiguous FP64 tensor on the simulator's device")
+        g_off_in = torch.empty((first["M"], D), dtype=torch.float64, device=dev)
+        g_f_in = torch.empty((first["M"], Q), dtype=torch.float64, device=dev)
+        with torch.cuda.device(dev):
+            _check_tape(self.lib.dbm_tape_backward_all(self._h, g_off_out.data_ptr(), g_f_out.data_ptr(),
+                                                       g_off_in.data_ptr(), g_f_in.data_ptr(), g_tau.data_ptr(),
+                                                       _stream()), "dbm_tape_backward_all")
+        return g_off_in, g_f_in
 
     def __len__(self) -> int:
         return int(self.lib.dbm_tape_length(self._h))
 
     def _query_counts(self, i: int) -> dict:
         c = (ctypes.c_int64 * 8)()
-        _lib.check(self.lib.dbm_tape_counts(self._h, int(i), c), "dbm_tape_counts")
+        _check_tape(self.lib.dbm_tape_counts(self._h, int(i), c), "dbm_tape_counts")
         return {"M": c[0], "P": c[1], "refine": c[2], "resample": c[3], "gapfill": c[4]}
 
     def counts(self, i: int) -> dict:
         """Moments in (M), control points out (P) and the pair counts of recorded step i."""
         if 0 <= i < len(self._counts):
+            if self._counts[i] is None:
+                self._counts[i] = self._query_counts(i)
             return self._counts[i]
         return self._query_counts(i)
 
@@ -161,12 +209,16 @@ class _Rollout(torch.autograd.Function):
         for seg in reversed(range(nseg)):
             s0 = seg * ctx.every
             s1 = min(s0 + ctx.every, ctx.steps)
-            sim.restore(ctx.snaps[seg], s0)
-            tape.clear()
-            for _ in range(s0, s1):
-                tape.step()
-            for i in reversed(range(s1 - s0)):
-                g_off, g_f = tape.backward(i, g_off, g_f, g_tau)
+            for attempt in range(3):
+                sim.restore(ctx.snaps[seg], s0)
+                tape.clear()
+                try:
+                    tape.record(s1 - s0)
+                    g_off, g_f = tape.backward_all(g_off, g_f, g_tau)
+                    break
+                except TapeOverflow:
+                    if attempt == 2:
+                        raise
         tape.clear()
         sim.restore(ctx.final, ctx.steps)
         g_pos_in = torch.empty_like(g_off)

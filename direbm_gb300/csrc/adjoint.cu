@@ -914,10 +914,12 @@ __global__ void k_dev_to_f64(const float* __restrict__ rho, const float* __restr
 
 struct TapeBase {
   virtual ~TapeBase() = default;
+  virtual void set_estimate(double) = 0;
   virtual int clear() = 0;
   virtual int step(cudaStream_t) = 0;
+  virtual int backward_all(const double*, const double*, double*, double*, double*, cudaStream_t) = 0;
   virtual int length() const = 0;
-  virtual int counts(int, int64_t*) const = 0;
+  virtual int counts(int, int64_t*) = 0;
   virtual int backward(int, const double*, const double*, double*, double*, double*, cudaStream_t) = 0;
   virtual int export_(int, int, void*, int64_t, int64_t*, cudaStream_t) = 0;
 };
@@ -965,10 +967,13 @@ struct TapeImpl : TapeBase, StepHook {
   uint32_t known_P = 0;                // and its moment count
   cudaEvent_t done = nullptr;
   cudaStream_t side = nullptr;   // second stream for the recording kernels
+  double* io[1] = {nullptr};     // intermediate cotangents of backward_all
+  int64_t io_cap = 0;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   explicit TapeImpl(SimBase* s) : sim(s) {}
   ~TapeImpl() override {
+    if (io[0]) cudaFree(io[0]);
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -990,14 +995,20 @@ struct TapeImpl : TapeBase, StepHook {
 
   int clear() override {
     steps.clear();
+    pending = -1;
+    invalid = false;
     rec_mem.reset();
     wk = nullptr;
     DBM_TRY(rec_mem.get(&wk, Q));
     return DBM_OK;
   }
   int length() const override { return (int)steps.size(); }
-  int counts(int i, int64_t* c) const override {
+  void set_estimate(double per) override {
+    for (auto& v : per_row) v = per;
+  }
+  int counts(int i, int64_t* c) override {
     if (i < 0 || i >= (int)steps.size()) { set_last_error("tape: no step %d", i); return DBM_ERR_INVALID; }
+    DBM_TRY(settle(nullptr));
     const auto& r = steps[i];
     c[0] = r.M; c[1] = r.P; c[2] = r.ref.f.n; c[3] = r.res.f.n; c[4] = r.gap.f.n; c[5] = 0; c[6] = 0; c[7] = 0;
     return DBM_OK;
@@ -1109,10 +1120,23 @@ struct TapeImpl : TapeBase, StepHook {
     const Args<Q, D, P>& A = *(const Args<Q, D, P>*)av;
     StepRec<real, D>& r = cur;
     tmp_mem.reset();
-    {
+    rec_stream = s;
+    if (invalid) return DBM_ERR_CAPACITY;
+    if (pending >= 0) {  // one synchronisation: this step's count and the previous step's counters
+      const uint32_t* src[8] = {A.status, A.d_P, pending_counts, pending_counts + 1, pending_counts + 2,
+                                pending_counts + 3, pending_counts + 4, pending_counts + 5};
+      DBM_TRY(fetch(src, 8, s));
+      const uint32_t st = hbuf[0], pn = hbuf[1];
+      uint32_t need[6];
+      for (int i = 0; i < 6; ++i) need[i] = hbuf[2 + i];
+      DBM_TRY(settle_counts(need));
+      hbuf[0] = st;
+      hbuf[1] = pn;
+    } else {
       const uint32_t* src[2] = {A.status, A.d_P};
       DBM_TRY(fetch(src, 2, s));
     }
+    DBM_TRY(rec_mem.get(&cur_counts, 6));
     if (hbuf[0] & ST_NONFINITE) {
       set_last_error("tape: the step produced a non-finite refine move; it has no derivative");
       return DBM_ERR_INVALID;
@@ -1161,25 +1185,62 @@ struct TapeImpl : TapeBase, StepHook {
     for (int kind : {kRefineComp, kResComp, kGapCP, kGapNb}) DBM_TRY(launch_list(A, r, kind, cp_of_cell, side));
     DBM_CUDA(cudaEventRecord(ev_join, side));
     DBM_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
-    const uint32_t* src[6] = {d_count, d_count + 1, d_count + 2, d_count + 3, d_count + 4, d_count + 5};
-    DBM_TRY(fetch(src, 6, s));
-    uint32_t need[6];
-    for (int kind = 0; kind < 6; ++kind) need[kind] = hbuf[kind];
+    // the slot counters are read at the next synchronisation (see settle): no wait here
+    DBM_CUDA(cudaMemcpyAsync(r_counts_dev(), d_count, 6 * 4, cudaMemcpyDeviceToDevice, s));
+    pending = (int)steps.size();  // this step's index once step() appends it
+    pending_counts = cur_counts;
+    return DBM_OK;
+  }
+
+  // Per-step device copy of the six slot counters (in the tape's arena).
+  uint32_t* cur_counts = nullptr;
+  uint32_t* r_counts_dev() { return cur_counts; }
+  int pending = -1;                 // step whose counters are not read yet
+  cudaStream_t rec_stream = nullptr;  // the simulator's stream the recording kernels ran on
+  uint32_t* pending_counts = nullptr;
+  bool invalid = false;             // a list outgrew its capacity: the tape must be recorded again
+
+  // Read the pending step's counters (the caller synchronises `s` or has just done so through
+  // fetch): set the list sizes, grow the capacity estimates, and mark the tape invalid if a list
+  // did not fit.  Returns DBM_ERR_CAPACITY then.
+  int settle_counts(const uint32_t* need) {
+    StepRec<real, D>& r = steps[pending];
+    const int idx = pending;
+    pending = -1;
+    bool over = false;
     for (int kind = 0; kind < 6; ++kind) {
       PairList<real, D>& Lst = list_of(r, kind);
       Lst.n = need[kind];
-      if (rows[kind] > 0) per_row[kind] = std::max(per_row[kind], (double)need[kind] / (double)rows[kind]);
-      if ((int64_t)need[kind] > Lst.cap) {  // too small: allocate the exact size and run it again
-        DBM_TRY(alloc_list(Lst, rows[kind], (int64_t)need[kind], kind == kGapCP));
-        DBM_TRY(launch_list(A, r, kind, cp_of_cell, s));
-      }
+      if (Lst.rows > 0) per_row[kind] = std::max(per_row[kind], (double)need[kind] / (double)Lst.rows);
+      over |= (int64_t)need[kind] > Lst.cap;
+    }
+    if (over) {
+      invalid = true;
+      set_last_error("tape: a neighbour list of step %d outgrew its estimate; restore the state of the first "
+                     "recorded step, clear the tape and record again (the estimate has grown)", idx);
+      return DBM_ERR_CAPACITY;
     }
     if (need[kRefineCP] != need[kRefineComp] || need[kResCP] != need[kResComp] || need[kGapCP] != need[kGapNb]) {
+      invalid = true;
       set_last_error("tape: the two orientations of a neighbour list disagree (%u/%u, %u/%u, %u/%u)",
                      need[0], need[1], need[2], need[3], need[4], need[5]);
       return DBM_ERR_STATE;
     }
     return DBM_OK;
+  }
+
+  // Settle the pending step now (one synchronisation of the stream the recording ran on); no-op
+  // when nothing is pending.
+  int settle(cudaStream_t) {
+    if (invalid) return DBM_ERR_CAPACITY;
+    if (pending < 0) return DBM_OK;
+    cudaStream_t s = rec_stream;
+    const uint32_t* src[6] = {pending_counts, pending_counts + 1, pending_counts + 2, pending_counts + 3,
+                              pending_counts + 4, pending_counts + 5};
+    DBM_TRY(fetch(src, 6, s));
+    uint32_t need[6];
+    for (int i = 0; i < 6; ++i) need[i] = hbuf[i];
+    return settle_counts(need);
   }
 
   RecK<Q, D, P> reck(const StepRec<real, D>& r) const {
@@ -1196,6 +1257,7 @@ struct TapeImpl : TapeBase, StepHook {
   int backward(int idx, const double* goff_out, const double* gf_out, double* goff_in, double* gf_in, double* gtau,
                cudaStream_t s) override {
     if (idx < 0 || idx >= (int)steps.size()) { set_last_error("tape: no step %d", idx); return DBM_ERR_INVALID; }
+    DBM_TRY(settle(s));
     const StepRec<real, D>& r = steps[idx];
     const int64_t M = r.M, Pn = r.P, QM = (int64_t)Q * M, PQ = Pn * Q;
     if ((Pn > 0 && (!goff_out || !gf_out)) || (M > 0 && (!goff_in || !gf_in)) || !gtau) {
@@ -1255,6 +1317,34 @@ struct TapeImpl : TapeBase, StepHook {
     return DBM_OK;
   }
 
+  // Every recorded step in reverse: the output cotangents of the last step in, the input
+  // cotangents of the first step out, intermediate ones in two device buffers of the tape.
+  int backward_all(const double* goff_out, const double* gf_out, double* goff_in, double* gf_in, double* gtau,
+                   cudaStream_t s) override {
+    const int n = (int)steps.size();
+    if (n == 0) { set_last_error("tape: nothing recorded"); return DBM_ERR_INVALID; }
+    DBM_TRY(settle(s));
+    int64_t cap = 1;
+    for (const auto& r : steps) cap = std::max(cap, std::max(r.M, r.P));
+    if (cap > io_cap) {
+      if (io[0]) cudaFree(io[0]);
+      io[0] = nullptr;
+      DBM_CUDA(cudaMalloc(&io[0], sizeof(double) * (size_t)cap * (D + Q) * 2));
+      io_cap = cap;
+    }
+    double* buf[2] = {io[0], io[0] + (size_t)io_cap * (D + Q)};
+    const double* go = goff_out;
+    const double* gfo = gf_out;
+    for (int i = n - 1; i >= 0; --i) {
+      double* oo = i == 0 ? goff_in : buf[i & 1];
+      double* of = i == 0 ? gf_in : buf[i & 1] + (size_t)io_cap * D;
+      DBM_TRY(backward(i, go, gfo, oo, of, gtau, s));
+      go = oo;
+      gfo = of;
+    }
+    return DBM_OK;
+  }
+
   // A list in canonical CSR form (rows ascending, each row's pairs in enumeration order):
   // what = 0 start u32[rows + 1], 1 items u32[n], 2 displacements f64[D][n], 3 bits u32[n].
   int export_list(const PairList<real, D>& Lst, int what, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) {
@@ -1284,6 +1374,7 @@ struct TapeImpl : TapeBase, StepHook {
 
   int export_(int idx, int what, void* dst, int64_t nbytes, int64_t* needed, cudaStream_t s) override {
     if (idx < 0 || idx >= (int)steps.size()) { set_last_error("tape: no step %d", idx); return DBM_ERR_INVALID; }
+    DBM_TRY(settle(s));
     const StepRec<real, D>& r = steps[idx];
     const void* src = nullptr;
     int64_t n = 0;
@@ -1381,6 +1472,22 @@ int dbm_tape_clear(dbm_tape* t) {
 int dbm_tape_step(dbm_tape* t, void* stream) {
   TAPE_CHECK(t);
   return t->impl->step((cudaStream_t)stream);
+}
+int dbm_tape_set_estimate(dbm_tape* t, double pairs_per_row) {
+  TAPE_CHECK(t);
+  if (!(pairs_per_row >= 0)) { set_last_error("dbm_tape_set_estimate: bad estimate"); return DBM_ERR_INVALID; }
+  t->impl->set_estimate(pairs_per_row);
+  return DBM_OK;
+}
+int dbm_tape_record(dbm_tape* t, int32_t steps, void* stream) {
+  TAPE_CHECK(t);
+  for (int i = 0; i < steps; ++i) DBM_TRY(t->impl->step((cudaStream_t)stream));
+  return DBM_OK;
+}
+int dbm_tape_backward_all(dbm_tape* t, const double* goff_out, const double* gf_out, double* goff_in, double* gf_in,
+                          double* gtau, void* stream) {
+  TAPE_CHECK(t);
+  return t->impl->backward_all(goff_out, gf_out, goff_in, gf_in, gtau, (cudaStream_t)stream);
 }
 int32_t dbm_tape_length(dbm_tape* t) {
   if (!t || !t->impl) return -1;

@@ -230,6 +230,16 @@ int32_t dbm_tape_length(dbm_tape* tape);
 int dbm_tape_counts(dbm_tape* tape, int32_t index, int64_t* counts);
 int dbm_tape_backward(dbm_tape* tape, int32_t index, const double* d_g_off_out, const double* d_g_f_out,
                       double* d_g_off_in, double* d_g_f_in, double* d_g_tau, void* stream);
+/* dbm_tape_step `steps` times; and every recorded step in reverse, from the cotangents of the last
+ * step's output to those of the first step's input (one call per checkpoint segment). */
+int dbm_tape_record(dbm_tape* tape, int32_t steps, void* stream);
+/* Lists are sized from an estimate of pairs per row (grown to the largest seen; default 16).  A
+ * recording whose list outgrows it is found at the next synchronisation: the call then returns
+ * DBM_ERR_CAPACITY and the tape must be cleared and the segment recorded again from its start
+ * state.  Setting the estimate trades memory against such retries. */
+int dbm_tape_set_estimate(dbm_tape* tape, double pairs_per_row);
+int dbm_tape_backward_all(dbm_tape* tape, const double* d_g_off_out, const double* d_g_f_out, double* d_g_off_in,
+                          double* d_g_f_in, double* d_g_tau, void* stream);
 /* Copy a recorded array (DBM_TAPE_*) of step `index` into d_dst, converted to the listed type;
  * *needed returns its size in bytes. */
 int dbm_tape_export(dbm_tape* tape, int32_t index, int32_t what, void* d_dst, int64_t bytes, int64_t* needed,

@@ -254,3 +254,37 @@ def test_fp32dev_rollout_gradient_close_to_fp64():
     l32, g32 = out["fp32dev"]
     assert abs(l32 - l64) <= 1e-5 * abs(l64)
     assert np.linalg.norm(g32 - g64) <= 1e-3 * np.linalg.norm(g64), np.linalg.norm(g32 - g64) / np.linalg.norm(g64)
+
+
+def test_list_overflow_is_reported_and_a_second_recording_fits():
+    """A tape whose list estimate is far too small reports the overflow (TapeOverflow) at the next
+    synchronisation; the rollout then records the segment again and the gradient is unchanged."""
+    from direbm_gb300.adjoint import Tape, TapeOverflow, inverse_problem_loss
+
+    n, steps = 24, 4
+    x, field, target = _mode_problem(n, steps)
+    x_d = torch.as_tensor(x, device="cuda")
+    grads = []
+    for tiny in (False, True):
+        sim = _sim("D2Q9", [{"dims": (n, n), "tau": 0.6}], 1.0, 1.5, 1.0, "fp64", cap=4 * len(x))
+        tape = Tape(sim)
+        if tiny:
+            tape.set_estimate(0.01)
+        coeffs = torch.tensor(field.coeffs, dtype=torch.float64, device="cuda", requires_grad=True)
+        tau = torch.tensor([0.6], dtype=torch.float64, device="cuda", requires_grad=True)
+        loss = inverse_problem_loss(sim, x_d, field, coeffs, tau, target, steps, 2, tape)
+        loss.backward()
+        grads.append(torch.cat([coeffs.grad, tau.grad]).cpu().numpy())
+    np.testing.assert_array_equal(grads[0], grads[1])
+    # the error itself, on a direct recording
+    sim = _sim("D2Q9", [{"dims": (n, n), "tau": 0.6}], 1.0, 1.5, 1.0, "fp64", cap=4 * len(x))
+    from direbm_gb300.lattices import D2Q9
+    from direbm_gb300.adjoint import equilibrium
+
+    sim.set_state(None, x_d, equilibrium(torch.ones(len(x), dtype=torch.float64, device="cuda"),
+                                        field(x_d, torch.as_tensor(field.coeffs, device="cuda")), D2Q9))
+    tape = Tape(sim)
+    tape.set_estimate(0.0)
+    with pytest.raises(TapeOverflow):
+        tape.record(2)
+        tape.counts(1)
