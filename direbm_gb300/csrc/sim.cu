@@ -460,7 +460,8 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
     hi[a] = (int)floor(base + A.R + A.tiny);
   }
   double acc = 0;
-  CSum sa, sb;
+  CSum sa;
+  float sb = 0.f;  // deviation part: small, plain FMA accumulation suffices
 #pragma unroll 1
   for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
@@ -489,7 +490,7 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
                 acc += wgt * A.a.f64[(int64_t)k * A.mcap + m];
               } else {
                 sa.add_prod(wgt, A.a.rho[m]);
-                sb.add_prod(wgt, A.a.dev[(int64_t)k * A.mcap + m]);
+                sb = __fmaf_rn(wgt, A.a.dev[(int64_t)k * A.mcap + m], sb);
               }
             }
           }
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
                 acc += wgt * A.a.f64[(int64_t)kb * A.mcap + m];
               } else {
                 sa.add_prod(wgt, A.a.rho[m]);
-                sb.add_prod(wgt, A.a.dev[(int64_t)kb * A.mcap + m]);
+                sb = __fmaf_rn(wgt, A.a.dev[(int64_t)kb * A.mcap + m], sb);
               }
             }
           }
@@ -544,7 +545,7 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
   } else {
     // F = W_k * A + B in double-float
     DF Ad = df_norm(sa.hi, sa.lo);
-    DF Bd = df_norm(sb.hi, sb.lo);
+    DF Bd = DF{sb, 0.f};
     DF Fv = df_add(df_mul(DF{A.L.wf[k], A.L.wlo[k]}, Ad), Bd);
     A.cpfhi[(int64_t)k * A.ccap + j] = Fv.hi;
     A.cpflo[(int64_t)k * A.ccap + j] = Fv.lo;
