@@ -131,15 +131,15 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
   CSum csum[3];
 #pragma unroll 1
   for (int k = 0; k < Q; ++k) {
-    int lo[3] = {0, 0, 0};
+    int lo[3] = {0, 0, 0}, nn[3] = {1, 1, 1};
 #pragma unroll
-    for (int a = 0; a < D; ++a) lo[a] = -(int)floor((real)A.L.cd[k][a]) - 1;
+    for (int a = 0; a < D; ++a) thin_sources<real>((real)A.L.cd[k][a], &lo[a], &nn[a]);
 #pragma unroll 1
-    for (int oz = 0; oz < (D == 3 ? 2 : 1); ++oz)
+    for (int oz = 0; oz < nn[2]; ++oz)
 #pragma unroll 1
-      for (int oy = 0; oy < 2; ++oy)
+      for (int oy = 0; oy < nn[1]; ++oy)
 #pragma unroll 1
-        for (int ox = 0; ox < 2; ++ox) {
+        for (int ox = 0; ox < nn[0]; ++ox) {
           const int so[3] = {lo[0] + ox, lo[1] + oy, D == 3 ? lo[2] + oz : 0};
           uint32_t Sg;
           if (!cell_at<D>(I, Fc[0] + so[0], Fc[1] + so[1], Fc[2] + so[2], &Sg)) continue;

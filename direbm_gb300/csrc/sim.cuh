@@ -174,6 +174,18 @@ __device__ __forceinline__ T cell_d2_lower(const T (&c)[3]) {
 template <class P>
 __device__ __forceinline__ typename P::real floor_r(typename P::real x) { return floor(x); }
 
+// Source-cell offsets (per axis) from which a component of displacement cd can land in a cell:
+// floor(off + cd) over off in [0, 1), rounded in the working precision, takes only the values
+// floor(cd) .. floor(rn(below1 + cd)) (monotone rounding), so so = -floor(...) lies in
+// [lo, lo + n) with n = 1 or 2.  Cells outside this range hold no landing component.
+template <class real>
+__device__ __forceinline__ void thin_sources(real cd, int* lo, int* n) {
+  const real below1 = std::is_same<real, double>::value ? (real)nextafter(1.0, 0.0) : (real)nextafterf(1.0f, 0.0f);
+  const int fmin = (int)floor(cd), fmax = (int)floor(rn_add(below1, cd));
+  *lo = -fmax;
+  *n = fmax - fmin + 1;
+}
+
 // Squared distance (FP32, approximate) from the instance's sphere center to local cell S + o; used
 // only against margins that are wider than its error, to skip exact tests far from the solid.
 template <int D, class T>

@@ -197,11 +197,13 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
 #pragma unroll 1
     for (int k = 0; k < Q; ++k) {
       const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
-      const int lox = -(int)floor(cdx) - 1, loy = -(int)floor(cdy) - 1;
-#pragma unroll
-      for (int oy = 0; oy < 2; ++oy)
-#pragma unroll
-        for (int ox = 0; ox < 2; ++ox) {
+      int lox, nx, loy, ny;
+      thin_sources<real>(cdx, &lox, &nx);
+      thin_sources<real>(cdy, &loy, &ny);
+#pragma unroll 1
+      for (int oy = 0; oy < ny; ++oy)
+#pragma unroll 1
+        for (int ox = 0; ox < nx; ++ox) {
           const int sox = lox + ox, soy = loy + oy;
           const real fx0 = (real)(-sox), fy0 = (real)(-soy);
           const int ci = (by + soy) * rw + (bx + sox);
@@ -363,13 +365,15 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
 #pragma unroll 1
   for (int k = 0; k < Q; ++k) {
     const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
-    const int lox = -(int)floor(cdx) - 1, loy = -(int)floor(cdy) - 1;
-#pragma unroll
-    for (int oy = 0; oy < 2; ++oy) {
+    int lox, nx, loy, ny;
+    thin_sources<real>(cdx, &lox, &nx);
+    thin_sources<real>(cdy, &loy, &ny);
+#pragma unroll 1
+    for (int oy = 0; oy < ny; ++oy) {
       const int soy = loy + oy;
       const real fy0 = (real)(-soy), sy = (real)soy;
       const int row = (by + soy) * rw + bx;
-      const int m1 = s_end[row + lox + 1];
+      const int m1 = s_end[row + lox + nx - 1];
       for (int m = s_beg[row + lox]; m < m1; ++m) {
         const Item<real> it = s_it[m];
         const real tx = rn_add(it.ox, cdx), ty = rn_add(it.oy, cdy);
