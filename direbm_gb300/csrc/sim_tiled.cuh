@@ -85,15 +85,19 @@ __device__ __forceinline__ void stage_region(const InstK& I, int xr0, int yr0, i
     if (lane == 0) s_row[ry] = cnt;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (warp == 0) {  // exclusive prefix over the region rows, 32 at a time
     int acc = 0;
-    for (int ry = 0; ry < rh; ++ry) {
-      const int c = s_row[ry];
-      s_row[ry] = acc;
-      acc += c;
+    for (int r0 = 0; r0 < rh; r0 += 32) {
+      const int ry = r0 + lane;
+      const int c = ry < rh ? s_row[ry] : 0;
+      const int incl = warp_incl_scan(c);
+      if (ry < rh) s_row[ry] = acc + incl - c;
+      acc += __shfl_sync(0xffffffffu, incl, 31);
     }
-    s_row[rh] = acc;
-    s_row[rh + 1] = acc <= cap ? 1 : 0;
+    if (lane == 0) {
+      s_row[rh] = acc;
+      s_row[rh + 1] = acc <= cap ? 1 : 0;
+    }
   }
   __syncthreads();
   const bool local = s_row[rh + 1] != 0;
@@ -536,22 +540,26 @@ __device__ __forceinline__ int tile_items(const InstK& I, const Tile2& T, const 
                                           const uint32_t* __restrict__ start, const uint32_t* __restrict__ cellv,
                                           const real* __restrict__ off, int64_t stride, int c0, int cap_t,
                                           int* s_tr, int* s_ij, short* s_bx, short* s_by, Pair<real>* s_p) {
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {  // the tile's rows, one lane each (ty <= 32), prefix by a warp scan
     const int txe = min(G.tx, I.dims[0] - T.x0);
     int acc = 0;
-    for (int r = 0; r < G.ty; ++r) {
+    for (int r0 = 0; r0 < G.ty; r0 += 32) {
+      const int r = r0 + (int)threadIdx.x;
       const int y = T.y0 + r;
       int b = 0, c = 0;
-      if (y < I.dims[1]) {
+      if (r < G.ty && y < I.dims[1]) {
         const uint32_t g0 = I.base + (uint32_t)T.x0 + (uint32_t)I.dims[0] * (uint32_t)y;
         b = (int)start[g0];
         c = (int)start[g0 + txe] - b;
       }
-      s_tr[2 * r] = b;
-      s_tr[2 * r + 1] = acc;
-      acc += c;
+      const int incl = warp_incl_scan(c);
+      if (r < G.ty) {
+        s_tr[2 * r] = b;
+        s_tr[2 * r + 1] = acc + incl - c;
+      }
+      acc += __shfl_sync(0xffffffffu, incl, 31);
     }
-    s_tr[2 * G.ty] = acc;
+    if (threadIdx.x == 0) s_tr[2 * G.ty] = acc;
   }
   __syncthreads();
   const int n = s_tr[2 * G.ty];
