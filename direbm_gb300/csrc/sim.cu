@@ -208,25 +208,34 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
       lo[a] = (int)floor(base - A.R - A.tiny);
       hi[a] = (int)floor(base + A.R + A.tiny);
     }
+    const real bxr = cen[0] - cdk[0];
+    // window rows (sz, sy) in order, each one x range as runs of consecutive cells (see k_gather)
 #pragma unroll 1
     for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
-      for (int sy = lo[1]; sy <= hi[1]; ++sy)
-#pragma unroll 1
-        for (int sx = lo[0]; sx <= hi[0]; ++sx) {
-          const int dS[3] = {sx, sy, sz};
-          real c[3] = {0, 0, 0};
-#pragma unroll
-          for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], cen[a]);
-          if (cell_d2_lower<D, real>(c) > A.R2) continue;
-          uint32_t Sg;
-          if (!cell_at<D>(I, Fc[0] + sx, Fc[1] + sy, Fc[2] + sz, &Sg)) continue;
-          const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
-          for (uint32_t m = m0; m < m1; ++m) {
+      for (int sy = lo[1]; sy <= hi[1]; ++sy) {
+        const real cy = canon_c<real>(sy, cdk[1], cen[1]);
+        const real cz = D == 3 ? canon_c<real>(sz, cdk[2], cen[2]) : (real)0;
+        const real ly = axis_lb<real>(cy);
+        real lb2 = rn_mul(ly, ly);
+        if (D == 3) {
+          const real lz = axis_lb<real>(cz);
+          lb2 = rn_add(lb2, rn_mul(lz, lz));
+        }
+        if (lb2 > A.R2) continue;
+        const real hw = row_halfwidth2<real>(A.R2, lb2);
+        if (hw < (real)0) continue;
+        const int lox = max((int)floor(bxr - hw - A.tiny), lo[0]), hix = min((int)floor(bxr + hw + A.tiny), hi[0]);
+        if (lox > hix) continue;
+        row_runs<D>(I, Fc[0], Fc[1] + sy, Fc[2] + sz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
+          const uint32_t m1 = A.a.start[g1 + 1];
+          for (uint32_t m = A.a.start[g0]; m < m1; ++m) {
             if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: visited below
-            real o[3] = {0, 0, 0}, e[3];
-#pragma unroll
-            for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+            const PackItem<real> it = A.a.pk[m];
+            const int sx = (int)it.cx + shift - Fc[0];
+            const real c[3] = {canon_c<real>(sx, cdk[0], cen[0]), cy, cz};
+            const real o[3] = {it.x, it.y, it.z};
+            real e[3];
             if (canon_d2<D, real>(o, c, e) <= A.R2) {
               mask |= 1u << k;
               const real w = exp(fstar_at<Q, D, P>(A, m, k));
@@ -243,7 +252,8 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
               }
             }
           }
-        }
+        });
+      }
   }
   if (A.any_obstacle && I.has_obs && sphere_dist2<D, real>(I, Fc, cen) < I.reach2) {
     // bounced components (displacement 0, opposite label): window order, then moment, then slot
@@ -346,6 +356,24 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
   }
 }
 
+// Packed copy (offsets + cell x coordinate) of a state for the untiled window kernels.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_pack(const __grid_constant__ Args<Q, D, P> A, StateP<P> S, int64_t stride,
+                                              const uint32_t* __restrict__ d_n) {
+  using real = typename P::real;
+  const uint32_t n = *d_n;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t g = S.cell[i];
+    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
+    PackItem<real> it;
+    it.x = S.off[i];
+    it.y = D > 1 ? S.off[stride + i] : (real)0;
+    it.z = D > 2 ? S.off[2 * stride + i] : (real)0;
+    it.cx = (real)((g - I.base) % (uint32_t)I.dims[0]);
+    S.pk[i] = it;
+  }
+}
+
 // Sorted pairs -> next state's cells and offsets.
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_finalize(const __grid_constant__ Args<Q, D, P> A) {
@@ -398,40 +426,46 @@ __global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q,
   }
   double swd = 0;
   CSum sws;
+  // window rows (gz, gy) in order; per row one x range narrowed by the row's smallest |e_y|, |e_z|,
+  // visited as runs of consecutive cells (the items of a run are contiguous, in cell order)
+  const real tx = rn_add(o[0], cdk[0]);
 #pragma unroll 1
   for (int gz = lo[2]; gz <= hi[2]; ++gz)
 #pragma unroll 1
-    for (int gy = lo[1]; gy <= hi[1]; ++gy)
-#pragma unroll 1
-      for (int gx = lo[0]; gx <= hi[0]; ++gx) {
-        const int dG[3] = {gx, gy, gz};
-        // per cell: base = float(dS) + cd with dS = -dG; control-point offsets lie in [0, 1)
-        real base[3] = {0, 0, 0}, lb[3] = {0, 0, 0};
+    for (int gy = lo[1]; gy <= hi[1]; ++gy) {
+      // per axis: base = float(dS) + cd with dS = -dG; candidates have e in [fl(o + fl(base - 1)),
+      // fl(o + base)] (control-point offsets lie in [0, 1))
+      real base[3] = {0, 0, 0};
+      const int dG[3] = {0, gy, gz};
+      real lb2 = 0;
 #pragma unroll
-        for (int a = 0; a < D; ++a) {
-          base[a] = rn_add((real)(-dG[a]), cdk[a]);
-          // candidates have e in [fl(o + fl(base - 1)), fl(o + base)]
-          const real elo = rn_add(o[a], rn_sub(base[a], (real)1)), ehi = rn_add(o[a], base[a]);
-          lb[a] = elo > (real)0 ? elo : (ehi < (real)0 ? -ehi : (real)0);
-        }
-        real lb2 = 0;
-#pragma unroll
-        for (int a = 0; a < D; ++a) lb2 = a == 0 ? rn_mul(lb[a], lb[a]) : rn_add(lb2, rn_mul(lb[a], lb[a]));
-        if (lb2 > A.R2) continue;
-        uint32_t Gg;
-        if (!cell_at<D>(I, Sc[0] + gx, Sc[1] + gy, Sc[2] + gz, &Gg)) continue;
-        const uint32_t c0 = A.b.start[Gg], c1 = A.b.start[Gg + 1];
-        for (uint32_t c = c0; c < c1; ++c) {
-          real cc[3] = {0, 0, 0}, e[3];
-#pragma unroll
-          for (int a = 0; a < D; ++a) cc[a] = rn_sub(base[a], A.b.off[(int64_t)a * A.ccap + c]);
+      for (int a = 1; a < D; ++a) {
+        base[a] = rn_add((real)(-dG[a]), cdk[a]);
+        const real elo = rn_add(o[a], rn_sub(base[a], (real)1)), ehi = rn_add(o[a], base[a]);
+        const real lb = elo > (real)0 ? elo : (ehi < (real)0 ? -ehi : (real)0);
+        lb2 = a == 1 ? rn_mul(lb, lb) : rn_add(lb2, rn_mul(lb, lb));
+      }
+      if (lb2 > A.R2) continue;
+      const real hw = row_halfwidth2<real>(A.R2, lb2);
+      if (hw < (real)0) continue;
+      const int lox = max((int)floor(tx - hw - A.tiny), lo[0]), hix = min((int)floor(tx + hw + A.tiny), hi[0]);
+      if (lox > hix) continue;
+      row_runs<D>(I, Sc[0], Sc[1] + gy, Sc[2] + gz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
+        const uint32_t c1 = A.b.start[g1 + 1];
+        for (uint32_t c = A.b.start[g0]; c < c1; ++c) {
+          const PackItem<real> it = A.b.pk[c];
+          const int gx = (int)it.cx + shift - Sc[0];
+          const real cc[3] = {rn_sub(rn_add((real)(-gx), cdk[0]), it.x), rn_sub(base[1], it.y),
+                              D == 3 ? rn_sub(base[2], it.z) : (real)0};
+          real e[3];
           const real d2 = canon_d2<D, real>(o, cc, e);
           if (d2 <= A.R2) {
             const real d = rn_sqrt(d2);
             if constexpr (std::is_same<P, PF64>::value) swd += A.R - d; else sws.add(A.R - d);
           }
         }
-      }
+      });
+    }
   real sw;
   if constexpr (std::is_same<P, PF64>::value) sw = swd; else sw = sws.value();
   A.sw[(int64_t)k * A.mcap + m] = sw > (real)0 ? (real)1 / sw : (real)0;  // stored inverted
@@ -462,25 +496,35 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
   double acc = 0;
   CSum sa;
   float sb = 0.f;  // deviation part: small, plain FMA accumulation suffices
+  const real bxr = p[0] - cdk[0];
+  // window rows (sz, sy) in order; per row one x range narrowed by the row's smallest |e_y|, |e_z|,
+  // visited as runs of consecutive cells (the items of a run are contiguous, in cell order)
 #pragma unroll 1
   for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
-    for (int sy = lo[1]; sy <= hi[1]; ++sy)
-#pragma unroll 1
-      for (int sx = lo[0]; sx <= hi[0]; ++sx) {
-        const int dS[3] = {sx, sy, sz};
-        real c[3] = {0, 0, 0};
-#pragma unroll
-        for (int a = 0; a < D; ++a) c[a] = canon_c<real>(dS[a], cdk[a], p[a]);
-        if (cell_d2_lower<D, real>(c) > A.R2) continue;
-        uint32_t Sg;
-        if (!cell_at<D>(I, Gc[0] + sx, Gc[1] + sy, Gc[2] + sz, &Sg)) continue;
-        const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
-        for (uint32_t m = m0; m < m1; ++m) {
+    for (int sy = lo[1]; sy <= hi[1]; ++sy) {
+      const real cy = canon_c<real>(sy, cdk[1], p[1]);
+      const real cz = D == 3 ? canon_c<real>(sz, cdk[2], p[2]) : (real)0;
+      const real ly = axis_lb<real>(cy);
+      real lb2 = rn_mul(ly, ly);
+      if (D == 3) {
+        const real lz = axis_lb<real>(cz);
+        lb2 = rn_add(lb2, rn_mul(lz, lz));
+      }
+      if (lb2 > A.R2) continue;
+      const real hw = row_halfwidth2<real>(A.R2, lb2);
+      if (hw < (real)0) continue;
+      const int lox = max((int)floor(bxr - hw - A.tiny), lo[0]), hix = min((int)floor(bxr + hw + A.tiny), hi[0]);
+      if (lox > hix) continue;
+      row_runs<D>(I, Gc[0], Gc[1] + sy, Gc[2] + sz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
+        const uint32_t m1 = A.a.start[g1 + 1];
+        for (uint32_t m = A.a.start[g0]; m < m1; ++m) {
           if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: label opp[k]
-          real o[3] = {0, 0, 0}, e[3];
-#pragma unroll
-          for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
+          const PackItem<real> it = A.a.pk[m];
+          const int sx = (int)it.cx + shift - Gc[0];
+          const real c[3] = {canon_c<real>(sx, cdk[0], p[0]), cy, cz};
+          const real o[3] = {it.x, it.y, it.z};
+          real e[3];
           const real d2 = canon_d2<D, real>(o, c, e);
           if (d2 <= A.R2) {
             const real inv = A.sw[(int64_t)k * A.mcap + m];
@@ -495,7 +539,8 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
             }
           }
         }
-      }
+      });
+    }
   if (A.any_obstacle && k > 0 && I.has_obs && sphere_dist2<D, real>(I, Gc, p) < I.reach2) {
     // components of slot kb = opp[k] that bounced carry label k and sit at their moment's offset
     const int kb = A.L.opp[k];
@@ -920,6 +965,7 @@ struct SimImpl : SimBase {
       const int64_t cap = std::max(mcap, ccap);
       DBM_TRY(alloc(&S.cell, cap));
       DBM_TRY(alloc(&S.off, (int64_t)D * cap));
+      DBM_TRY(alloc(&S.pk, cap));
       if constexpr (std::is_same<P, PF64>::value) {
         DBM_TRY(alloc(&S.f64, (int64_t)Q * cap));
       } else {
@@ -1168,6 +1214,12 @@ struct SimImpl : SimBase {
     const unsigned gm = std::min<unsigned>(div_up(mcap, 256), (unsigned)sm_count() * 16);
     k_collide<Q, D, P><<<gm, 256, 0, s>>>(A);
     DBM_LAUNCH_CHECK();
+    // the untiled window kernels (3D, obstacles, or tiles off) read packed items
+    const bool untiled = !(D == 2 && tiled && use_tiles && !A.any_obstacle);
+    if (untiled) {
+      k_pack<Q, D, P><<<gm, 256, 0, s>>>(A, A.a, A.mcap, A.a.count);
+      DBM_LAUNCH_CHECK();
+    }
     mark(1, s);
     if (upto <= 1) return DBM_OK;
     if constexpr (D == 2) {
@@ -1189,6 +1241,10 @@ struct SimImpl : SimBase {
     const unsigned gc = std::min<unsigned>(div_up(ccap, 256), (unsigned)sm_count() * 16);
     k_finalize<Q, D, P><<<gc, 256, 0, s>>>(A);
     DBM_LAUNCH_CHECK();
+    if (untiled) {
+      k_pack<Q, D, P><<<gc, 256, 0, s>>>(A, A.b, A.ccap, A.d_P);
+      DBM_LAUNCH_CHECK();
+    }
     k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, s>>>(
         A.skeys, A.d_P, ncells, A.b.start);
     DBM_LAUNCH_CHECK();

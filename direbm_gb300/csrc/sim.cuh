@@ -41,11 +41,19 @@ struct PF32 {
   static constexpr int id = DBM_FP32DEV;
 };
 
+// A moment (or control point) packed for the untiled window loops: its offsets and its cell's x
+// coordinate in the box (an exact small integer), one aligned load.
+template <class real>
+struct alignas(4 * sizeof(real)) PackItem {
+  real x, y, z, cx;
+};
+
 template <class P>
 struct StateP {
   using real = typename P::real;
   uint32_t* cell = nullptr;   // [cap]
   real* off = nullptr;        // [D][cap]
+  PackItem<real>* pk = nullptr;  // [cap] packed copy for the untiled window kernels
   double* f64 = nullptr;      // FP64: [Q][cap]
   float* rho = nullptr;       // FP32DEV: [cap]
   float* dev = nullptr;       // FP32DEV: [Q][cap]
@@ -173,6 +181,59 @@ __device__ __forceinline__ T cell_d2_lower(const T (&c)[3]) {
 
 template <class P>
 __device__ __forceinline__ typename P::real floor_r(typename P::real x) { return floor(x); }
+
+// One window row of cells (x0 + lo .. x0 + hi, unwrapped, at box row y, z) as at most two runs of
+// consecutive cells of the box, in ascending unwrapped x: fn(first global cell, last global cell,
+// shift) with unwrapped x = (cell x in the box) + shift.  Returns false if the row lies outside a
+// bounded box.  Windows are narrower than every box, so a row wraps at most once.
+template <int D, class Fn>
+__device__ __forceinline__ bool row_runs(const InstK& I, int x0, int y, int z, int lo, int hi, Fn&& fn) {
+  const int nx = I.dims[0], ny = I.dims[1], nz = I.dims[2];
+  if (I.periodic) {
+    y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+    if (D == 3) z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
+  } else if (y < 0 || y >= ny || (D == 3 && (z < 0 || z >= nz))) {
+    return false;
+  }
+  const uint32_t row = I.base + (uint32_t)nx * ((uint32_t)y + (D == 3 ? (uint32_t)ny * (uint32_t)z : 0u));
+  int a = x0 + lo, b = x0 + hi;
+  if (!I.periodic) {
+    a = max(a, 0);
+    b = min(b, nx - 1);
+    if (a <= b) fn(row + (uint32_t)a, row + (uint32_t)b, 0);
+    return true;
+  }
+  if (a < 0) {
+    fn(row + (uint32_t)(a + nx), row + (uint32_t)(nx - 1), -nx);
+    a = 0;
+  }
+  if (b >= nx) {
+    if (a <= nx - 1) fn(row + (uint32_t)a, row + (uint32_t)(nx - 1), 0);
+    fn(row, row + (uint32_t)(b - nx), nx);
+  } else if (a <= b) {
+    fn(row + (uint32_t)a, row + (uint32_t)b, 0);
+  }
+  return true;
+}
+
+// Half-width bound on |e_x| for a window row whose candidates have e_y^2 + e_z^2 >= lb2 (each
+// square and the sum rounded): any hit has fl(e_x^2) + lb2 <= R2 up to a couple of roundings, so
+// |e_x| <= sqrt(R2 - lb2 + R2 * 2^-20).  Returns < 0 if the row cannot hold a hit.
+template <class real>
+__device__ __forceinline__ real row_halfwidth2(real R2, real lb2) {
+  const float rem = (float)(R2 - lb2);
+  if (rem < -(float)R2 * 1e-6f) return (real)-1;
+  const float x = fmaxf(rem, 0.f) + (float)R2 * 9.5367431640625e-07f;
+  return (real)(__fsqrt_rz(x) * 1.0001f + 1e-6f);
+}
+
+// Lower bound of |e| on one axis over the candidates of a window cell whose e lies in
+// [fl(c), fl(c + 1)] (offsets in [0, 1), rounding monotonic).
+template <class real>
+__device__ __forceinline__ real axis_lb(real c) {
+  const real hi = rn_add(c, (real)1);
+  return c > (real)0 ? c : (hi < (real)0 ? -hi : (real)0);
+}
 
 // Source-cell offsets (per axis) from which a component of displacement cd can land in a cell:
 // floor(off + cd) over off in [0, 1), rounded in the working precision, takes only the values
