@@ -661,8 +661,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=N_INST, help="first N ensemble members (profiling runs)")
-    ap.add_argument("--legs", default="all", choices=["all", "main", "adjoint", "sphere"],
-                    help="main = timed step only; adjoint / sphere = that leg only")
+    ap.add_argument("--legs", default="all", choices=["all", "main", "adjoint", "sphere", "lbm"],
+                    help="main = timed step only; adjoint / sphere / lbm = that leg only")
     ap.add_argument("--adjoint-n", type=int, default=256, help="adjoint leg: points per side")
     ap.add_argument("--adjoint-steps", type=int, default=100, help="adjoint leg: rollout steps")
     ap.add_argument("--adjoint-every", type=int, default=10, help="adjoint leg: checkpoint interval")
@@ -670,6 +670,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.legs == "lbm" and args.impl == "ours":
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"lbm": lbm_leg()}), flush=True)
+        return
     if args.legs == "sphere" and args.impl == "ours":
         import torch
 

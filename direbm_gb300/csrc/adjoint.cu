@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(256) k_rec_thin_cell(const __grid_constant__ A
     for (int k = 0; k < Q; ++k) {
       int x[3] = {Sc[0], Sc[1], Sc[2]};
 #pragma unroll
-      for (int a = 0; a < D; ++a) x[a] += (int)floor(rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]));
+      for (int a = 0; a < D; ++a) x[a] += (int)floor(rn_add(A.a.off[(int64_t)a * A.mcap + m], A.L.template cd_as<real>(k, a)));
       uint32_t F;
       thin_cell[(int64_t)k * M + m] = cell_at<D>(I, x[0], x[1], x[2], &F) ? F : kNone;
     }
@@ -227,7 +227,7 @@ __device__ __forceinline__ uint32_t enum_refine_cp(const Args<Q, D, P>& A, const
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     cen[a] = r.cp_cen[(int64_t)a * r.P + j];
-    cdk[a] = (real)A.L.cd[k][a];
+    cdk[a] = A.L.template cd_as<real>(k, a);
     const real base = cen[a] - cdk[a];
     lo[a] = (int)floor(base - A.R - A.tiny);
     hi[a] = (int)floor(base + A.R + A.tiny);
@@ -274,7 +274,7 @@ __device__ __forceinline__ uint32_t enum_resample_cp(const Args<Q, D, P>& A, int
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     p[a] = A.b.off[(int64_t)a * A.ccap + j];
-    cdk[a] = (real)A.L.cd[k][a];
+    cdk[a] = A.L.template cd_as<real>(k, a);
     const real base = p[a] - cdk[a];
     lo[a] = (int)floor(base - A.R - A.tiny);
     hi[a] = (int)floor(base + A.R + A.tiny);
@@ -324,7 +324,7 @@ __device__ __forceinline__ uint32_t enum_comp(const Args<Q, D, P>& A, const Step
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     o[a] = A.a.off[(int64_t)a * A.mcap + m];
-    cdk[a] = (real)A.L.cd[k][a];
+    cdk[a] = A.L.template cd_as<real>(k, a);
     const real tt = rn_add(o[a], cdk[a]);
     lo[a] = (int)floor(tt - A.R - A.tiny);
     hi[a] = (int)floor(tt + A.R + A.tiny);
@@ -795,7 +795,7 @@ __global__ void __launch_bounds__(256) k_bwd_moment(const __grid_constant__ RecK
     }
     const InstK I = K.inst[find_instance(K.inst_base, K.n_inst, K.r.in_cell[m])];
     const real tau = (real)I.tau, itau = (real)1 / tau;
-    const real inv = (real)K.L.inv_cs2;
+    const real inv = K.L.template inv_cs2_as<real>();
     real rho, u[D], fmfeq[Q], feqw[Q];  // fmfeq = feq - f;  feqw = feq / rho
     if constexpr (std::is_same<P, PF64>::value) {
       real f[Q], mom[D];
@@ -848,10 +848,10 @@ __global__ void __launch_bounds__(256) k_bwd_moment(const __grid_constant__ RecK
       tb += g[k] * fmfeq[k];
       real cu = 0;
 #pragma unroll
-      for (int a = 0; a < D; ++a) cu += (real)K.L.c[k][a] * u[a];
-      const real gw = g[k] * (real)K.L.w[k] * inv;
+      for (int a = 0; a < D; ++a) cu += K.L.template c_as<real>(k, a) * u[a];
+      const real gw = g[k] * K.L.template w_as<real>(k) * inv;
 #pragma unroll
-      for (int a = 0; a < D; ++a) h[a] += gw * ((real)K.L.c[k][a] * ((real)1 + inv * cu) - u[a]);
+      for (int a = 0; a < D; ++a) h[a] += gw * (K.L.template c_as<real>(k, a) * ((real)1 + inv * cu) - u[a]);
     }
     real hu = 0;
 #pragma unroll
@@ -860,7 +860,7 @@ __global__ void __launch_bounds__(256) k_bwd_moment(const __grid_constant__ RecK
     for (int q = 0; q < Q; ++q) {
       real hc = 0;
 #pragma unroll
-      for (int a = 0; a < D; ++a) hc += h[a] * (real)K.L.c[q][a];
+      for (int a = 0; a < D; ++a) hc += h[a] * K.L.template c_as<real>(q, a);
       gf_in[m * Q + q] = (double)(((real)1 - itau) * g[q] + itau * (phi + hc - hu));
     }
 #pragma unroll

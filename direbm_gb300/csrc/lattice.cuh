@@ -42,7 +42,26 @@ struct LatK {
   double cd[Q][D]; // c * dx / cell (cell units)
   float cdf[Q][D]; // float(c * dx / cell)
   double inv_cs2;
+  float inv_cs2f;  // float(1/cs^2): a double->float conversion runs on the narrow FP64 pipe
   int opp[Q];      // index of -c_k
+
+  // 1/cs^2 in the arithmetic type T, without a per-thread conversion for T = float
+  template <class T>
+  __host__ __device__ __forceinline__ T inv_cs2_as() const {
+    if constexpr (sizeof(T) == sizeof(float)) return inv_cs2f; else return (T)inv_cs2;
+  }
+  template <class T>
+  __host__ __device__ __forceinline__ T c_as(int k, int a) const {
+    if constexpr (sizeof(T) == sizeof(float)) return cf[k][a]; else return (T)c[k][a];
+  }
+  template <class T>
+  __host__ __device__ __forceinline__ T cd_as(int k, int a) const {
+    if constexpr (sizeof(T) == sizeof(float)) return cdf[k][a]; else return (T)cd[k][a];
+  }
+  template <class T>
+  __host__ __device__ __forceinline__ T w_as(int k) const {
+    if constexpr (sizeof(T) == sizeof(float)) return wf[k]; else return (T)w[k];
+  }
 };
 
 template <int Q, int D>
@@ -61,6 +80,7 @@ LatK<Q, D> make_latk(const LatHost& h, double dx, double cell) {
     }
   }
   k.inv_cs2 = 1.0 / h.cs2;
+  k.inv_cs2f = (float)k.inv_cs2;
   for (int q = 0; q < Q; ++q) {
     k.opp[q] = q;
     for (int r = 0; r < Q; ++r) {
@@ -75,7 +95,7 @@ LatK<Q, D> make_latk(const LatHost& h, double dx, double cell) {
 // f_eq of (rho, u) for all directions, in T arithmetic (reference formula and operation order).
 template <int Q, int D, class T>
 __device__ __forceinline__ void equilibrium_all(T rho, const T (&u)[D], const LatK<Q, D>& L, T (&feq)[Q]) {
-  const T inv = (T)L.inv_cs2;
+  const T inv = L.template inv_cs2_as<T>();
   T usq = 0;
 #pragma unroll
   for (int a = 0; a < D; ++a) usq += u[a] * u[a];
@@ -83,9 +103,9 @@ __device__ __forceinline__ void equilibrium_all(T rho, const T (&u)[D], const La
   for (int k = 0; k < Q; ++k) {
     T cu = 0;
 #pragma unroll
-    for (int a = 0; a < D; ++a) cu += (T)L.c[k][a] * u[a];
+    for (int a = 0; a < D; ++a) cu += L.template c_as<T>(k, a) * u[a];
     T br = (T)1 + inv * cu + (T)0.5 * inv * inv * cu * cu - (T)0.5 * inv * usq;
-    feq[k] = rho * (T)L.w[k] * br;
+    feq[k] = rho * L.template w_as<T>(k) * br;
   }
 }
 
@@ -93,7 +113,7 @@ __device__ __forceinline__ void equilibrium_all(T rho, const T (&u)[D], const La
 template <int Q, int D>
 __device__ __forceinline__ void eq_deviation_f32(float rho, const float (&u)[D], const LatK<Q, D>& L,
                                                  float (&deq)[Q]) {
-  const float inv = (float)L.inv_cs2;
+  const float inv = L.inv_cs2f;
   float usq = 0.f;
 #pragma unroll
   for (int a = 0; a < D; ++a) usq += u[a] * u[a];
@@ -119,7 +139,7 @@ __device__ __forceinline__ void collide_moment(T (&f)[Q], T tau, const LatK<Q, D
   for (int k = 0; k < Q; ++k) {
     rho += f[k];
 #pragma unroll
-    for (int a = 0; a < D; ++a) mom[a] += f[k] * (T)L.c[k][a];
+    for (int a = 0; a < D; ++a) mom[a] += f[k] * L.template c_as<T>(k, a);
   }
   T u[D];
 #pragma unroll

@@ -42,18 +42,26 @@ __global__ void __launch_bounds__(256) k_lbm_f64(const T* __restrict__ src, T* _
   }
 }
 
-__global__ void __launch_bounds__(256) k_lbm_dev(const float* __restrict__ src, float* __restrict__ dst, int ni,
-                                                 int nj, int runs, const double* __restrict__ taus, float rho0,
-                                                 LatK<7, 2> L) {
+__global__ void __launch_bounds__(256, 8) k_lbm_dev(const float* __restrict__ src, float* __restrict__ dst, int ni,
+                                                    int nj, int runs, const double* __restrict__ taus, float rho0,
+                                                    LatK<7, 2> L) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int jr = blockIdx.y;
-  if (i >= ni) return;
   const int j = jr % nj, r = jr / nj;
   const int64_t plane = (int64_t)ni * nj;
-  const float* s = src + (int64_t)r * 7 * plane + (int64_t)j * ni + i;
+  const bool live = i < ni;
   float dv[7];
+  if (live) {
+    const float* s = src + (int64_t)r * 7 * plane + (int64_t)j * ni + i;
 #pragma unroll
-  for (int k = 0; k < 7; ++k) dv[k] = s[k * plane];
+    for (int k = 0; k < 7; ++k) dv[k] = s[k * plane];
+  }
+  // One block covers one row of one run, so 1/tau is formed once per block, while the loads
+  // above are in flight: an FP64 divide in every thread made the narrow FP64 pipe the limiter.
+  __shared__ float s_inv_tau;
+  if (threadIdx.x == 0) s_inv_tau = (float)(1.0 / taus[r]);
+  __syncthreads();
+  if (!live) return;
   // rho - rho0 and momentum from the deviations only
   float drho = 0.f, mx = 0.f, my = 0.f;
 #pragma unroll
@@ -66,7 +74,7 @@ __global__ void __launch_bounds__(256) k_lbm_dev(const float* __restrict__ src, 
   const float u[2] = {mx / rho, my / rho};
   float deq[7];
   eq_deviation_f32<7, 2>(rho, u, L, deq);  // rho*W*(...) without the rest part
-  const float inv_tau = (float)(1.0 / taus[r]);
+  const float inv_tau = s_inv_tau;
   float* d = dst + (int64_t)r * 7 * plane;
 #pragma unroll
   for (int k = 0; k < 7; ++k) {

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) k_collide(const __grid_constant__ Args<Q,
         if ((bm >> k) & 1u) continue;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
-          real t = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
+          real t = rn_add(A.a.off[(int64_t)a * A.mcap + m], A.L.template cd_as<real>(k, a));
           int x = c[a] + (int)floor(t);
           out |= (x < 0) | (x >= I.dims[a]);
         }
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
   for (int k = 0; k < Q; ++k) {
     int lo[3] = {0, 0, 0}, nn[3] = {1, 1, 1};
 #pragma unroll
-    for (int a = 0; a < D; ++a) thin_sources<real>((real)A.L.cd[k][a], &lo[a], &nn[a]);
+    for (int a = 0; a < D; ++a) thin_sources<real>(A.L.template cd_as<real>(k, a), &lo[a], &nn[a]);
 #pragma unroll 1
     for (int oz = 0; oz < nn[2]; ++oz)
 #pragma unroll 1
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
             bool land = true;
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-              t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], (real)A.L.cd[k][a]);
+              t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], A.L.template cd_as<real>(k, a));
               land &= (so[a] + (int)floor(t[a])) == 0;
             }
             if (land) {
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
     real cdk[3] = {0, 0, 0};
 #pragma unroll
     for (int a = 0; a < D; ++a) {
-      cdk[a] = (real)A.L.cd[k][a];
+      cdk[a] = A.L.template cd_as<real>(k, a);
       const real base = cen[a] - cdk[a];
       lo[a] = (int)floor(base - A.R - A.tiny);
       hi[a] = (int)floor(base + A.R + A.tiny);
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q,
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     o[a] = A.a.off[(int64_t)a * A.mcap + m];
-    cdk[a] = bounced ? (real)0 : (real)A.L.cd[k][a];
+    cdk[a] = bounced ? (real)0 : A.L.template cd_as<real>(k, a);
     const real t = rn_add(o[a], cdk[a]);
     lo[a] = (int)floor(t - A.R - A.tiny);
     hi[a] = (int)floor(t + A.R + A.tiny);
@@ -488,7 +488,7 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
 #pragma unroll
   for (int a = 0; a < D; ++a) {
     p[a] = A.b.off[(int64_t)a * A.ccap + j];
-    cdk[a] = (real)A.L.cd[k][a];
+    cdk[a] = A.L.template cd_as<real>(k, a);
     const real base = p[a] - cdk[a];
     lo[a] = (int)floor(base - A.R - A.tiny);
     hi[a] = (int)floor(base + A.R + A.tiny);

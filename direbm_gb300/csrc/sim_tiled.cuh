@@ -200,7 +200,7 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
     CSum csum[2];
 #pragma unroll 1
     for (int k = 0; k < Q; ++k) {
-      const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+      const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
       int lox, nx, loy, ny;
       thin_sources<real>(cdx, &lox, &nx);
       thin_sources<real>(cdy, &loy, &ny);
@@ -253,7 +253,7 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
       __syncthreads();
     }
     if (!occupied) continue;
-    const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+    const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
     const real bxr = cen[0] - cdx, byr = cen[1] - cdy;
     const int lox = max((int)floor(bxr - A.R - A.tiny), -bx), hix = min((int)floor(bxr + A.R + A.tiny), rw - 1 - bx);
     const int loy = max((int)floor(byr - A.R - A.tiny), -by), hiy = min((int)floor(byr + A.R + A.tiny), rh - 1 - by);
@@ -368,7 +368,7 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
   CSum csum[2];
 #pragma unroll 1
   for (int k = 0; k < Q; ++k) {
-    const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+    const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
     int lox, nx, loy, ny;
     thin_sources<real>(cdx, &lox, &nx);
     thin_sources<real>(cdy, &loy, &ny);
@@ -419,7 +419,7 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
   float swf = 0.f, sxf[2] = {0.f, 0.f};
 #pragma unroll 1
   for (int k = 0; k < Q; ++k) {
-    const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+    const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
     const real bxr = cen[0] - cdx, byr = cen[1] - cdy;
     const int loy = max((int)floor(byr - A.R - A.tiny), -by), hiy = min((int)floor(byr + A.R + A.tiny), rh - 1 - by);
     const real* wk = s_w + k * cap;
@@ -601,7 +601,7 @@ __device__ __forceinline__ void weights_body(const Args<Q, 2, P>& A, const InstK
     const int nc = min(cap_t, n - c0);
 #pragma unroll 1
     for (int k = 0; k < Q; ++k) {
-      const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+      const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
       for (int i = threadIdx.x; i < nc; i += blockDim.x) {
         const int bx = s_bx[i], by = s_by[i];
         const Pair<real> mo = s_mpos[i];
@@ -665,7 +665,7 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
     // so the threads of a block finish together; each unit's sum is still one thread's loop
     for (int wu = threadIdx.x; wu < nc * Q; wu += blockDim.x) {
       const int k = wu / nc, i = wu - k * nc;
-      const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+      const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
       {
         const int bx = s_bx[i], by = s_by[i];
         const real bxf = (real)bx;
@@ -769,7 +769,7 @@ __device__ __forceinline__ void gather_body(const Args<Q, 2, P>& A, const InstK&
         }
         __syncthreads();
       }
-      const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+      const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
       for (int i = threadIdx.x; i < nc; i += blockDim.x) {
         const int bx = s_bx[i], by = s_by[i];
         const Pair<real> pp = s_cpos[i];
@@ -867,7 +867,7 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
         s_kv[l] = Pair<real>{ginv[gm], gfk[gm]};
       }
       __syncthreads();
-      const real cdx = (real)A.L.cd[k][0], cdy = (real)A.L.cd[k][1];
+      const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
       for (int i = threadIdx.x; i < nc; i += blockDim.x) {
         const int bx = s_bx[i], by = s_by[i];
         const real bxf = (real)bx;
