@@ -298,9 +298,12 @@ def lbm_leg(steps=100, warmup=5):
     return res
 
 
-def e2e_leg(sim, ib, x, f, steps=2):
+def e2e_leg(sim, ib, x, f, steps=3, warmup=1):
     """Same metric through the public API with host buffers: every step copies the state from pinned
-    host memory, loads it, steps once, exports it and copies it back."""
+    host memory, loads it, steps once, exports it and copies it back.  One untimed step first, so
+    that the output tensors' first allocation is not timed.  The host<->device copies move ~1.4 GB
+    each way per step; their rate depends on the host side (NUMA placement, other jobs), so the
+    line also reports the copy bandwidth seen on a separate timed copy."""
     import torch
 
     M = len(x)
@@ -313,7 +316,31 @@ def e2e_leg(sim, ib, x, f, steps=2):
     o_inst = torch.empty(M, dtype=torch.int32).pin_memory()
     o_pos = torch.empty((M, 2), dtype=torch.float64).pin_memory()
     o_f = torch.empty((M, 9), dtype=torch.float64).pin_memory()
+    def one_step():
+        d_inst.copy_(h_inst, non_blocking=True)
+        d_pos.copy_(h_pos, non_blocking=True)
+        d_f.copy_(h_f, non_blocking=True)
+        sim.set_state(d_inst, d_pos, d_f)
+        sim.step(1)
+        gi, gp, gf = sim.state()
+        m2 = gi.shape[0]
+        o_inst[:m2].copy_(gi, non_blocking=True)
+        o_pos[:m2].copy_(gp, non_blocking=True)
+        o_f[:m2].copy_(gf, non_blocking=True)
+
+    for _ in range(warmup):
+        one_step()
     torch.cuda.synchronize()
+    # copy bandwidth alone (the largest array, each way)
+    c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    c0.record()
+    d_f.copy_(h_f, non_blocking=True)
+    c1.record()
+    o_f.copy_(d_f, non_blocking=True)
+    c2.record()
+    torch.cuda.synchronize()
+    h2d_gbs = h_f.numel() * 8 / (c0.elapsed_time(c1) * 1e-3) / 1e9
+    d2h_gbs = h_f.numel() * 8 / (c1.elapsed_time(c2) * 1e-3) / 1e9
     t0 = time.perf_counter()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -338,7 +365,8 @@ def e2e_leg(sim, ib, x, f, steps=2):
     wall = time.perf_counter() - t0
     ms = e0.elapsed_time(e1)
     return {"value": points / (ms * 1e-3), "unit": "point-steps/s", "h2d_bytes_per_step": int(h2d // steps),
-            "d2h_bytes_per_step": int(d2h // steps), "ms_per_step": ms / steps, "wall_s": wall,
+            "d2h_bytes_per_step": int(d2h // steps), "ms_per_step": ms / steps, "wall_s": wall, "steps": steps,
+            "warmup": warmup, "copy_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs},
             "path": "Simulation.set_state/step/state (C ABI dbm_sim_*) with pinned host buffers"}
 
 
@@ -618,7 +646,7 @@ def run_ours(args):
               flush=True)
         sim.close()
         return
-    e2e = e2e_leg(sim, ib, x, f, steps=2)
+    e2e = e2e_leg(sim, ib, x, f)
     sim.close()
 
     # FP64 store on the same workload

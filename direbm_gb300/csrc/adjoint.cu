@@ -1015,6 +1015,10 @@ struct TapeImpl : TapeBase, StepHook {
   }
 
   int step(cudaStream_t s) override {
+    if (sim->kappa_soft > 0) {  // spawned control points have no recorded VJP
+      set_last_error("tape: the adjoint does not cover the soft-outer spawn (DBM_OPT_KAPPA_SOFT)");
+      return DBM_ERR_INVALID;
+    }
     cur = StepRec<real, D>{};
     known_version = ~0ull - 1;
     DBM_TRY(sim->step_hooked(this, s));

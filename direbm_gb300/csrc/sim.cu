@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
   }
   if (cnt == 0) {
     A.occ[F] = 0u;
+    if (A.kappa_soft > 0) A.occ[A.ncells + F] = 0u;
     if (A.write_trace) { A.tcnt[F] = 0u; A.mask[F] = 0u; }
     return;
   }
@@ -197,8 +198,11 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
   uint32_t mask = 0;
   double swd = 0, sxd[3] = {0, 0, 0};
   float swf = 0.f, sxf[3] = {0.f, 0.f, 0.f};
+  // soft spawn: sum of the components' direction vectors, FP64 (regular ones as count * c_k)
+  double csr[3] = {0, 0, 0}, csb[3] = {0, 0, 0};
 #pragma unroll 1
   for (int k = 0; k < Q; ++k) {
+    int nk = 0;
     int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     real cdk[3] = {0, 0, 0};
 #pragma unroll
@@ -238,6 +242,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
             real e[3];
             if (canon_d2<D, real>(o, c, e) <= A.R2) {
               mask |= 1u << k;
+              ++nk;
               const real w = exp(fstar_at<Q, D, P>(A, m, k));
               if constexpr (std::is_same<P, PF64>::value) {
                 // separate rounding of product and sum (no FMA), in loop order: the oracle
@@ -254,6 +259,10 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
           }
         });
       }
+    if (A.kappa_soft > 0 && nk > 0) {
+#pragma unroll
+      for (int a = 0; a < D; ++a) csr[a] = __dadd_rn(csr[a], __dmul_rn((double)nk, A.L.c[k][a]));
+    }
   }
   if (A.any_obstacle && I.has_obs && sphere_dist2<D, real>(I, Fc, cen) < I.reach2) {
     // bounced components (displacement 0, opposite label): window order, then moment, then slot
@@ -287,6 +296,10 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
             for (int k = 1; k < Q; ++k) {
               if (!((bits >> k) & 1u)) continue;
               mask |= 1u << A.L.opp[k];
+              if (A.kappa_soft > 0) {
+#pragma unroll
+                for (int a = 0; a < D; ++a) csb[a] = __dadd_rn(csb[a], A.L.c[A.L.opp[k]][a]);
+              }
               const real w = exp(fstar_at<Q, D, P>(A, m, k));
               if constexpr (std::is_same<P, PF64>::value) {
                 swd = __dadd_rn(swd, w);
@@ -348,6 +361,52 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
   A.fkey[F] = inside ? G : 0xffffffffu;
 #pragma unroll
   for (int a = 0; a < D; ++a) A.foff[(int64_t)a * A.ncells + F] = off[a];
+  if (A.kappa_soft > 0) {
+    // soft-outer spawn (direbm/reference/simulator.py:126-166): the new CP sits soft_off cells from
+    // the centroid (the CP before its move) along the normalised direction sum; every operation
+    // in FP64 with one rounding each, the offset then rounded to the working precision
+    bool spawned = false;
+    uint32_t G2 = 0xffffffffu;
+    real off2[3] = {0, 0, 0};
+    if (kappa > A.kappa_hard && kappa <= A.kappa_soft) {
+      double cs[3] = {0, 0, 0};
+#pragma unroll
+      for (int a = 0; a < D; ++a) cs[a] = __dadd_rn(csr[a], csb[a]);
+      double n2 = __dmul_rn(cs[0], cs[0]);
+#pragma unroll
+      for (int a = 1; a < D; ++a) n2 = __dadd_rn(n2, __dmul_rn(cs[a], cs[a]));
+      const double nrm = __dsqrt_rn(n2);
+      if (nrm > 1e-8) {
+        int sh2[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          const double sp = __dadd_rn((double)cen[a], __dmul_rn(__ddiv_rn(cs[a], nrm), A.soft_off));
+          const double fl = floor(sp);
+          real o = (real)(sp - fl);
+          sh2[a] = (int)fl;
+          if (o >= (real)1) {
+            o = 0;
+            sh2[a] += 1;
+          }
+          off2[a] = o;
+        }
+        spawned = cell_at<D>(I, Fc[0] + sh2[0], Fc[1] + sh2[1], Fc[2] + sh2[2], &G2);
+        if (!spawned) atomicOr(A.status, ST_OUT_OF_BOX);
+        if (spawned && I.has_obs) {
+          int Gc[3];
+          decode_cell<D>(I, G2, Gc);
+          double o[3] = {0, 0, 0};
+#pragma unroll
+          for (int a = 0; a < D; ++a) o[a] = (double)off2[a];
+          if (inside_sphere<D>(I, Gc, o)) spawned = false;
+        }
+      }
+    }
+    A.occ[A.ncells + F] = spawned ? 1u : 0u;
+    A.fkey[A.ncells + F] = spawned ? G2 : 0xffffffffu;
+#pragma unroll
+    for (int a = 0; a < D; ++a) A.foff2[(int64_t)a * A.ncells + F] = off2[a];
+  }
   if (A.write_trace) {
     A.tcnt[F] = cnt;
     A.mask[F] = mask;
@@ -382,7 +441,9 @@ __global__ void __launch_bounds__(256) k_finalize(const __grid_constant__ Args<Q
     const uint32_t src = A.svals[j];
     A.b.cell[j] = A.skeys[j];
 #pragma unroll
-    for (int a = 0; a < D; ++a) A.b.off[(int64_t)a * A.ccap + j] = A.foff[(int64_t)a * A.ncells + src];
+    for (int a = 0; a < D; ++a)
+      A.b.off[(int64_t)a * A.ccap + j] = src < A.ncells ? A.foff[(int64_t)a * A.ncells + src]
+                                                        : A.foff2[(int64_t)a * A.ncells + (src - A.ncells)];
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *A.b.count = Pn;
 }
@@ -999,6 +1060,9 @@ struct SimImpl : SimBase {
     DBM_TRY(alloc(&A.mask, ncells));
     DBM_TRY(alloc(&A.fkey, ncells));
     DBM_TRY(alloc(&A.foff, (int64_t)D * ncells));
+    A.kappa_soft = 0;
+    A.soft_off = 2.0 * (1.0 - std::sqrt(3.0) / 2.0) * d.dx / d.cell;  // direbm/reference/simulator.py:27
+    A.foff2 = nullptr;
     const int64_t sort_cap = std::max<int64_t>(ncells, mcap);  // set_state sorts up to mcap moments
     DBM_TRY(alloc(&k_in, sort_cap));
     DBM_TRY(alloc(&v_in, sort_cap));
@@ -1151,6 +1215,46 @@ struct SimImpl : SimBase {
   }
   int set_tiling_v(int tx, int persistent) override { return set_tiling(tx, persistent); }
 
+  // Soft-outer spawn (direbm/reference/simulator.py:126-166) for kappa_hard < kappa <= ks; 0 turns
+  // it off.  Up to one extra CP per thinning cell, so the CP capacity must hold 2 ncells.
+  int set_soft_spawn(int ks) override {
+    if (ks < 0) { set_last_error("soft spawn: kappa_soft must be >= 0"); return DBM_ERR_INVALID; }
+    if (ks > 0) {
+      if (ccap < 2 * (int64_t)ncells || 2 * (uint64_t)ncells >= 0xffffffffull) {
+        set_last_error("soft spawn needs a moment capacity of at least 2 x cells (%lld), have %lld",
+                       (long long)(2 * (int64_t)ncells), (long long)ccap);
+        return DBM_ERR_CAPACITY;
+      }
+      if (!spawn_ready) {
+        DBM_CUDA(cudaStreamSynchronize(own));  // no step may still use the single-block buffers
+        uint32_t *occ2 = nullptr, *fkey2 = nullptr;
+        DBM_TRY(alloc(&occ2, 2 * (int64_t)ncells));
+        DBM_TRY(alloc(&fkey2, 2 * (int64_t)ncells));
+        DBM_TRY(alloc(&args.foff2, (int64_t)D * ncells));
+        char* tmp;
+        DBM_TRY(alloc(&tmp, (int64_t)compact_tmp_bytes(2 * (int64_t)ncells)));
+        release(args.occ);
+        release(args.fkey);
+        release(compact_tmp);
+        args.occ = occ2;
+        args.fkey = fkey2;
+        compact_tmp = tmp;
+        spawn_ready = true;
+      }
+    }
+    args.kappa_soft = ks;
+    kappa_soft = ks;
+    invalidate_graphs();  // captured launches hold the flag and the buffers
+    return DBM_OK;
+  }
+  bool spawn_ready = false;
+
+  void release(void* p) {
+    if (!p) return;
+    cudaFree(p);
+    allocs.erase(std::remove(allocs.begin(), allocs.end(), p), allocs.end());
+  }
+
   void invalidate_graphs() override {
     for (auto* set : {graph, graph_tr})
       for (int i = 0; i < 2; ++i)
@@ -1207,6 +1311,10 @@ struct SimImpl : SimBase {
     if (stage_ev) cudaEventRecord(stage_ev[i], s);
   }
 
+  // The tiled 2D kernels serve plain periodic/bounded boxes; obstacles and the soft spawn run on
+  // the untiled window kernels.
+  bool tiled_path() const { return D == 2 && tiled && use_tiles && !args.any_obstacle && args.kappa_soft == 0; }
+
   int launch_step(cudaStream_t s, int upto) {
     bind();
     Args<Q, D, P>& A = args;
@@ -1215,7 +1323,7 @@ struct SimImpl : SimBase {
     k_collide<Q, D, P><<<gm, 256, 0, s>>>(A);
     DBM_LAUNCH_CHECK();
     // the untiled window kernels (3D, obstacles, or tiles off) read packed items
-    const bool untiled = !(D == 2 && tiled && use_tiles && !A.any_obstacle);
+    const bool untiled = !tiled_path();
     if (untiled) {
       k_pack<Q, D, P><<<gm, 256, 0, s>>>(A, A.a, A.mcap, A.a.count);
       DBM_LAUNCH_CHECK();
@@ -1223,7 +1331,7 @@ struct SimImpl : SimBase {
     mark(1, s);
     if (upto <= 1) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled && use_tiles && !A.any_obstacle)
+      if (tiled_path())
         k_thin_refine_t<Q, P><<<use_persistent ? pgrid[0] : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo, ntiles);
       else k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
     } else {
@@ -1232,9 +1340,12 @@ struct SimImpl : SimBase {
     DBM_LAUNCH_CHECK();
     mark(2, s);
     if (upto <= 2) return DBM_OK;
-    DBM_TRY(compact_flags_u32(A.occ, A.fkey, k_in, v_in, ncells, A.d_P, compact_tmp, s));
+    // slots: regular CPs [0, ncells), spawned ones [ncells, 2 ncells); the stable sort keeps that
+    // order among CPs of one cell
+    const int64_t nslots = A.kappa_soft > 0 ? 2 * (int64_t)ncells : (int64_t)ncells;
+    DBM_TRY(compact_flags_u32(A.occ, A.fkey, k_in, v_in, nslots, A.d_P, compact_tmp, s));
     bool alt = false;
-    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, ncells, A.d_P, key_bits, sort_tmp, s, &alt));
+    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, nslots, A.d_P, key_bits, sort_tmp, s, &alt));
     sorted_in_alt = alt;
     A.skeys = alt ? k_alt : k_in;
     A.svals = alt ? v_alt : v_in;
@@ -1251,7 +1362,7 @@ struct SimImpl : SimBase {
     mark(3, s);
     if (upto <= 3) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled && use_tiles && !A.any_obstacle)
+      if (tiled_path())
         k_weights_t<Q, P><<<use_persistent ? pgrid[1] : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo, ntiles);
       else k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
     } else {
@@ -1262,7 +1373,7 @@ struct SimImpl : SimBase {
     if (upto <= 4) return DBM_OK;
     DBM_CUDA(cudaMemsetAsync(A.emask, 0, (size_t)ccap * 4, s));
     if constexpr (D == 2) {
-      if (tiled && use_tiles && !A.any_obstacle)
+      if (tiled_path())
         k_gather_t<Q, P><<<use_persistent ? pgrid[2] : ntiles, 256, sm_gather, s>>>(A, d_tiles, geo, ntiles);
       else k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
     } else {
@@ -1739,6 +1850,8 @@ int dbm_sim_set_option(dbm_sim* s, int32_t option, int32_t value) {
     s->impl->tiling(&tx, &pers);
     if (option == DBM_OPT_TILE_WIDTH) tx = value; else pers = value;
     return s->impl->set_tiling_v(tx, pers);
+  } else if (option == DBM_OPT_KAPPA_SOFT) {
+    return s->impl->set_soft_spawn(value);
   } else {
     set_last_error("dbm_sim_set_option: unknown option %d", option);
     return DBM_ERR_INVALID;

@@ -75,16 +75,21 @@ struct Args {
   int kappa_hard;
   real eps;
   int64_t mcap;    // moment buffer capacity
-  int64_t ccap;    // control-point buffer capacity (= ncells)
+  int64_t ccap;    // control-point buffer capacity (>= ncells; >= 2 ncells with the soft spawn)
   StateP<P> a;     // input moments (collided in place)
   StateP<P> b;     // output moments (= sorted control points)
-  // scratch, per cell
+  // scratch, per cell (occ and fkey have a second block of ncells slots for spawned CPs)
   uint32_t* occ;
   uint32_t* tcnt;
   real* cen;       // [D][ncells]
   uint32_t* mask;
   uint32_t* fkey;
   real* foff;      // [D][ncells]
+  // soft-outer spawn: a CP with kappa_hard < kappa <= kappa_soft adds one CP soft_off cells along
+  // the normalised sum of its components' directions (0: off)
+  int kappa_soft;
+  double soft_off;
+  real* foff2;     // [D][ncells] offsets of the spawned CPs (slot ncells + F)
   // sort (keys_in/vals_in before, skeys/svals = the sorted result)
   uint32_t* skeys;
   uint32_t* svals;
@@ -307,6 +312,8 @@ struct SimBase {
   virtual void invalidate_graphs() = 0;
   virtual int tiling(int* tx, int* persistent) const = 0;
   virtual int set_tiling_v(int tx, int persistent) = 0;
+  virtual int set_soft_spawn(int kappa_soft) = 0;
+  int kappa_soft = 0;  // soft-outer spawn threshold (0: off)
   int use_graphs = 1;
   int use_tiles = 1;
   uint64_t version = 0;  // bumped by every change of the state (load, step, restore)

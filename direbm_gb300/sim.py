@@ -68,6 +68,7 @@ class Simulation:
         moment_capacity: int = 0,
         graphs: bool = True,
         tiles: bool = True,
+        kappa_soft: int = 0,
         device=None,
     ):
         self.device = _require_cuda(device)
@@ -83,6 +84,10 @@ class Simulation:
         self.eps = float(eps)
         self.instances = [inst if isinstance(inst, Instance) else Instance(**inst) for inst in instances]
         D = self.lattice.D
+        self.ncells = int(sum(int(np.prod(inst.dims)) for inst in self.instances))
+        self.kappa_soft = int(kappa_soft)
+        if self.kappa_soft > 0:  # up to one spawned control point per thinning cell
+            moment_capacity = max(int(moment_capacity), 2 * self.ncells)
         desc = _lib.SimDesc(
             lattice=self.lattice.id, precision=_PREC[precision], dx=self.dx, r_res=self.r_res,
             cell=self.cell, kappa_hard=self.kappa_hard, eps=self.eps, moment_capacity=int(moment_capacity),
@@ -98,7 +103,6 @@ class Simulation:
             arr[i].periodic = 1 if inst.periodic else 0
             arr[i].tau = float(inst.tau)
             arr[i].rho_rest = float(inst.rho_rest)
-        self.ncells = int(sum(int(np.prod(inst.dims)) for inst in self.instances))
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.lib.dbm_sim_create(ctypes.byref(desc), arr, len(self.instances), ctypes.byref(h)),
@@ -106,6 +110,8 @@ class Simulation:
         self._h = h
         _lib.check(self.lib.dbm_sim_set_option(self._h, 1, 1 if graphs else 0), "dbm_sim_set_option")
         _lib.check(self.lib.dbm_sim_set_option(self._h, 2, 1 if tiles else 0), "dbm_sim_set_option")
+        if self.kappa_soft > 0:
+            self.set_soft_spawn(self.kappa_soft)
         self.iteration = 0
         for i, inst in enumerate(self.instances):
             if inst.obstacle is not None:
@@ -250,7 +256,7 @@ class Simulation:
         self.instances[inst].inflow = (tuple(v), int(width)) if width > 0 else None
 
     # ---- launch configuration -------------------------------------------------------------------
-    OPT_TILE_WIDTH, OPT_PERSISTENT = 3, 4
+    OPT_TILE_WIDTH, OPT_PERSISTENT, OPT_KAPPA_SOFT = 3, 4, 5
 
     def tiling(self) -> tuple:
         """(tile width in cells, persistent launches) of the 2D tiled kernels."""
@@ -267,6 +273,15 @@ class Simulation:
             if persistent is not None:
                 _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_PERSISTENT, 1 if persistent else 0),
                            "set persistent")
+
+    def set_soft_spawn(self, kappa_soft: int):
+        """Soft-outer spawn (the CPU simulator's soft_mode="spawn", direbm/reference/simulator.py:
+        126-166): control points with kappa_hard < kappa <= kappa_soft also emit one new control
+        point 2(1 - sqrt(3)/2) dx ahead along their components' mean direction.  0 turns it off.
+        Needs moment_capacity >= 2 x cells (the constructor's kappa_soft sets that up)."""
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_KAPPA_SOFT, int(kappa_soft)), "set kappa_soft")
+        self.kappa_soft = int(kappa_soft)
 
     # ---- parameters, checkpoints ----------------------------------------------------------------
     def set_tau(self, tau):

@@ -171,6 +171,14 @@ int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
  * by timing. */
 #define DBM_OPT_TILE_WIDTH 3
 #define DBM_OPT_PERSISTENT 4
+/* DBM_OPT_KAPPA_SOFT: soft-outer spawn threshold (default 0 = off).  Replaces the CPU simulator's
+ * soft_mode="spawn" / kappa_soft (direbm/reference/simulator.py:126-166; the Warp path,
+ * direbm/warp/propagation.py:108, treats soft_outer as inner).  A control point with
+ * kappa_hard < kappa <= value also emits one new control point 2(1 - sqrt(3)/2) dx from its
+ * pre-move position, along the normalised sum of the direction vectors of its components within
+ * r (none when that sum is below 1e-8).  Needs a moment capacity of 2 x cells (DBM_ERR_CAPACITY
+ * otherwise); runs on the untiled kernels; the tape (dbm_tape_*) refuses a simulator with it on. */
+#define DBM_OPT_KAPPA_SOFT 5
 int dbm_sim_set_option(dbm_sim* sim, int32_t option, int32_t value);
 int dbm_sim_get_tiling(dbm_sim* sim, int32_t* tile_width, int32_t* persistent);
 /* Run one step but stop after `stage` (1 collide, 2 thin+refine, 3 sort, 4 weights, 5 gather,

@@ -25,6 +25,12 @@ Step, in order (each line cites the reference function it follows):
   6. per CP and direction: f = sum over components within r of (r - d)*(1/sw) * f (propagation.py:179-186)
   7. gap fill: directions with f < eps get (r / sum_{CPs within r, also empty}(r - d)) * f_rest;
      emptiness is judged on the pre-fill values; emit one moment per CP      (propagation.py:189-218)
+Optional soft-outer spawn (kappa_soft > 0; the reference CPU simulator's rule,
+direbm/reference/simulator.py:126-166, which its Warp path omits): a CP with kappa_hard < kappa <=
+kappa_soft also emits one new CP at p + n * 2(1 - sqrt(3)/2) dx, with p the CP's position before
+its move and n the normalised sum of the direction vectors c of the components within r; no spawn
+when |sum| <= 1e-8.  New CPs are not refined; they join the CP set before stage 4 (after the
+regular CPs of the same cell).
 
 The radius test uses one canonical operation order (each step rounded, no fused multiply-add),
 with dS the integer cell difference (component cell - reference cell), cd = c*dx/cell and p the
@@ -75,6 +81,7 @@ class GridSpec:
     instances: list
     eps: float = 1e-6
     dtype: type = np.float64  # working precision of the decision arithmetic
+    kappa_soft: int = 0  # soft-outer spawn for kappa_hard < kappa <= kappa_soft (0: off)
     base: np.ndarray = field(init=False)
     ncells: int = field(init=False)
 
@@ -103,6 +110,11 @@ class GridSpec:
     @property
     def R(self):
         return self.dtype(self.r_res / self.cell)
+
+    @property
+    def soft_offset(self):
+        """Spawn distance in cell units: 2(1 - sqrt(3)/2) dx (direbm/reference/simulator.py:27), FP64."""
+        return 2.0 * (1.0 - np.sqrt(3.0) / 2.0) * float(self.dx) / float(self.cell)
 
     def dims_arr(self):
         return np.array([inst.dims for inst in self.instances], dtype=np.int64)
@@ -407,6 +419,71 @@ def refine(spec: GridSpec, st: GridState, fstar, cells, cen):
     return mask, kappa, G, off
 
 
+def direction_sum(n, C):
+    """Sum of direction vectors from per-direction counts n (P, Q): acc = acc + n_k * c_k for
+    k = 0..Q-1, FP64, one rounding per operation."""
+    acc = np.zeros((n.shape[0], C.shape[1]))
+    for q in range(C.shape[0]):
+        acc = acc + n[:, q:q + 1].astype(np.float64) * C[q][None, :]
+    return acc
+
+
+def spawn_point(p, acc, offset):
+    """p + (acc / |acc|) * offset and whether |acc| > 1e-8 (direbm/reference/simulator.py:153-166:
+    c_sum, norm, normal, p.x + normal * _SOFT_OFFSET * dx), FP64, |acc| = sqrt(sum_a acc_a^2)."""
+    nrm2 = acc[:, 0] * acc[:, 0]
+    for a in range(1, acc.shape[1]):
+        nrm2 = nrm2 + acc[:, a] * acc[:, a]
+    nrm = np.sqrt(nrm2)
+    go = nrm > 1e-8
+    safe = np.where(go, nrm, 1.0)
+    return p + (acc / safe[:, None]) * offset, go
+
+
+def soft_spawn(spec: GridSpec, st: GridState, cells, cen, kappa):
+    """Soft-outer spawn (direbm/reference/simulator.py:126-166).  Returns (global cell, offset) of the
+    spawned CP per thinning CP (cell -1: none, or outside a bounded box).
+
+    The direction sum follows the kernel's order, in FP64: the regular components as per-direction
+    counts, acc = acc + n_k * c_k for k = 0..Q-1; the bounced ones (label opp(k)) one by one in
+    window / moment / slot order into a second sum; then sum = acc + bounced.  The new point is
+    cen + (sum / |sum|) * offset, |sum| = sqrt(sum_a sum_a^2), every operation rounded in FP64,
+    split into cell + offset and the offset rounded to the working precision."""
+    P = len(cells)
+    G2 = np.full(P, -1, dtype=np.int64)
+    off2 = np.zeros((P, spec.D), dtype=spec.dtype)
+    soft = (kappa > spec.kappa_hard) & (kappa <= spec.kappa_soft)
+    if spec.kappa_soft <= 0 or not soft.any():
+        return G2, off2
+    comps = components(spec, st)
+    m, k, b, S, t, lab, blk, _ = comps
+    ci, pj, d, e, dS = _pairs_comp_cp(spec, st, cells, cen, comps)
+    C = np.asarray(spec.lattice.C, dtype=np.float64)
+    reg = ~blk[ci]
+    n = np.zeros((P, spec.Q), dtype=np.int64)
+    np.add.at(n, (pj[reg], k[ci[reg]]), 1)
+    acc = direction_sum(n, C)
+    bc = ~reg
+    if bc.any():
+        keys = _so_keys(dS[bc], spec.D) + [m[ci[bc]], k[ci[bc]]]
+        acc = acc + ordered_sums(pj[bc], keys, C[lab[ci[bc]]], P)
+    sp, go = spawn_point(cen.astype(np.float64), acc, spec.soft_offset)
+    go &= soft
+    if not go.any():
+        return G2, off2
+    sp = sp[go]
+    shift = np.floor(sp)
+    o = (sp - shift).astype(spec.dtype)
+    shift = shift.astype(np.int64)
+    over = o >= spec.dtype(1.0)
+    o[over] = 0
+    shift[over] += 1
+    bcp, F = decode(spec, cells[go])
+    G2[go] = encode(spec, bcp, F + shift)
+    off2[go] = o
+    return G2, off2
+
+
 def sort_cps(G):
     """Stage 4: stable ascending sort by final cell (ties keep thinning order)."""
     return np.argsort(G, kind="stable")
@@ -482,6 +559,10 @@ def step(spec: GridSpec, st: GridState, trace: dict | None = None) -> GridState:
     fstar = collide_state(spec, st)
     cells, cnt, cen, comp_cell = thin(spec, st)
     mask, kappa, G, off = refine(spec, st, fstar, cells, cen)
+    if spec.kappa_soft > 0:  # spawned CPs follow the regular ones (slot order of the kernels)
+        G2, off2 = soft_spawn(spec, st, cells, cen, kappa)
+        G = np.concatenate([G, G2])
+        off = np.concatenate([off, off2])
     keep = G >= 0
     if keep.any() and any(inst.obstacle is not None for inst in spec.instances):
         bq, Fq = decode(spec, np.where(keep, G, 0))

@@ -139,6 +139,27 @@ def main(ref_root: str) -> None:
     fv = np.stack([m.f for m in sim.moments])
     rv, _, _ = bin_fields(xv, fv, -3, 3, h=1.0)
     np.savez_compressed(HERE / "simulator.npz", pos0=pos, f0=fs, x3=xv, f3=fv, rho3=rv)
+
+    # -- soft-outer spawn point (direbm/reference/simulator.py:153-166) on seeded sets of nearby
+    #    component directions, plus the balanced sets that spawn nothing --------------------------
+    from direbm.reference.types import Component, ControlPoint
+
+    sim = Simulator([], tau=0.6)  # D2Q7, soft_mode="spawn", dx = 1
+    rng = np.random.default_rng(7)
+    sets = [list(rng.integers(0, 7, size=int(rng.integers(1, 40)))) for _ in range(64)]
+    sets += [[1, 2, 3, 4, 5, 6], [0, 0, 0], [1, 4], [2, 5, 0], [1], [6, 6, 6, 1]]
+    L = max(len(x) for x in sets)
+    labels = np.full((len(sets), L), -1, dtype=np.int64)
+    p = rng.uniform(-5.0, 5.0, size=(len(sets), 2))
+    spawn = np.full((len(sets), 2), np.nan)
+    for j, lab in enumerate(sets):
+        labels[j, : len(lab)] = lab
+        cp = ControlPoint(x=p[j].copy(), f=np.zeros(7))
+        cp.nu_near = [Component(f=0.0, i=int(i), x=np.zeros(2)) for i in lab]
+        r = sim._soft_new_point(cp)
+        if r is not None:
+            spawn[j] = r
+    np.savez_compressed(HERE / "soft_spawn.npz", labels=labels, p=p, spawn=spawn)
     print("golden vectors written to", HERE)
 
 

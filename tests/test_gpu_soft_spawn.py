@@ -1,0 +1,139 @@
+"""Soft-outer spawn on the GPU (DBM_OPT_KAPPA_SOFT) against the oracle (oracle/grid_step.py,
+GridSpec.kappa_soft): the same spawned control points and FP64 values to 1e-12 on a jittered patch,
+with and without an obstacle in the way; the purpose of the rule (tests/test_reference.py:68-85: a point pulse's
+front is more isotropic with the spawn); switching it on and off between captured steps; and the
+refusals (capacity, the tape)."""
+
+import numpy as np
+import pytest
+
+from _cases import oracle_spec
+from oracle import grid_step
+from oracle.lattices import D2Q7
+from oracle.physics import equilibrium
+from test_oracle_soft_spawn import front_anisotropy
+
+pytestmark = pytest.mark.gpu
+
+# reference-form parameters: r = dx = 1, thinning cell dx / alpha = 0.25, kappa_hard 4, kappa_soft 5.
+# With r = dx a component one dispersion step from an unmoved control point sits at d = r exactly, so
+# the inclusive radius test is a tie that one ulp of exp() (the refine weights, CUDA vs numpy) can
+# tip either way; the bit-level comparisons therefore use r = 1.02 dx (every pair >= 1e-6 cells
+# away from the radius), the anisotropy check the reference form.
+N = 96
+INST = dict(dims=(N, N), origin=(-N // 2, -N // 2), periodic=True, tau=0.6)
+R_PARITY = 1.02
+
+
+def _pulse(rho=1.6):
+    return np.zeros((1, 2)), equilibrium(np.array([rho]), np.zeros((1, 2)), D2Q7)
+
+
+def _blob(seed=3, rho=1.3):
+    """19 moments on a jittered hexagonal patch off the cell corners: the pulse's lattice symmetry
+    puts points exactly on cell edges, where one ulp of exp() in the refine weights picks the
+    neighbouring cell; this patch keeps every offset well inside its cell."""
+    rng = np.random.default_rng(seed)
+    p0 = np.array([0.0123, 0.0371])
+    C = np.asarray(D2Q7.C)
+    pts = [p0] + [p0 + C[k] * s for k in range(1, 7) for s in (1, 2)] + [p0 + C[k] + C[k % 6 + 1] for k in range(1, 7)]
+    x = np.array(pts) + rng.uniform(-0.05, 0.05, size=(len(pts), 2))
+    return x, equilibrium(np.full(len(x), rho), np.zeros((len(x), 2)), D2Q7)
+
+
+def _sim(precision, ks=5, inst=INST, graphs=True, cap=0, r_res=1.0):
+    from direbm_gb300.sim import Instance, Simulation
+
+    return Simulation([Instance(**inst)], lattice="D2Q7", precision=precision, dx=1.0, r_res=r_res, cell=0.25,
+                      kappa_hard=4, kappa_soft=ks, graphs=graphs, moment_capacity=cap)
+
+
+def _spec(inst=INST, ks=5, r_res=R_PARITY):
+    spec = oracle_spec("D2Q7", [inst], 1.0, r_res, 0.25)
+    spec.kappa_soft = ks
+    return spec
+
+
+CASES = {
+    "blob": (INST, 4),
+    "blob_disc": (dict(INST, obstacle=((2.3, 0.6), 0.8)), 4),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_soft_spawn_matches_oracle_fp64(name):
+    inst, steps = CASES[name]
+    x, f = _blob()
+    spec = _spec(inst)
+    st = grid_step.from_world(spec, np.zeros(len(x), np.int64), x, f)
+    sim = _sim("fp64", inst=inst, r_res=R_PARITY)
+    sim.set_state(None, x, f)
+    for s in range(steps):
+        st = grid_step.step(spec, st)
+        sim.step(1)
+        sim.check_status()
+        _, xg, fg = sim.state_numpy()
+        _, xo, fo = grid_step.to_world(spec, st)
+        assert len(xg) == len(xo), (s, len(xg), len(xo))
+        np.testing.assert_allclose(xg, xo, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(fg, fo, rtol=0, atol=1e-12 * np.abs(fo).max())
+    off = _spec(inst, ks=0)
+    st0 = grid_step.from_world(off, np.zeros(len(x), np.int64), x, f)
+    for _ in range(steps):
+        st0 = grid_step.step(off, st0)
+    assert len(st.cell) > len(st0.cell)  # the spawn did add control points
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_soft_spawn_reduces_front_anisotropy(precision):
+    x, f = _pulse()
+    out = {}
+    for ks in (0, 5):
+        sim = _sim(precision, ks=ks, cap=2 * N * N)
+        sim.set_state(None, x, f)
+        sim.step(10)
+        sim.check_status()
+        _, xg, _ = sim.state_numpy()
+        out[ks] = (len(xg), front_anisotropy(xg))
+    assert out[5][0] > out[0][0]
+    assert out[5][1] < 0.5 * out[0][1], out
+
+
+def test_soft_spawn_toggle_between_captured_steps():
+    x, f = _blob()
+    res = []
+    for graphs in (True, False):
+        sim = _sim("fp64", graphs=graphs, r_res=R_PARITY)
+        sim.set_state(None, x, f)
+        sim.step(2)
+        sim.set_soft_spawn(0)
+        sim.step(1)
+        sim.set_soft_spawn(5)
+        sim.step(1)
+        res.append(sim.state_numpy())
+    spec = _spec()
+    st = grid_step.from_world(spec, np.zeros(len(x), np.int64), x, f)
+    for ks in (5, 5, 0, 5):
+        spec.kappa_soft = ks
+        st = grid_step.step(spec, st)
+    _, xo, fo = grid_step.to_world(spec, st)
+    for _, xg, fg in res:
+        assert len(xg) == len(xo)
+        np.testing.assert_allclose(xg, xo, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(fg, fo, rtol=0, atol=1e-12 * np.abs(fo).max())
+    assert np.array_equal(res[0][1], res[1][1]) and np.array_equal(res[0][2], res[1][2])
+
+
+def test_soft_spawn_refusals():
+    from direbm_gb300._lib import DbmError
+    from direbm_gb300.adjoint import Tape
+
+    sim = _sim("fp64", ks=0)  # capacity = cells: no room for spawned points
+    with pytest.raises(DbmError, match="capacity"):
+        sim.set_soft_spawn(5)
+    sim = _sim("fp64")
+    x, f = _pulse()
+    sim.set_state(None, x, f)
+    tape = Tape(sim)
+    with pytest.raises(DbmError, match="soft-outer"):
+        tape.step()
