@@ -162,6 +162,16 @@ __device__ __forceinline__ PairRec<real, D> make_rec(uint32_t row, uint32_t item
 
 // ---- recording kernels (read the step's buffers through Args, see StepHook) --------------------
 
+// Gather up to 8 device words into mapped pinned host memory: one launch instead of one small
+// device-to-host copy per word at every recorded step's synchronisation.
+struct FetchSrc {
+  const uint32_t* p[8];
+};
+__global__ void k_fetch_words(FetchSrc src, int n, uint32_t* __restrict__ dst) {
+  const int i = threadIdx.x;
+  if (i < n) dst[i] = *src.p[i];
+}
+
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_rec_thin_cell(const __grid_constant__ Args<Q, D, P> A, int64_t M,
                                                        uint32_t* __restrict__ thin_cell) {
@@ -440,38 +450,67 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t cnt, uint32_t* counter
   return base + incl - cnt;
 }
 
-// One pass per list: each row counts its pairs, reserves their slots and writes them (a second,
-// cache-warm enumeration).  A list whose capacity is too small writes nothing past it; the counter
-// then holds the size needed and the host runs the kernel again.
+// One pass per list.  Each row enumerates its pairs once: it counts them all and stages the first
+// kListStage records in shared memory (record i of thread t at i * blockDim + t, so a warp's
+// accesses are conflict-free).  Then the row reserves its slots and copies the staged records out.
+// Only a row with more pairs than that enumerates a second time, writing straight to the list.
+// Within a row the order is the enumeration order either way.  A list whose capacity is too small
+// writes nothing past it; the counter then holds the size needed and the host runs the kernel again.
 enum ListKind { kRefineCP = 0, kRefineComp = 1, kResCP = 2, kResComp = 3, kGapCP = 4, kGapNb = 5 };
+constexpr int kListStage = 12;
+
+template <class real, int D, int KIND>
+constexpr size_t list_smem_bytes(int threads) {
+  return (size_t)kListStage * threads * (sizeof(PairRec<real, D>) + (KIND == kGapCP ? 4 : 0));
+}
 
 template <int Q, int D, class P, int KIND>
 __global__ void __launch_bounds__(256) k_list(const __grid_constant__ Args<Q, D, P> A,
                                               const __grid_constant__ StepRec<typename P::real, D> r,
                                               const uint32_t* __restrict__ cp_of_cell, uint32_t* __restrict__ counter) {
   using real = typename P::real;
+  using Rec = PairRec<real, D>;
+  extern __shared__ __align__(16) unsigned char list_smem[];
+  Rec* s_rec = reinterpret_cast<Rec*>(list_smem);
+  uint32_t* s_bits = reinterpret_cast<uint32_t*>(s_rec + (size_t)kListStage * blockDim.x);  // kGapCP only
   const auto& Lst = KIND == kRefineCP ? r.ref.f : KIND == kRefineComp ? r.ref.t : KIND == kResCP ? r.res.f
                   : KIND == kResComp ? r.res.t : KIND == kGapCP ? r.gap.f : r.gap.t;
   const int64_t rows = Lst.rows;
+  const int tid = threadIdx.x, nt = blockDim.x;
   for (int64_t t0 = blockIdx.x * (int64_t)blockDim.x; t0 < rows; t0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = t0 + threadIdx.x;
+    const int64_t row = t0 + tid;
     const bool act = row < rows;
-    const auto nop2 = [](uint32_t, const real(&)[3]) {};
-    const auto nop3 = [](uint32_t, uint32_t, const real(&)[3]) {};
     uint32_t cnt = 0;
     int64_t j = 0, m = 0;
     int k = 0;
+    uint32_t i_comp = 0;
+    // stage: count every pair, keep the first kListStage
+    const auto stage2 = [&](uint32_t row_id, uint32_t item, const real(&e)[3]) {
+      if (cnt < (uint32_t)kListStage) s_rec[(size_t)cnt * nt + tid] = make_rec<D, real>(row_id, item, e);
+      ++cnt;
+    };
     if (act) {
       if constexpr (KIND == kRefineCP || KIND == kResCP) {
         j = row / Q;
         k = (int)(row - j * Q);
-        cnt = KIND == kRefineCP ? enum_refine_cp<Q, D, P>(A, r, j, k, nop2) : enum_resample_cp<Q, D, P>(A, j, k, nop2);
+        const auto put = [&](uint32_t item, const real(&e)[3]) { stage2((uint32_t)j, item, e); };
+        if constexpr (KIND == kRefineCP) enum_refine_cp<Q, D, P>(A, r, j, k, put);
+        else enum_resample_cp<Q, D, P>(A, j, k, put);
       } else if constexpr (KIND == kRefineComp || KIND == kResComp) {
         k = (int)(row / r.M);
         m = row - (int64_t)k * r.M;
-        cnt = enum_comp<Q, D, P, KIND == kRefineComp>(A, r, cp_of_cell, (uint32_t)m, k, nop2);
+        i_comp = (uint32_t)m * (uint32_t)Q + (uint32_t)k;
+        const auto put = [&](uint32_t cp, const real(&e)[3]) { stage2(cp, i_comp, e); };
+        enum_comp<Q, D, P, KIND == kRefineComp>(A, r, cp_of_cell, (uint32_t)m, k, put);
+      } else if constexpr (KIND == kGapCP) {
+        const auto put = [&](uint32_t l, uint32_t both, const real(&e)[3]) {
+          if (cnt < (uint32_t)kListStage) s_bits[(size_t)cnt * nt + tid] = both;
+          stage2((uint32_t)row, l, e);
+        };
+        enum_gap<Q, D, P, false>(A, row, put);
       } else {
-        cnt = enum_gap<Q, D, P, KIND == kGapNb>(A, row, nop3);
+        const auto put = [&](uint32_t jj, uint32_t both, const real(&e)[3]) { stage2(jj, both, e); };
+        enum_gap<Q, D, P, true>(A, row, put);
       }
     }
     const uint32_t pos = warp_reserve(cnt, counter);
@@ -479,14 +518,20 @@ __global__ void __launch_bounds__(256) k_list(const __grid_constant__ Args<Q, D,
     Lst.start[row] = pos;
     Lst.cnt[row] = cnt;
     if (!cnt || (int64_t)pos + cnt > Lst.cap) continue;
-    uint32_t w = pos;
+    if (cnt <= (uint32_t)kListStage) {
+      for (uint32_t q = 0; q < cnt; ++q) {
+        Lst.rec[pos + q] = s_rec[(size_t)q * nt + tid];
+        if constexpr (KIND == kGapCP) Lst.bits[pos + q] = s_bits[(size_t)q * nt + tid];
+      }
+      continue;
+    }
+    uint32_t w = pos;  // a long row: enumerate again, writing straight to the list
     if constexpr (KIND == kRefineCP || KIND == kResCP) {
       const auto put = [&](uint32_t item, const real(&e)[3]) { Lst.rec[w++] = make_rec<D, real>((uint32_t)j, item, e); };
       if constexpr (KIND == kRefineCP) enum_refine_cp<Q, D, P>(A, r, j, k, put);
       else enum_resample_cp<Q, D, P>(A, j, k, put);
     } else if constexpr (KIND == kRefineComp || KIND == kResComp) {
-      const uint32_t i = (uint32_t)m * (uint32_t)Q + (uint32_t)k;
-      const auto put = [&](uint32_t cp, const real(&e)[3]) { Lst.rec[w++] = make_rec<D, real>(cp, i, e); };
+      const auto put = [&](uint32_t cp, const real(&e)[3]) { Lst.rec[w++] = make_rec<D, real>(cp, i_comp, e); };
       enum_comp<Q, D, P, KIND == kRefineComp>(A, r, cp_of_cell, (uint32_t)m, k, put);
     } else if constexpr (KIND == kGapCP) {
       const auto put = [&](uint32_t l, uint32_t both, const real(&e)[3]) {
@@ -960,7 +1005,8 @@ struct TapeImpl : TapeBase, StepHook {
   real R = 0;
   int64_t ncells = 0;
   double* wk = nullptr;        // W_k in FP64 (export of FP32DEV f)
-  uint32_t* hbuf = nullptr;    // pinned host words read back while recording
+  uint32_t* hbuf = nullptr;    // mapped pinned host words read back while recording
+  uint32_t* hbuf_dev = nullptr;  // the same words as seen from the device
   uint32_t* d_count = nullptr; // slot counters of the six lists
   double per_row[6] = {16, 16, 16, 16, 4, 4};  // capacity estimate: pairs per row, grown as seen
   uint64_t known_version = ~0ull - 1;  // simulator state version right after this tape's last step
@@ -987,7 +1033,8 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-    DBM_CUDA(cudaMallocHost(&hbuf, 64));
+    DBM_CUDA(cudaHostAlloc(&hbuf, 64, cudaHostAllocMapped));
+    DBM_CUDA(cudaHostGetDevicePointer(&hbuf_dev, hbuf, 0));
     DBM_CUDA(cudaMalloc(&d_count, 6 * 4));
     DBM_TRY(rec_mem.get(&wk, Q));
     return DBM_OK;
@@ -1030,7 +1077,10 @@ struct TapeImpl : TapeBase, StepHook {
 
   // Copy n device words into hbuf[0..n) and wait for them.
   int fetch(const uint32_t* const* src, int n, cudaStream_t s) {
-    for (int i = 0; i < n; ++i) DBM_CUDA(cudaMemcpyAsync(hbuf + i, src[i], 4, cudaMemcpyDeviceToHost, s));
+    FetchSrc fs{};
+    for (int i = 0; i < n && i < 8; ++i) fs.p[i] = src[i];
+    k_fetch_words<<<1, 32, 0, s>>>(fs, n < 8 ? n : 8, hbuf_dev);
+    DBM_LAUNCH_CHECK();
     DBM_CUDA(cudaStreamSynchronize(s));
     return DBM_OK;
   }
@@ -1109,13 +1159,26 @@ struct TapeImpl : TapeBase, StepHook {
     if (Lst.rows == 0) return DBM_OK;
     const unsigned g = grid_for(Lst.rows);
     switch (kind) {
-      case kRefineCP: k_list<Q, D, P, kRefineCP><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
-      case kRefineComp: k_list<Q, D, P, kRefineComp><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
-      case kResCP: k_list<Q, D, P, kResCP><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
-      case kResComp: k_list<Q, D, P, kResComp><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
-      case kGapCP: k_list<Q, D, P, kGapCP><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
-      default: k_list<Q, D, P, kGapNb><<<g, 256, 0, s>>>(A, r, cp_of_cell, d_count + kind); break;
+      case kRefineCP: return launch_list_k<kRefineCP>(A, r, cp_of_cell, g, s);
+      case kRefineComp: return launch_list_k<kRefineComp>(A, r, cp_of_cell, g, s);
+      case kResCP: return launch_list_k<kResCP>(A, r, cp_of_cell, g, s);
+      case kResComp: return launch_list_k<kResComp>(A, r, cp_of_cell, g, s);
+      case kGapCP: return launch_list_k<kGapCP>(A, r, cp_of_cell, g, s);
+      default: return launch_list_k<kGapNb>(A, r, cp_of_cell, g, s);
     }
+  }
+
+  bool list_attr_set[6] = {false, false, false, false, false, false};
+  template <int KIND>
+  int launch_list_k(const Args<Q, D, P>& A, const StepRec<real, D>& r, const uint32_t* cp_of_cell, unsigned g,
+                    cudaStream_t s) {
+    const size_t sm = list_smem_bytes<real, D, KIND>(256);
+    if (!list_attr_set[KIND]) {
+      DBM_CUDA(cudaFuncSetAttribute((const void*)k_list<Q, D, P, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sm));
+      list_attr_set[KIND] = true;
+    }
+    k_list<Q, D, P, KIND><<<g, 256, sm, s>>>(A, r, cp_of_cell, d_count + KIND);
     DBM_LAUNCH_CHECK();
     return DBM_OK;
   }
