@@ -433,6 +433,14 @@ __global__ void __launch_bounds__(256) k_pack(const __grid_constant__ Args<Q, D,
   }
 }
 
+// Copy one device word to a mapped host word (and optionally clear it).
+__global__ void k_read_word(uint32_t* __restrict__ src, int clear, uint32_t* __restrict__ dst) {
+  if (threadIdx.x == 0) {
+    *dst = *src;
+    if (clear) *src = 0u;
+  }
+}
+
 // Sorted pairs -> next state's cells and offsets.
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_finalize(const __grid_constant__ Args<Q, D, P> A) {
@@ -953,7 +961,25 @@ struct SimImpl : SimBase {
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
     if (own) cudaStreamDestroy(own);
+    if (hword) cudaFreeHost(hword);
     for (void* p : allocs) cudaFree(p);
+  }
+
+  // Host-visible words for status and count reads: a one-thread kernel writes them into mapped
+  // pinned memory.  A 4-byte device-to-host copy would queue on the copy engine behind a caller's
+  // bulk copies in flight (a pipelined load/export), stalling the read by milliseconds.
+  uint32_t* hword = nullptr;
+  uint32_t* hword_dev = nullptr;
+  int read_word(uint32_t* src, int clear, int slot, cudaStream_t s, uint32_t* out) {
+    if (!hword) {
+      DBM_CUDA(cudaHostAlloc(&hword, 16, cudaHostAllocMapped));
+      DBM_CUDA(cudaHostGetDevicePointer(&hword_dev, hword, 0));
+    }
+    k_read_word<<<1, 32, 0, s>>>(src, clear, hword_dev + slot);
+    DBM_LAUNCH_CHECK();
+    DBM_CUDA(cudaStreamSynchronize(s));
+    *out = ((volatile uint32_t*)hword)[slot];
+    return DBM_OK;
   }
 
   template <class T>
@@ -1272,8 +1298,10 @@ struct SimImpl : SimBase {
 
   int import_sorted_states(int64_t m, cudaStream_t s, const int32_t* inst_of, const double* pos, const double* fin) {
     bind();
-    real* toff;
-    DBM_TRY(alloc(&toff, (int64_t)D * std::max<int64_t>(m, 1)));  // freed with the handle (rare call)
+    // the unsorted offsets [D][m] live in the weight scratch sw ([Q][mcap], Q > D, idle outside a
+    // step): an allocation here (and its cudaFree) would wait for every stream of the device,
+    // including a caller's copies that overlap the load
+    real* toff = args.sw;
     const unsigned grid = std::min<unsigned>(div_up(std::max<int64_t>(m, 1), 256), (unsigned)sm_count() * 8);
     k_import_keys<Q, D, P><<<grid, 256, 0, s>>>(args, inst_of, pos, m, desc.cell, k_in, v_in, toff);
     DBM_LAUNCH_CHECK();
@@ -1289,11 +1317,6 @@ struct SimImpl : SimBase {
     k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, s>>>(
         ks, args.d_P, ncells, args.a.start);
     DBM_LAUNCH_CHECK();
-    // release the temporary offsets right away
-    DBM_CUDA(cudaStreamSynchronize(s));
-    cudaFree(toff);
-    allocs.pop_back();
-    bytes -= (int64_t)((size_t)D * std::max<int64_t>(m, 1) * sizeof(real));
     return DBM_OK;
   }
 
@@ -1657,8 +1680,7 @@ struct SimImpl : SimBase {
 
   int count(int64_t* m, cudaStream_t s) override {
     uint32_t h = 0;
-    DBM_CUDA(cudaMemcpyAsync(&h, st[cur].count, 4, cudaMemcpyDeviceToHost, s));
-    DBM_CUDA(cudaStreamSynchronize(s));
+    DBM_TRY(read_word(st[cur].count, 0, 1, s, &h));
     *m = h;
     return DBM_OK;
   }
@@ -1673,9 +1695,7 @@ struct SimImpl : SimBase {
 
   int status(uint32_t* flags, int clear, cudaStream_t s) override {
     uint32_t h = 0;
-    DBM_CUDA(cudaMemcpyAsync(&h, args.status, 4, cudaMemcpyDeviceToHost, s));
-    if (clear) DBM_CUDA(cudaMemsetAsync(args.status, 0, 4, s));
-    DBM_CUDA(cudaStreamSynchronize(s));
+    DBM_TRY(read_word(args.status, clear, 0, s, &h));
     *flags = h;
     return DBM_OK;
   }

@@ -186,13 +186,27 @@ class Simulation:
             _lib.check(self.lib.dbm_sim_count(self._h, ctypes.byref(m), _stream()), "dbm_sim_count")
         return int(m.value)
 
-    def state(self):
-        """(instance (M,) int32, positions (M, D) fp64, f (M, Q) fp64) as CUDA tensors."""
+    def state(self, out=None):
+        """(instance (M,) int32, positions (M, D) fp64, f (M, Q) fp64) as CUDA tensors.  With
+        ``out`` = (inst, pos, f), contiguous CUDA tensors of at least M rows, the state is written
+        into their first M rows and those views are returned (no allocation)."""
         M = self.count()
         dev = self.device
-        inst = torch.empty(M, dtype=torch.int32, device=dev)
-        pos = torch.empty((M, self.lattice.D), dtype=torch.float64, device=dev)
-        f = torch.empty((M, self.lattice.Q), dtype=torch.float64, device=dev)
+        D, Q = self.lattice.D, self.lattice.Q
+        if out is not None:
+            oi, op, of = out
+            ok = (oi.is_cuda and op.is_cuda and of.is_cuda and oi.dtype == torch.int32 and op.dtype == torch.float64
+                  and of.dtype == torch.float64 and oi.is_contiguous() and op.is_contiguous() and of.is_contiguous()
+                  and oi.shape[0] >= M and op.shape[0] >= M and of.shape[0] >= M and tuple(op.shape[1:]) == (D,)
+                  and tuple(of.shape[1:]) == (Q,))
+            if not ok:
+                raise ValueError(f"state(out=...): need contiguous CUDA int32 (>= {M},), fp64 (>= {M}, {D}), "
+                                 f"fp64 (>= {M}, {Q})")
+            inst, pos, f = oi[:M], op[:M], of[:M]
+        else:
+            inst = torch.empty(M, dtype=torch.int32, device=dev)
+            pos = torch.empty((M, D), dtype=torch.float64, device=dev)
+            f = torch.empty((M, Q), dtype=torch.float64, device=dev)
         if M:
             with torch.cuda.device(dev):
                 _lib.check(self.lib.dbm_sim_get_state(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), _stream()),
