@@ -72,6 +72,13 @@ __device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, 
 __device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float rn_sqrt(float a) { return __fsqrt_rn(a); }
+// Square root for bounds only (PTX sqrt.approx.f32, one instruction, relative error near 2^-23);
+// callers inflate the result far beyond that error.
+__device__ __forceinline__ float bound_sqrt(float a) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
 
 template <class T>
 __device__ __forceinline__ int ifloor(T x) { return (int)floor(x); }

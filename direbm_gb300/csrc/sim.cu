@@ -537,11 +537,20 @@ __global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q,
     }
   real sw;
   if constexpr (std::is_same<P, PF64>::value) sw = swd; else sw = sws.value();
-  A.sw[(int64_t)k * A.mcap + m] = sw > (real)0 ? (real)1 / sw : (real)0;  // stored inverted
+  const real inv = sw > (real)0 ? (real)1 / sw : (real)0;  // stored inverted
+  const int64_t i = (int64_t)k * A.mcap + m;
+  A.sw[i] = inv;
+  if constexpr (std::is_same<P, PF64>::value) A.kv[i] = KV<real>{inv, A.a.f64[i]};
+  else A.kv[i] = KV<real>{inv, A.a.dev[i]};
 }
 
+// FP32: six resident blocks per SM (the gather waits on loads and needs the warps); FP64 keeps its
+// registers (forcing the same bound spills the double accumulators).
+template <class P>
+constexpr int gather_min_blocks() { return std::is_same<P, PF64>::value ? 1 : 6; }
+
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, D, P> A) {
+__global__ void __launch_bounds__(256, gather_min_blocks<P>()) k_gather(const __grid_constant__ Args<Q, D, P> A) {
   using real = typename P::real;
   const uint32_t Pn = *A.d_P;
   const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -596,14 +605,14 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
           real e[3];
           const real d2 = canon_d2<D, real>(o, c, e);
           if (d2 <= A.R2) {
-            const real inv = A.sw[(int64_t)k * A.mcap + m];
-            if (inv > (real)0) {
-              const real wgt = (A.R - rn_sqrt(d2)) * inv;
+            const KV<real> kv = A.kv[(int64_t)k * A.mcap + m];
+            if (kv.inv > (real)0) {
+              const real wgt = (A.R - rn_sqrt(d2)) * kv.inv;
               if constexpr (std::is_same<P, PF64>::value) {
-                acc += wgt * A.a.f64[(int64_t)k * A.mcap + m];
+                acc += wgt * kv.f;
               } else {
                 sa.add_prod(wgt, A.a.rho[m]);
-                sb = __fmaf_rn(wgt, A.a.dev[(int64_t)k * A.mcap + m], sb);
+                sb = __fmaf_rn(wgt, kv.f, sb);
               }
             }
           }
@@ -639,14 +648,14 @@ __global__ void __launch_bounds__(256) k_gather(const __grid_constant__ Args<Q, 
             for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + m];
             const real d2 = canon_d2<D, real>(o, c, e);
             if (d2 > A.R2) continue;
-            const real inv = A.sw[(int64_t)kb * A.mcap + m];
-            if (inv > (real)0) {
-              const real wgt = (A.R - rn_sqrt(d2)) * inv;
+            const KV<real> kv = A.kv[(int64_t)kb * A.mcap + m];
+            if (kv.inv > (real)0) {
+              const real wgt = (A.R - rn_sqrt(d2)) * kv.inv;
               if constexpr (std::is_same<P, PF64>::value) {
-                acc += wgt * A.a.f64[(int64_t)kb * A.mcap + m];
+                acc += wgt * kv.f;
               } else {
                 sa.add_prod(wgt, A.a.rho[m]);
-                sb = __fmaf_rn(wgt, A.a.dev[(int64_t)kb * A.mcap + m], sb);
+                sb = __fmaf_rn(wgt, kv.f, sb);
               }
             }
           }
@@ -1100,6 +1109,7 @@ struct SimImpl : SimBase {
     DBM_TRY(alloc(&tmp, (int64_t)compact_tmp_bytes(ncells)));
     compact_tmp = tmp;
     DBM_TRY(alloc(&A.sw, (int64_t)Q * mcap));
+    DBM_TRY(alloc(&A.kv, (int64_t)Q * mcap));
     if constexpr (std::is_same<P, PF64>::value) {
       DBM_TRY(alloc(&A.cpf64, (int64_t)Q * ccap));
     } else {

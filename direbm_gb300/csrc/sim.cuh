@@ -61,6 +61,12 @@ struct StateP {
   uint32_t* count = nullptr;  // device scalar
 };
 
+// (1/sw, f*_k) of one component: what a resampling hit reads, in one load.
+template <class real>
+struct alignas(2 * sizeof(real)) KV {
+  real inv, f;
+};
+
 template <int Q, int D, class P>
 struct Args {
   using real = typename P::real;
@@ -95,6 +101,7 @@ struct Args {
   uint32_t* svals;
   // resampling
   real* sw;        // [Q][mcap]
+  KV<real>* kv;    // [Q][mcap] (1/sw, f*_k), written by the untiled weights kernel for the untiled gather
   double* cpf64;   // FP64: [Q][ccap]
   float* cpfhi;    // FP32DEV: [Q][ccap]
   float* cpflo;    // FP32DEV: [Q][ccap]
@@ -229,7 +236,7 @@ __device__ __forceinline__ real row_halfwidth2(real R2, real lb2) {
   const float rem = (float)(R2 - lb2);
   if (rem < -(float)R2 * 1e-6f) return (real)-1;
   const float x = fmaxf(rem, 0.f) + (float)R2 * 9.5367431640625e-07f;
-  return (real)(__fsqrt_rz(x) * 1.0001f + 1e-6f);
+  return (real)(bound_sqrt(x) * 1.0001f + 1e-6f);
 }
 
 // Lower bound of |e| on one axis over the candidates of a window cell whose e lies in

@@ -164,7 +164,7 @@ __device__ __forceinline__ real row_halfwidth(real R2, real lby) {
   if (rem < -(float)R2 * 1e-6f) return (real)-1;
   // a fast square root is enough for a bound: inflate it well past its error
   const float x = fmaxf(rem, 0.f) + (float)R2 * 9.5367431640625e-07f;
-  return (real)(__fsqrt_rz(x) * 1.0001f + 1e-6f);
+  return (real)(bound_sqrt(x) * 1.0001f + 1e-6f);
 }
 
 // ---- thinning + refine ------------------------------------------------------------------------
