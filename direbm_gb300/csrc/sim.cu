@@ -57,6 +57,10 @@ __global__ void __launch_bounds__(256) k_collide(const __grid_constant__ Args<Q,
       }
 #pragma unroll
       for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + m] = f[k];
+      if (A.want_wexp) {  // the refine weight exp(f*) once per component (its window kernel reads it)
+#pragma unroll
+        for (int k = 0; k < Q; ++k) A.wexp[(int64_t)k * A.mcap + m] = exp(f[k]);
+      }
     } else {
       float dv[Q];
 #pragma unroll
@@ -71,6 +75,11 @@ __global__ void __launch_bounds__(256) k_collide(const __grid_constant__ Args<Q,
       }
 #pragma unroll
       for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + m] = dv[k];
+      if (A.want_wexp) {
+        const float rho = A.a.rho[m];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) A.wexp[(int64_t)k * A.mcap + m] = exp(__fmaf_rn(rho, A.L.wf[k], dv[k]));
+      }
     }
     uint32_t bm = 0;
     real om[3] = {0, 0, 0};
@@ -243,7 +252,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
             if (canon_d2<D, real>(o, c, e) <= A.R2) {
               mask |= 1u << k;
               ++nk;
-              const real w = exp(fstar_at<Q, D, P>(A, m, k));
+              const real w = A.want_wexp ? A.wexp[(int64_t)k * A.mcap + m] : exp(fstar_at<Q, D, P>(A, m, k));
               if constexpr (std::is_same<P, PF64>::value) {
                 // separate rounding of product and sum (no FMA), in loop order: the oracle
                 // reproduces this sum bit for bit
@@ -300,7 +309,7 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
 #pragma unroll
                 for (int a = 0; a < D; ++a) csb[a] = __dadd_rn(csb[a], A.L.c[A.L.opp[k]][a]);
               }
-              const real w = exp(fstar_at<Q, D, P>(A, m, k));
+              const real w = A.want_wexp ? A.wexp[(int64_t)k * A.mcap + m] : exp(fstar_at<Q, D, P>(A, m, k));
               if constexpr (std::is_same<P, PF64>::value) {
                 swd = __dadd_rn(swd, w);
 #pragma unroll
@@ -1110,6 +1119,8 @@ struct SimImpl : SimBase {
     compact_tmp = tmp;
     DBM_TRY(alloc(&A.sw, (int64_t)Q * mcap));
     DBM_TRY(alloc(&A.kv, (int64_t)Q * mcap));
+    DBM_TRY(alloc(&A.wexp, (int64_t)Q * mcap));
+    A.want_wexp = 0;
     if constexpr (std::is_same<P, PF64>::value) {
       DBM_TRY(alloc(&A.cpf64, (int64_t)Q * ccap));
     } else {
@@ -1353,10 +1364,12 @@ struct SimImpl : SimBase {
     Args<Q, D, P>& A = args;
     mark(0, s);
     const unsigned gm = std::min<unsigned>(div_up(mcap, 256), (unsigned)sm_count() * 16);
+    // the untiled window kernels (3D, obstacles, the soft spawn, or tiles off) read packed items
+    // and the refine weights exp(f*) precomputed by the collision
+    const bool untiled = !tiled_path();
+    A.want_wexp = untiled ? 1 : 0;
     k_collide<Q, D, P><<<gm, 256, 0, s>>>(A);
     DBM_LAUNCH_CHECK();
-    // the untiled window kernels (3D, obstacles, or tiles off) read packed items
-    const bool untiled = !tiled_path();
     if (untiled) {
       k_pack<Q, D, P><<<gm, 256, 0, s>>>(A, A.a, A.mcap, A.a.count);
       DBM_LAUNCH_CHECK();

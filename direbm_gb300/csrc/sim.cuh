@@ -102,6 +102,8 @@ struct Args {
   // resampling
   real* sw;        // [Q][mcap]
   KV<real>* kv;    // [Q][mcap] (1/sw, f*_k), written by the untiled weights kernel for the untiled gather
+  real* wexp;      // [Q][mcap] exp(f*_k), written by the collision when want_wexp (untiled refine)
+  int want_wexp;
   double* cpf64;   // FP64: [Q][ccap]
   float* cpfhi;    // FP32DEV: [Q][ccap]
   float* cpflo;    // FP32DEV: [Q][ccap]
