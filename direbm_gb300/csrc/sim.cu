@@ -124,8 +124,11 @@ __device__ __forceinline__ typename P::real fstar_at(const Args<Q, D, P>& A, uin
   }
 }
 
+template <class P>
+constexpr int thin_min_blocks() { return std::is_same<P, PF64>::value ? 1 : 12; }
+
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Args<Q, D, P> A) {
+__global__ void __launch_bounds__(128, thin_min_blocks<P>()) k_thin_refine(const __grid_constant__ Args<Q, D, P> A) {
   using real = typename P::real;
   const uint32_t F = blockIdx.x * blockDim.x + threadIdx.x;
   if (F >= A.ncells) return;
@@ -155,11 +158,13 @@ __global__ void __launch_bounds__(128) k_thin_refine(const __grid_constant__ Arg
           const uint32_t m0 = A.a.start[Sg], m1 = A.a.start[Sg + 1];
           for (uint32_t m = m0; m < m1; ++m) {
             if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: stays in its cell
+            const PackItem<real> it = A.a.pk[m];  // the offsets in one load
+            const real om[3] = {it.x, it.y, it.z};
             real t[3];
             bool land = true;
 #pragma unroll
             for (int a = 0; a < D; ++a) {
-              t[a] = rn_add(A.a.off[(int64_t)a * A.mcap + m], A.L.template cd_as<real>(k, a));
+              t[a] = rn_add(om[a], A.L.template cd_as<real>(k, a));
               land &= (so[a] + (int)floor(t[a])) == 0;
             }
             if (land) {
