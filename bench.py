@@ -604,10 +604,22 @@ def _oracle_instance_steps(args):
     return pts, time.perf_counter() - t0
 
 
-def cpu_baseline_leg(n=128, steps=2):
+def cpu_baseline_leg(n=128, steps=2, lbm_steps=3):
     pts, sec = _oracle_instance_steps((n, 0.8, 100, steps))
-    return {"value": pts / sec, "unit": "point-steps/s", "cores": 1, "kind": "port",
-            "sample": f"numpy oracle of the step, one {n}x{n} periodic D2Q9 instance, {steps} steps, {sec:.1f} s"}
+    out = {"value": pts / sec, "unit": "point-steps/s", "cores": 1, "kind": "port",
+           "sample": f"numpy oracle of the step, one {n}x{n} periodic D2Q9 instance, {steps} steps, {sec:.1f} s"}
+    # the hex LBM on one host thread: the numpy oracle (the reference's HexLBM restated), one
+    # 1024 x 1024 run of the shear wave, FP64
+    from oracle import lbm as olbm
+
+    f0 = olbm.shear_wave(1024, 1024, 0.01)
+    olbm.run(f0, 0.7, 1)
+    t0 = time.perf_counter()
+    olbm.run(f0, 0.7, lbm_steps)
+    sec = time.perf_counter() - t0
+    out["lbm"] = {"value": 1024 * 1024 * lbm_steps / sec, "unit": "node-steps/s", "cores": 1, "kind": "port",
+                  "sample": f"numpy oracle HexLBM, one 1024x1024 run, {lbm_steps} steps, {sec:.1f} s"}
+    return out
 
 
 def run_reference(args):
