@@ -950,6 +950,7 @@ struct SimImpl : SimBase {
   int key_bits = 1;
   int64_t mcap = 0, ccap = 0;
   std::vector<void*> allocs;
+  std::vector<size_t> alloc_sizes;  // bytes of allocs[i]
   int64_t bytes = 0;
   Args<Q, D, P> args{};  // args for the current direction (a = current state)
   StateP<P> st[2];
@@ -1011,6 +1012,7 @@ struct SimImpl : SimBase {
     void* q = nullptr;
     DBM_CUDA(cudaMalloc(&q, b));
     allocs.push_back(q);
+    alloc_sizes.push_back(b);
     bytes += (int64_t)b;
     *p = (T*)q;
     return DBM_OK;
@@ -1224,8 +1226,7 @@ struct SimImpl : SimBase {
         for (int x0 = 0; x0 < inst_h[i].dims[0]; x0 += geo.tx) tiles.push_back({i, x0, y0});
     ntiles = (int)tiles.size();
     if (d_tiles) {  // re-tiling: release the previous list
-      cudaFree(d_tiles);
-      allocs.erase(std::remove(allocs.begin(), allocs.end(), (void*)d_tiles), allocs.end());
+      release(d_tiles);
       d_tiles = nullptr;
     }
     DBM_TRY(alloc(&d_tiles, ntiles));
@@ -1301,10 +1302,17 @@ struct SimImpl : SimBase {
   }
   bool spawn_ready = false;
 
+  // Free one of this handle's allocations (the caller syncs first if a step may still use it).
   void release(void* p) {
     if (!p) return;
-    cudaFree(p);
-    allocs.erase(std::remove(allocs.begin(), allocs.end(), p), allocs.end());
+    for (size_t i = 0; i < allocs.size(); ++i) {
+      if (allocs[i] != p) continue;
+      cudaFree(p);
+      bytes -= (int64_t)alloc_sizes[i];
+      allocs.erase(allocs.begin() + (std::ptrdiff_t)i);
+      alloc_sizes.erase(alloc_sizes.begin() + (std::ptrdiff_t)i);
+      return;
+    }
   }
 
   void invalidate_graphs() override {

@@ -105,3 +105,36 @@ def test_bad_arguments_raise():
         sim.set_tiling(12, False)  # must divide 256
     with pytest.raises(DbmError):
         sim.set_tau([0.4])
+
+
+def test_state_into_caller_buffers_and_status_reads_on_busy_copy_streams():
+    """state(out=...) writes the same rows as state() into the caller's (larger) buffers and checks
+    them; count and status read correctly while a bulk copy runs on another stream."""
+    import torch
+
+    from direbm_gb300.sim import Instance, Simulation
+
+    x, f = periodic_tg(24, "D2Q9", seed=5)
+    sim = Simulation([Instance(dims=(24, 24), tau=0.7)], lattice="D2Q9", precision="fp32dev", r_res=1.5, cell=1.0)
+    sim.set_state(None, x, f)
+    sim.step(2)
+    ref = [t.clone() for t in sim.state()]
+    n = ref[0].shape[0]
+    out = (torch.full((n + 7,), -1, dtype=torch.int32, device="cuda"),
+           torch.full((n + 7, 2), -1.0, dtype=torch.float64, device="cuda"),
+           torch.full((n + 7, 9), -1.0, dtype=torch.float64, device="cuda"))
+    side = torch.cuda.Stream()
+    big = torch.empty(64 << 20, dtype=torch.uint8).pin_memory()
+    dbig = torch.empty(big.shape, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(side):
+        dbig.copy_(big, non_blocking=True)
+    got = sim.state(out=out)
+    assert sim.count() == n and sim.status() == 0
+    torch.cuda.synchronize()
+    for g, r, o in zip(got, ref, out):
+        assert g.data_ptr() == o.data_ptr() and torch.equal(g, r)
+        assert bool((o[n:] == -1).all())
+    with pytest.raises(ValueError):
+        sim.state(out=(out[0][: n - 1], out[1], out[2]))
+    with pytest.raises(ValueError):
+        sim.state(out=(out[0], out[1].float(), out[2]))
