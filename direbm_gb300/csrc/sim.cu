@@ -470,18 +470,43 @@ __global__ void __launch_bounds__(256) k_finalize(const __grid_constant__ Args<Q
   if (blockIdx.x == 0 && threadIdx.x == 0) *A.b.count = Pn;
 }
 
-// start[c] = number of sorted keys < c, for c in [0, ncells].
+// start[c] = number of sorted keys < c, for c in [0, ncells].  Each thread takes 8 consecutive cells:
+// one binary search for the first, then a walk along the sorted keys (8x fewer dependent-load
+// searches; a thread's walk covers only the keys of its own cells).
+constexpr int kCellStartChunk = 8;
 __global__ void __launch_bounds__(256) k_cell_start(const uint32_t* __restrict__ keys, const uint32_t* d_n,
                                                     uint32_t ncells, uint32_t* __restrict__ start) {
   const uint32_t n = *d_n;
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c <= ncells; c += gridDim.x * blockDim.x) {
+  const uint64_t nchunks = ((uint64_t)ncells + kCellStartChunk) / kCellStartChunk;  // cells 0..ncells
+  for (uint64_t ch = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; ch < nchunks;
+       ch += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c0 = (uint32_t)(ch * kCellStartChunk);
     uint32_t lo = 0, hi = n;
     while (lo < hi) {
-      uint32_t mid = (lo + hi) >> 1;
-      if (keys[mid] < c) lo = mid + 1; else hi = mid;
+      const uint32_t mid = (lo + hi) >> 1;
+      if (keys[mid] < c0) lo = mid + 1; else hi = mid;
     }
-    start[c] = lo;
+    uint32_t v[kCellStartChunk];
+#pragma unroll
+    for (int i = 0; i < kCellStartChunk; ++i) {
+      v[i] = lo;  // = number of keys < c0 + i
+      while (lo < n && keys[lo] == c0 + (uint32_t)i) ++lo;
+    }
+    if ((uint64_t)c0 + kCellStartChunk <= (uint64_t)ncells + 1) {
+      uint4* dst = reinterpret_cast<uint4*>(start + c0);  // 32-byte aligned: c0 is a multiple of 8
+      dst[0] = make_uint4(v[0], v[1], v[2], v[3]);
+      dst[1] = make_uint4(v[4], v[5], v[6], v[7]);
+    } else {
+      for (int i = 0; (uint64_t)c0 + i <= ncells; ++i) start[c0 + i] = v[i];
+    }
   }
+}
+
+static void launch_cell_start(const uint32_t* keys, const uint32_t* d_n, uint32_t ncells, uint32_t* start,
+                              cudaStream_t s) {
+  const int64_t nchunks = ((int64_t)ncells + kCellStartChunk) / kCellStartChunk;
+  k_cell_start<<<std::min<unsigned>(div_up(nchunks, 256), (unsigned)sm_count() * 16), 256, 0, s>>>(keys, d_n, ncells,
+                                                                                                  start);
 }
 
 template <int Q, int D, class P>
@@ -1340,7 +1365,9 @@ struct SimImpl : SimBase {
     k_import_keys<Q, D, P><<<grid, 256, 0, s>>>(args, inst_of, pos, m, desc.cell, k_in, v_in, toff);
     DBM_LAUNCH_CHECK();
     bool alt = false;
-    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, m, nullptr, 32, sort_tmp, s, &alt));
+    // valid keys are < ncells < 2^key_bits; the marker 0xffffffff of a moment outside its box is
+    // all ones in those bits too, so it still sorts after every valid key
+    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, m, nullptr, key_bits, sort_tmp, s, &alt));
     import_in_alt = alt;
     const uint32_t* ks = alt ? k_alt : k_in;
     const uint32_t* vs = alt ? v_alt : v_in;
@@ -1348,8 +1375,7 @@ struct SimImpl : SimBase {
     DBM_LAUNCH_CHECK();
     // count of valid keys = m (invalid ones sort last with key 0xffffffff and raise ST_BAD_INPUT)
     DBM_CUDA(cudaMemcpyAsync(args.d_P, args.a.count, 4, cudaMemcpyDeviceToDevice, s));
-    k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, s>>>(
-        ks, args.d_P, ncells, args.a.start);
+    launch_cell_start(ks, args.d_P, ncells, args.a.start, s);
     DBM_LAUNCH_CHECK();
     return DBM_OK;
   }
@@ -1415,8 +1441,7 @@ struct SimImpl : SimBase {
       k_pack<Q, D, P><<<gc, 256, 0, s>>>(A, A.b, A.ccap, A.d_P);
       DBM_LAUNCH_CHECK();
     }
-    k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, s>>>(
-        A.skeys, A.d_P, ncells, A.b.start);
+    launch_cell_start(A.skeys, A.d_P, ncells, A.b.start, s);
     DBM_LAUNCH_CHECK();
     mark(3, s);
     if (upto <= 3) return DBM_OK;
@@ -1705,8 +1730,7 @@ struct SimImpl : SimBase {
     }
     DBM_CUDA(cudaMemcpyAsync(S.count, &m, 4, cudaMemcpyHostToDevice, own));
     DBM_CUDA(cudaMemcpyAsync(args.d_P, &m, 4, cudaMemcpyHostToDevice, own));
-    k_cell_start<<<std::min<unsigned>(div_up((int64_t)ncells + 1, 256), (unsigned)sm_count() * 16), 256, 0, own>>>(
-        S.cell, args.d_P, ncells, S.start);
+    launch_cell_start(S.cell, args.d_P, ncells, S.start, own);
     DBM_LAUNCH_CHECK();
     DBM_CUDA(cudaStreamSynchronize(own));  // `m` lives on this thread's stack
     DBM_CUDA(cudaEventRecord(ev_out, own));
