@@ -37,7 +37,7 @@ TAPE = {
     "gap_e": (23, "f64", "Dngap"), "inst_start": (24, "u32", "I+1"),
 }
 
-ST_OUT_OF_BOX, ST_CAPACITY, ST_NONFINITE, ST_BAD_INPUT = 1, 2, 4, 8
+ST_OUT_OF_BOX, ST_CAPACITY, ST_NONFINITE, ST_BAD_INPUT, ST_INTERNAL = 1, 2, 4, 8, 16
 
 
 class DbmError(RuntimeError):

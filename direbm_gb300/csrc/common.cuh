@@ -58,6 +58,7 @@ enum : uint32_t {
   ST_CAPACITY = 1u << 1,        // a buffer would overflow its capacity
   ST_NONFINITE = 1u << 2,       // a non-finite value was produced
   ST_BAD_INPUT = 1u << 3,       // set_state got a position outside its box
+  ST_INTERNAL = 1u << 4,        // an internal consistency check failed (a bug: please report)
 };
 
 // ---- round-to-nearest arithmetic with no contraction -----------------------------------------

@@ -470,6 +470,51 @@ __global__ void __launch_bounds__(256) k_finalize(const __grid_constant__ Args<Q
   if (blockIdx.x == 0 && threadIdx.x == 0) *A.b.count = Pn;
 }
 
+// ---- control points in cell order without a sort (2D, small move bound) ---------------------------
+// A refined control point lands within +-H cells of its thinning cell on each axis (H = floor(R) + 1:
+// centroid in [0, 1], move at most R).  So the stable order by (final cell, thinning cell) that a
+// sort would give follows from per-cell counts and, for each point, the number of earlier thinning
+// cells of its final cell's (2H+1)^2 neighbourhood that land in the same cell.
+
+// count[G] += 1 per control point (integer atomics: order-independent).
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_place_count(const __grid_constant__ Args<Q, D, P> A, uint32_t* __restrict__ cnt) {
+  for (uint32_t F = blockIdx.x * blockDim.x + threadIdx.x; F < A.ncells; F += gridDim.x * blockDim.x)
+    if (A.occ[F]) atomicAdd(cnt + A.fkey[F], 1u);
+}
+
+// Slot of each control point = start[G] + its rank among the thinning cells F' < F that land in G;
+// writes the next state's cell and offsets and the (key, thinning cell) pairs a sort would leave.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_place(const __grid_constant__ Args<Q, D, P> A, int H,
+                                               uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  for (uint32_t F = blockIdx.x * blockDim.x + threadIdx.x; F < A.ncells; F += gridDim.x * blockDim.x) {
+    if (!A.occ[F]) continue;
+    const uint32_t G = A.fkey[F];
+    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
+    int Gc[3];
+    decode_cell<D>(I, G, Gc);
+    uint32_t rank = 0, all = 0;
+    for (int dy = -H; dy <= H; ++dy)
+      for (int dx = -H; dx <= H; ++dx) {
+        uint32_t Fp;
+        if (!cell_at<D>(I, Gc[0] + dx, Gc[1] + dy, 0, &Fp)) continue;
+        const uint32_t hit = A.fkey[Fp] == G ? 1u : 0u;  // fkey is all ones where no control point was made
+        all += hit;
+        rank += Fp < F ? hit : 0u;
+      }
+    // every control point of G comes from this neighbourhood (the move bound): check it
+    if (all != A.b.start[G + 1] - A.b.start[G]) atomicOr(A.status, ST_INTERNAL);
+    const uint32_t j = A.b.start[G] + rank;
+    keys[j] = G;
+    vals[j] = F;
+    A.b.cell[j] = G;
+#pragma unroll
+    for (int a = 0; a < D; ++a) A.b.off[(int64_t)a * A.ccap + j] = A.foff[(int64_t)a * A.ncells + F];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.b.count = A.b.start[A.ncells];
+}
+
 // start[c] = number of sorted keys < c, for c in [0, ncells].  Each thread takes 8 consecutive cells:
 // one binary search for the first, then a walk along the sorted keys (8x fewer dependent-load
 // searches; a thread's walk covers only the keys of its own cells).
@@ -987,6 +1032,8 @@ struct SimImpl : SimBase {
   InstK* dinst = nullptr;
   void* sort_tmp = nullptr;
   void* compact_tmp = nullptr;
+  void* place_tmp = nullptr;  // scan scratch of the sort-free control-point placement
+  int place_h = 0;            // its neighbourhood half-width, 0 if it does not apply
   cudaStream_t own = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -1149,6 +1196,18 @@ struct SimImpl : SimBase {
     sort_tmp = tmp;
     DBM_TRY(alloc(&tmp, (int64_t)compact_tmp_bytes(ncells)));
     compact_tmp = tmp;
+    DBM_TRY(alloc(&tmp, (int64_t)scan_tmp_bytes((int64_t)ncells + 1)));
+    place_tmp = tmp;
+    // sort-free placement (2D): move bound H = floor(R) + 1 cells; used while the (2H+1)^2
+    // neighbourhood stays small and cannot wrap onto itself in a periodic box
+    place_h = 0;
+    if constexpr (D == 2) {
+      const int H = (int)std::floor(R) + 1;
+      bool ok = H <= 3;
+      for (const InstK& I : inst_h)
+        if (I.periodic && (I.dims[0] < 2 * H + 1 || I.dims[1] < 2 * H + 1)) ok = false;
+      if (ok) place_h = H;
+    }
     DBM_TRY(alloc(&A.sw, (int64_t)Q * mcap));
     DBM_TRY(alloc(&A.kv, (int64_t)Q * mcap));
     DBM_TRY(alloc(&A.wexp, (int64_t)Q * mcap));
@@ -1427,22 +1486,36 @@ struct SimImpl : SimBase {
     if (upto <= 2) return DBM_OK;
     // slots: regular CPs [0, ncells), spawned ones [ncells, 2 ncells); the stable sort keeps that
     // order among CPs of one cell
-    const int64_t nslots = A.kappa_soft > 0 ? 2 * (int64_t)ncells : (int64_t)ncells;
-    DBM_TRY(compact_flags_u32(A.occ, A.fkey, k_in, v_in, nslots, A.d_P, compact_tmp, s));
-    bool alt = false;
-    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, nslots, A.d_P, key_bits, sort_tmp, s, &alt));
-    sorted_in_alt = alt;
-    A.skeys = alt ? k_alt : k_in;
-    A.svals = alt ? v_alt : v_in;
     const unsigned gc = std::min<unsigned>(div_up(ccap, 256), (unsigned)sm_count() * 16);
-    k_finalize<Q, D, P><<<gc, 256, 0, s>>>(A);
-    DBM_LAUNCH_CHECK();
-    if (untiled) {
-      k_pack<Q, D, P><<<gc, 256, 0, s>>>(A, A.b, A.ccap, A.d_P);
+    if (!untiled && place_h > 0 && A.kappa_soft == 0) {
+      // counts per final cell -> cell starts (and P) by one scan -> each point's slot
+      const unsigned gf = std::min<unsigned>(div_up(ncells, 256), (unsigned)sm_count() * 16);
+      DBM_CUDA(cudaMemsetAsync(A.b.start, 0, ((size_t)ncells + 1) * 4, s));
+      k_place_count<Q, D, P><<<gf, 256, 0, s>>>(A, A.b.start);
+      DBM_LAUNCH_CHECK();
+      DBM_TRY(scan_exclusive_u32(A.b.start, A.b.start, (int64_t)ncells + 1, nullptr, A.d_P, place_tmp, s));
+      k_place<Q, D, P><<<gf, 256, 0, s>>>(A, place_h, k_in, v_in);
+      DBM_LAUNCH_CHECK();
+      sorted_in_alt = false;
+      A.skeys = k_in;
+      A.svals = v_in;
+    } else {
+      const int64_t nslots = A.kappa_soft > 0 ? 2 * (int64_t)ncells : (int64_t)ncells;
+      DBM_TRY(compact_flags_u32(A.occ, A.fkey, k_in, v_in, nslots, A.d_P, compact_tmp, s));
+      bool alt = false;
+      DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, nslots, A.d_P, key_bits, sort_tmp, s, &alt));
+      sorted_in_alt = alt;
+      A.skeys = alt ? k_alt : k_in;
+      A.svals = alt ? v_alt : v_in;
+      k_finalize<Q, D, P><<<gc, 256, 0, s>>>(A);
+      DBM_LAUNCH_CHECK();
+      if (untiled) {
+        k_pack<Q, D, P><<<gc, 256, 0, s>>>(A, A.b, A.ccap, A.d_P);
+        DBM_LAUNCH_CHECK();
+      }
+      launch_cell_start(A.skeys, A.d_P, ncells, A.b.start, s);
       DBM_LAUNCH_CHECK();
     }
-    launch_cell_start(A.skeys, A.d_P, ncells, A.b.start, s);
-    DBM_LAUNCH_CHECK();
     mark(3, s);
     if (upto <= 3) return DBM_OK;
     if constexpr (D == 2) {

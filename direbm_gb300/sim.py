@@ -226,7 +226,8 @@ class Simulation:
     def check_status(self):
         st = self.status(clear=False)
         if st:
-            names = [n for n, b in (("out_of_box", 1), ("capacity", 2), ("nonfinite", 4), ("bad_input", 8)) if st & b]
+            names = [n for n, b in (("out_of_box", 1), ("capacity", 2), ("nonfinite", 4), ("bad_input", 8),
+                                    ("internal", 16)) if st & b]
             raise _lib.DbmError(f"device status: {', '.join(names)}")
 
     def conservation(self) -> torch.Tensor:

@@ -155,7 +155,9 @@ int dbm_sim_step(dbm_sim* sim, int32_t steps, void* stream);
 int dbm_sim_count(dbm_sim* sim, int64_t* m, void* stream);
 /* Export the state (outputs sized by dbm_sim_count), world positions and f in FP64. */
 int dbm_sim_get_state(dbm_sim* sim, int32_t* d_inst, double* d_pos, double* d_f, void* stream);
-/* Synchronises and returns the device status word (ST_* bits); clears it when clear != 0. */
+/* Synchronises and returns the device status word; clears it when clear != 0.  Bits: 1 a point
+ * left a bounded box, 2 a capacity was exceeded, 4 a non-finite value, 8 set_state input outside
+ * its box, 16 an internal consistency check failed. */
 int dbm_sim_status(dbm_sim* sim, uint32_t* flags, int32_t clear, void* stream);
 /* Per-instance FP64 totals: mass, then momentum per axis -> d_out (n_inst, 1 + D). */
 int dbm_sim_conservation(dbm_sim* sim, double* d_out, void* stream);
