@@ -66,7 +66,7 @@ KERNEL_BYTES = {
 # DRAM bytes per input moment measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
 # one launch on a 4.18 M-moment case of this workload (profiles/gather_t_full_ensemble64.md);
 # traffic grows with the moments, so a full launch's traffic is this times M.
-KERNEL_TRAFFIC_PER_MOMENT = {"gather": 170.5}
+KERNEL_TRAFFIC_PER_MOMENT = {"gather": 170.6}
 
 # Per point-step byte model of the method (components materialised as 12-byte sort records):
 # B = M(Qs+b_p) + Nc k_b + 2 Nc k_b + 3(Nc k_b + M(Qs+b_p)) + 3 P b_p + P(Qs+b_p), with P ~ M,
