@@ -59,13 +59,15 @@ KERNEL_BYTES = {
     "emit": ("cp", 0, 8 * Q9 + 4 + 12 + 4 * (1 + Q9)),
     # per moment: read rho + dev, write dev
     "collide": ("moment", 4 * (1 + Q9) + 4 + 4 * Q9, 0),
-    # per CP: 3 passes x (hist read 4 + scatter read 8 + write 8) + compaction (8) + finalize (24)
+    # per CP, radix path: 3 passes x (hist read 4 + scatter read 8 + write 8) + compaction (8) +
+    # finalize (24); the 2D tiled path places points without a sort and moves fewer bytes
     "sort": ("cp", 0, 3 * 20 + 8 + 24),
 }
 
 # DRAM bytes per input moment measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
-# one launch on a 4.18 M-moment case of this workload (profiles/gather_t_full_ensemble64.md);
-# traffic grows with the moments, so a full launch's traffic is this times M.
+# one launch of k_gather_t on a 4.18 M-moment case of this workload (its first 64 members, 16x16
+# tiles): 436.4 MB read + 277.4 MB written.  Traffic grows with the moments, so a full launch's
+# traffic is this times M.
 KERNEL_TRAFFIC_PER_MOMENT = {"gather": 170.6}
 
 # Per point-step byte model of the method (components materialised as 12-byte sort records):
