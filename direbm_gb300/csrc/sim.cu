@@ -1209,8 +1209,8 @@ struct SimImpl : SimBase {
       if (ok) place_h = H;
     }
     DBM_TRY(alloc(&A.sw, (int64_t)Q * mcap));
-    DBM_TRY(alloc(&A.kv, (int64_t)Q * mcap));
-    DBM_TRY(alloc(&A.wexp, (int64_t)Q * mcap));
+    A.kv = nullptr;  // the untiled path's buffers: see ensure_untiled
+    A.wexp = nullptr;
     A.want_wexp = 0;
     if constexpr (std::is_same<P, PF64>::value) {
       DBM_TRY(alloc(&A.cpf64, (int64_t)Q * ccap));
@@ -1229,6 +1229,18 @@ struct SimImpl : SimBase {
     DBM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+    if (!tiled) DBM_TRY(ensure_untiled());  // 3D: always the untiled window kernels
+    return DBM_OK;
+  }
+
+  // Per-component buffers that only the untiled window kernels use: (1/sw, f*) pairs and exp(f*)
+  // ([Q][mcap] each).  Allocated by the calls that make that path possible (creation in 3D, an
+  // obstacle, the soft spawn, tiles off), so a tiled 2D simulation never holds them.
+  int ensure_untiled() override {
+    if (args.kv) return DBM_OK;
+    DBM_TRY(alloc(&args.kv, (int64_t)Q * mcap));
+    DBM_TRY(alloc(&args.wexp, (int64_t)Q * mcap));
+    invalidate_graphs();  // captured launches hold the pointers
     return DBM_OK;
   }
 
@@ -1379,6 +1391,7 @@ struct SimImpl : SimBase {
         spawn_ready = true;
       }
     }
+    if (ks > 0) DBM_TRY(ensure_untiled());
     args.kappa_soft = ks;
     kappa_soft = ks;
     invalidate_graphs();  // captured launches hold the flag and the buffers
@@ -1465,6 +1478,10 @@ struct SimImpl : SimBase {
     // the untiled window kernels (3D, obstacles, the soft spawn, or tiles off) read packed items
     // and the refine weights exp(f*) precomputed by the collision
     const bool untiled = !tiled_path();
+    if (untiled && !A.kv) {
+      set_last_error("internal: the untiled window kernels' buffers were not allocated");
+      return DBM_ERR_STATE;
+    }
     A.want_wexp = untiled ? 1 : 0;
     k_collide<Q, D, P><<<gm, 256, 0, s>>>(A);
     DBM_LAUNCH_CHECK();
@@ -1691,6 +1708,7 @@ struct SimImpl : SimBase {
         }
         I.obs_c[a] = c;
       }
+      DBM_TRY(ensure_untiled());
       I.obs_r2 = r * r;
       I.has_obs = 1;
       // margins (cell units, generous against FP32 rounding): a blocked direction ends inside the
@@ -1997,7 +2015,10 @@ int dbm_sim_conservation(dbm_sim* s, double* out, void* stream) {
 int dbm_sim_set_option(dbm_sim* s, int32_t option, int32_t value) {
   SIM_CHECK(s);
   if (option == DBM_OPT_GRAPHS) s->impl->use_graphs = value ? 1 : 0;
-  else if (option == DBM_OPT_TILES) s->impl->use_tiles = value ? 1 : 0;
+  else if (option == DBM_OPT_TILES) {
+    if (!value) DBM_TRY(s->impl->ensure_untiled());
+    s->impl->use_tiles = value ? 1 : 0;
+  }
   else if (option == DBM_OPT_TILE_WIDTH || option == DBM_OPT_PERSISTENT) {
     int tx = 0, pers = 0;
     s->impl->tiling(&tx, &pers);
