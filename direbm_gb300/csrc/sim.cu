@@ -125,15 +125,12 @@ __device__ __forceinline__ typename P::real fstar_at(const Args<Q, D, P>& A, uin
 }
 
 template <class P>
-constexpr int thin_min_blocks() { return std::is_same<P, PF64>::value ? 1 : 12; }
+constexpr int thin_min_blocks() { return std::is_same<P, PF64>::value ? 1 : 6; }
 
+// Thinning + refine of one cell F of instance I (the untiled window kernels).
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(128, thin_min_blocks<P>()) k_thin_refine(const __grid_constant__ Args<Q, D, P> A) {
+__device__ __forceinline__ void thin_refine_cell(const Args<Q, D, P>& A, const uint32_t F, const InstK& I) {
   using real = typename P::real;
-  const uint32_t F = blockIdx.x * blockDim.x + threadIdx.x;
-  if (F >= A.ncells) return;
-  const int b = find_instance(A.inst_base, A.n_inst, F);
-  const InstK I = A.inst[b];
   int Fc[3];
   decode_cell<D>(I, F, Fc);
 
@@ -429,6 +426,21 @@ __global__ void __launch_bounds__(128, thin_min_blocks<P>()) k_thin_refine(const
   }
 }
 
+// The untiled window kernels take one brick of cells per block (thread t <-> cell t of the brick):
+// a block's windows then cover a compact region that stays in L1, where consecutive points in cell
+// order would span a long strip of rows.
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256, thin_min_blocks<P>()) k_thin_refine(const __grid_constant__ Args<Q, D, P> A,
+                                                                           const Brick* __restrict__ bricks,
+                                                                           int nbricks, BrickGeo bg) {
+  for (int bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
+    const Brick B = bricks[bi];
+    const InstK I = A.inst[B.inst];
+    uint32_t F;
+    if (brick_cell<D>(B, I, bg, threadIdx.x, &F)) thin_refine_cell<Q, D, P>(A, F, I);
+  }
+}
+
 // Packed copy (offsets + cell x coordinate) of a state for the untiled window kernels.
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_pack(const __grid_constant__ Args<Q, D, P> A, StateP<P> S, int64_t stride,
@@ -554,16 +566,11 @@ static void launch_cell_start(const uint32_t* keys, const uint32_t* d_n, uint32_
                                                                                                   start);
 }
 
+// sw of component (m, k), m a moment in cell g of instance I.
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q, D, P> A) {
+__device__ __forceinline__ void weights_one(const Args<Q, D, P>& A, const uint32_t m, const int k, const uint32_t g,
+                                            const InstK& I) {
   using real = typename P::real;
-  const uint32_t M = *A.a.count;
-  const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
-  if (m >= M) return;
-  const uint32_t g = A.a.cell[m];
-  const int b = find_instance(A.inst_base, A.n_inst, g);
-  const InstK I = A.inst[b];
   int Sc[3];
   decode_cell<D>(I, g, Sc);
   real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
@@ -633,16 +640,11 @@ __global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q,
 template <class P>
 constexpr int gather_min_blocks() { return std::is_same<P, PF64>::value ? 1 : 6; }
 
+// Resampled f_k of control point j, in cell G of instance I.
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256, gather_min_blocks<P>()) k_gather(const __grid_constant__ Args<Q, D, P> A) {
+__device__ __forceinline__ void gather_one(const Args<Q, D, P>& A, const uint32_t j, const int k, const uint32_t G,
+                                           const InstK& I) {
   using real = typename P::real;
-  const uint32_t Pn = *A.d_P;
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int k = blockIdx.y;
-  if (j >= Pn) return;
-  const uint32_t G = A.b.cell[j];
-  const int b = find_instance(A.inst_base, A.n_inst, G);
-  const InstK I = A.inst[b];
   int Gc[3];
   decode_cell<D>(I, G, Gc);
   real p[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
@@ -759,6 +761,33 @@ __global__ void __launch_bounds__(256, gather_min_blocks<P>()) k_gather(const __
     empty = Fv.hi < A.eps;
   }
   if (empty) atomicOr(A.emask + j, 1u << k);
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q, D, P> A,
+                                                 const Brick* __restrict__ bricks, int nbricks, BrickGeo bg) {
+  const int k = blockIdx.y;
+  for (int bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
+    const Brick B = bricks[bi];
+    const InstK I = A.inst[B.inst];
+    uint32_t F;
+    if (!brick_cell<D>(B, I, bg, threadIdx.x, &F)) continue;
+    for (uint32_t m = A.a.start[F], m1 = A.a.start[F + 1]; m < m1; ++m) weights_one<Q, D, P>(A, m, k, F, I);
+  }
+}
+
+template <int Q, int D, class P>
+__global__ void __launch_bounds__(256, gather_min_blocks<P>()) k_gather(const __grid_constant__ Args<Q, D, P> A,
+                                                                        const Brick* __restrict__ bricks, int nbricks,
+                                                                        BrickGeo bg) {
+  const int k = blockIdx.y;
+  for (int bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
+    const Brick B = bricks[bi];
+    const InstK I = A.inst[B.inst];
+    uint32_t F;
+    if (!brick_cell<D>(B, I, bg, threadIdx.x, &F)) continue;
+    for (uint32_t j = A.b.start[F], j1 = A.b.start[F + 1]; j < j1; ++j) gather_one<Q, D, P>(A, j, k, F, I);
+  }
 }
 
 template <int Q, int D, class P>
@@ -1033,6 +1062,9 @@ struct SimImpl : SimBase {
   void* sort_tmp = nullptr;
   void* compact_tmp = nullptr;
   void* place_tmp = nullptr;  // scan scratch of the sort-free control-point placement
+  Brick* d_bricks = nullptr;  // bricks of cells for the untiled window kernels (one per block)
+  int nbricks = 0;
+  BrickGeo bgeo{1, 1, 1};
   int place_h = 0;            // its neighbourhood half-width, 0 if it does not apply
   cudaStream_t own = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -1229,6 +1261,21 @@ struct SimImpl : SimBase {
     DBM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+    // bricks of 256 cells: 8 x 8 x 4 in 3D, 16 x 16 in 2D
+    bgeo = D == 3 ? BrickGeo{8, 8, 4} : BrickGeo{16, 16, 1};
+    {
+      std::vector<Brick> bl;
+      for (int i = 0; i < (int)inst_h.size(); ++i) {
+        const int* dm = inst_h[i].dims;
+        for (int z0 = 0; z0 < (D == 3 ? dm[2] : 1); z0 += bgeo.bz)
+          for (int y0 = 0; y0 < dm[1]; y0 += bgeo.by)
+            for (int x0 = 0; x0 < dm[0]; x0 += bgeo.bx) bl.push_back({i, x0, y0, z0});
+      }
+      if (bl.size() >= 0x7fffffffu) { set_last_error("too many bricks"); return DBM_ERR_CAPACITY; }
+      nbricks = (int)bl.size();
+      DBM_TRY(alloc(&d_bricks, nbricks));
+      DBM_CUDA(cudaMemcpy(d_bricks, bl.data(), sizeof(Brick) * bl.size(), cudaMemcpyHostToDevice));
+    }
     if (!tiled) DBM_TRY(ensure_untiled());  // 3D: always the untiled window kernels
     return DBM_OK;
   }
@@ -1494,9 +1541,9 @@ struct SimImpl : SimBase {
     if constexpr (D == 2) {
       if (tiled_path())
         k_thin_refine_t<Q, P><<<use_persistent ? pgrid[0] : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo, ntiles);
-      else k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
+      else k_thin_refine<Q, D, P><<<nbricks, 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     } else {
-      k_thin_refine<Q, D, P><<<div_up(ncells, 128), 128, 0, s>>>(A);
+      k_thin_refine<Q, D, P><<<nbricks, 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     }
     DBM_LAUNCH_CHECK();
     mark(2, s);
@@ -1538,9 +1585,9 @@ struct SimImpl : SimBase {
     if constexpr (D == 2) {
       if (tiled_path())
         k_weights_t<Q, P><<<use_persistent ? pgrid[1] : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo, ntiles);
-      else k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
+      else k_weights<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     } else {
-      k_weights<Q, D, P><<<dim3(div_up(mcap, 256), Q), 256, 0, s>>>(A);
+      k_weights<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     }
     DBM_LAUNCH_CHECK();
     mark(4, s);
@@ -1549,9 +1596,9 @@ struct SimImpl : SimBase {
     if constexpr (D == 2) {
       if (tiled_path())
         k_gather_t<Q, P><<<use_persistent ? pgrid[2] : ntiles, 256, sm_gather, s>>>(A, d_tiles, geo, ntiles);
-      else k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
+      else k_gather<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     } else {
-      k_gather<Q, D, P><<<dim3(div_up(ccap, 256), Q), 256, 0, s>>>(A);
+      k_gather<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     }
     DBM_LAUNCH_CHECK();
     mark(5, s);

@@ -61,6 +61,23 @@ struct StateP {
   uint32_t* count = nullptr;  // device scalar
 };
 
+// A brick of cells of one instance (x0, y0, z0: its first cell) and the brick extent: the untiled
+// window kernels map thread t of a block to cell t of a brick, x fastest.
+struct Brick {
+  int inst, x0, y0, z0;
+};
+struct BrickGeo {
+  int bx, by, bz;  // bx * by * bz = threads per block
+};
+template <int D>
+__device__ __forceinline__ bool brick_cell(const Brick& B, const InstK& I, const BrickGeo& g, int t, uint32_t* F) {
+  const int lx = t % g.bx, ly = (t / g.bx) % g.by, lz = t / (g.bx * g.by);
+  const int x = B.x0 + lx, y = B.y0 + ly, z = B.z0 + lz;
+  if (lz >= g.bz || x >= I.dims[0] || y >= I.dims[1] || (D == 3 && z >= I.dims[2])) return false;
+  *F = I.base + (uint32_t)x + (uint32_t)I.dims[0] * ((uint32_t)y + (D == 3 ? (uint32_t)I.dims[1] * (uint32_t)z : 0u));
+  return true;
+}
+
 // (1/sw, f*_k) of one component: what a resampling hit reads, in one load.
 template <class real>
 struct alignas(2 * sizeof(real)) KV {
