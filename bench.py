@@ -545,6 +545,12 @@ def sphere_leg(steps=20, steps64=4):
                          moment_capacity=int(1.2 * len(x)))
         sim.set_state(None, x, f)
         m0 = float(sim.conservation()[0, 0])
+        if prec == "fp32dev":  # brick width of the untiled 3D kernels, by timing (results do not depend on it)
+            from direbm_gb300.autotune import autotune
+
+            out["brick_width"] = autotune(sim, steps=1, use_cache=False)["brick_width"]
+        else:
+            sim.set_brick_width(out["brick_width"])
         sim.step(1)  # warm-up (graph capture)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

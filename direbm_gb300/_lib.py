@@ -109,6 +109,7 @@ _SIGS = {
     "dbm_sim_trace": (ctypes.c_int, [_vp, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp]),
     "dbm_sim_device_bytes": (_i64, [_vp]),
     "dbm_sim_get_tiling": (ctypes.c_int, [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
+    "dbm_sim_get_brick_width": (ctypes.c_int, [_vp, ctypes.POINTER(_i32)]),
     "dbm_sim_set_tau": (ctypes.c_int, [_vp, _vp, _i32]),
     "dbm_sim_set_obstacle": (ctypes.c_int, [_vp, _i32, _vp, _f64]),
     "dbm_sim_set_inflow": (ctypes.c_int, [_vp, _i32, _vp, _i32]),

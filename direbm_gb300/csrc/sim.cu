@@ -764,8 +764,9 @@ __device__ __forceinline__ void gather_one(const Args<Q, D, P>& A, const uint32_
 }
 
 template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_weights(const __grid_constant__ Args<Q, D, P> A,
-                                                 const Brick* __restrict__ bricks, int nbricks, BrickGeo bg) {
+__global__ void __launch_bounds__(256, gather_min_blocks<P>()) k_weights(const __grid_constant__ Args<Q, D, P> A,
+                                                                         const Brick* __restrict__ bricks, int nbricks,
+                                                                         BrickGeo bg) {
   const int k = blockIdx.y;
   for (int bi = blockIdx.x; bi < nbricks; bi += gridDim.x) {
     const Brick B = bricks[bi];
@@ -1261,24 +1262,49 @@ struct SimImpl : SimBase {
     DBM_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
-    // bricks of 256 cells: 8 x 8 x 4 in 3D, 16 x 16 in 2D
-    bgeo = D == 3 ? BrickGeo{8, 8, 4} : BrickGeo{16, 16, 1};
-    {
-      std::vector<Brick> bl;
-      for (int i = 0; i < (int)inst_h.size(); ++i) {
-        const int* dm = inst_h[i].dims;
-        for (int z0 = 0; z0 < (D == 3 ? dm[2] : 1); z0 += bgeo.bz)
-          for (int y0 = 0; y0 < dm[1]; y0 += bgeo.by)
-            for (int x0 = 0; x0 < dm[0]; x0 += bgeo.bx) bl.push_back({i, x0, y0, z0});
-      }
-      if (bl.size() >= 0x7fffffffu) { set_last_error("too many bricks"); return DBM_ERR_CAPACITY; }
-      nbricks = (int)bl.size();
-      DBM_TRY(alloc(&d_bricks, nbricks));
-      DBM_CUDA(cudaMemcpy(d_bricks, bl.data(), sizeof(Brick) * bl.size(), cudaMemcpyHostToDevice));
-    }
+    DBM_TRY(set_brick(D == 3 ? 8 : 16));  // 8 x 8 x 4 in 3D, 16 x 16 in 2D
     if (!tiled) DBM_TRY(ensure_untiled());  // 3D: always the untiled window kernels
     return DBM_OK;
   }
+
+  // Bricks of 256 cells for the untiled window kernels, bx cells along x: 2D bx x (256 / bx); 3D the
+  // other 256 / bx cells split between y and z, y taking the larger half.  Results do not depend
+  // on the shape (each point's work is the same); only the L1 locality of a block does.
+  int set_brick(int bx) override {
+    const int minx = D == 3 ? 4 : 8, maxx = D == 3 ? 32 : 64;
+    if (bx < minx || bx > maxx || (bx & (bx - 1))) {
+      set_last_error("brick width %d: a power of two in %d..%d", bx, minx, maxx);
+      return DBM_ERR_INVALID;
+    }
+    BrickGeo g{bx, 256 / bx, 1};
+    if (D == 3) {
+      const int rest = 256 / bx;
+      int bz = 1;
+      while ((2 * bz) * (2 * bz) <= rest) bz *= 2;  // the largest power of two with bz^2 <= rest
+      g.bz = bz;
+      g.by = rest / bz;
+    }
+    std::vector<Brick> bl;
+    for (int i = 0; i < (int)inst_h.size(); ++i) {
+      const int* dm = inst_h[i].dims;
+      for (int z0 = 0; z0 < (D == 3 ? dm[2] : 1); z0 += g.bz)
+        for (int y0 = 0; y0 < dm[1]; y0 += g.by)
+          for (int x0 = 0; x0 < dm[0]; x0 += g.bx) bl.push_back({i, x0, y0, z0});
+    }
+    if (bl.size() >= 0x7fffffffu) { set_last_error("too many bricks"); return DBM_ERR_CAPACITY; }
+    if (d_bricks) {
+      if (own) DBM_CUDA(cudaStreamSynchronize(own));  // no step may still read the old list
+      release(d_bricks);
+      d_bricks = nullptr;
+    }
+    DBM_TRY(alloc(&d_bricks, (int64_t)bl.size()));
+    DBM_CUDA(cudaMemcpy(d_bricks, bl.data(), sizeof(Brick) * bl.size(), cudaMemcpyHostToDevice));
+    nbricks = (int)bl.size();
+    bgeo = g;
+    invalidate_graphs();  // captured launches hold the list and its size
+    return DBM_OK;
+  }
+  int brick_width() const override { return bgeo.bx; }
 
   // Per-component buffers that only the untiled window kernels use: (1/sw, f*) pairs and exp(f*)
   // ([Q][mcap] each).  Allocated by the calls that make that path possible (creation in 3D, an
@@ -2073,6 +2099,8 @@ int dbm_sim_set_option(dbm_sim* s, int32_t option, int32_t value) {
     return s->impl->set_tiling_v(tx, pers);
   } else if (option == DBM_OPT_KAPPA_SOFT) {
     return s->impl->set_soft_spawn(value);
+  } else if (option == DBM_OPT_BRICK_WIDTH) {
+    return s->impl->set_brick(value);
   } else {
     set_last_error("dbm_sim_set_option: unknown option %d", option);
     return DBM_ERR_INVALID;
@@ -2092,6 +2120,12 @@ int dbm_sim_trace(dbm_sim* s, int32_t what, void* dst, int64_t bytes, int64_t* n
 int64_t dbm_sim_device_bytes(dbm_sim* s) {
   if (!s || !s->impl) return -1;
   return s->impl->device_bytes();
+}
+int dbm_sim_get_brick_width(dbm_sim* s, int32_t* brick_width) {
+  SIM_CHECK(s);
+  if (!brick_width) return DBM_ERR_INVALID;
+  *brick_width = s->impl->brick_width();
+  return DBM_OK;
 }
 int dbm_sim_get_tiling(dbm_sim* s, int32_t* tile_width, int32_t* persistent) {
   SIM_CHECK(s);

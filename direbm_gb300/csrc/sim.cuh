@@ -340,6 +340,8 @@ struct SimBase {
   virtual int set_tiling_v(int tx, int persistent) = 0;
   virtual int set_soft_spawn(int kappa_soft) = 0;
   virtual int ensure_untiled() = 0;
+  virtual int set_brick(int bx) = 0;
+  virtual int brick_width() const = 0;
   int kappa_soft = 0;  // soft-outer spawn threshold (0: off)
   int use_graphs = 1;
   int use_tiles = 1;

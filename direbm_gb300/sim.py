@@ -271,7 +271,7 @@ class Simulation:
         self.instances[inst].inflow = (tuple(v), int(width)) if width > 0 else None
 
     # ---- launch configuration -------------------------------------------------------------------
-    OPT_TILE_WIDTH, OPT_PERSISTENT, OPT_KAPPA_SOFT = 3, 4, 5
+    OPT_TILE_WIDTH, OPT_PERSISTENT, OPT_KAPPA_SOFT, OPT_BRICK_WIDTH = 3, 4, 5, 6
 
     def tiling(self) -> tuple:
         """(tile width in cells, persistent launches) of the 2D tiled kernels."""
@@ -288,6 +288,19 @@ class Simulation:
             if persistent is not None:
                 _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_PERSISTENT, 1 if persistent else 0),
                            "set persistent")
+
+    def brick_width(self) -> int:
+        """Cells along x of the 256-cell bricks the untiled window kernels give each block."""
+        w = ctypes.c_int32()
+        _lib.check(self.lib.dbm_sim_get_brick_width(self._h, ctypes.byref(w)), "dbm_sim_get_brick_width")
+        return int(w.value)
+
+    def set_brick_width(self, width: int):
+        """Bricks of width x (256 / width) cells (2D) or width x by x bz (3D) for the untiled window
+        kernels (3D, obstacles, the soft spawn, tiles off).  Results are bit-identical for every
+        width; only the speed changes."""
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_BRICK_WIDTH, int(width)), "set brick width")
 
     def set_soft_spawn(self, kappa_soft: int):
         """Soft-outer spawn (the CPU simulator's soft_mode="spawn", direbm/reference/simulator.py:

@@ -181,6 +181,11 @@ int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
  * r (none when that sum is below 1e-8).  Needs a moment capacity of 2 x cells (DBM_ERR_CAPACITY
  * otherwise); runs on the untiled kernels; the tape (dbm_tape_*) refuses a simulator with it on. */
 #define DBM_OPT_KAPPA_SOFT 5
+/* DBM_OPT_BRICK_WIDTH: the untiled window kernels (3D, obstacles, the soft spawn, tiles off) give
+ * each block a brick of 256 cells, this many along x (a power of two, 4..32 in 3D, 8..64 in 2D;
+ * default 8 in 3D, 16 in 2D); results do not depend on it.  direbm_gb300.autotune picks it. */
+#define DBM_OPT_BRICK_WIDTH 6
+int dbm_sim_get_brick_width(dbm_sim* sim, int32_t* brick_width);
 int dbm_sim_set_option(dbm_sim* sim, int32_t option, int32_t value);
 int dbm_sim_get_tiling(dbm_sim* sim, int32_t* tile_width, int32_t* persistent);
 /* Run one step but stop after `stage` (1 collide, 2 thin+refine, 3 sort, 4 weights, 5 gather,

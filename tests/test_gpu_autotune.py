@@ -73,3 +73,47 @@ def test_autotuner_picks_a_candidate_keeps_the_state_and_caches(tmp_path, monkey
     sim.set_tiling(32, False)
     again = autotune.autotune(sim, steps=2)
     assert again["cached"] and sim.tiling() == (choice["tile_width"], choice["persistent"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_every_brick_width_gives_the_same_bits(precision):
+    """The untiled window kernels (3D here, and 2D with tiles off) give each block a brick of cells;
+    every brick width yields the same bits, and the 3D autotuner picks one of its candidates."""
+    from direbm_gb300 import autotune
+
+    x, f = periodic_tg(12, "D3Q19", seed=6, u0=0.04)
+    sim = _make("D3Q19", [{"dims": (12, 12, 12)}], 1.0, 1.5, 1.0, precision, x, f)
+    snap = sim.snapshot()
+    assert sim.brick_width() == 8
+    ref = None
+    for w in (4, 8, 16, 32):
+        sim.set_brick_width(w)
+        assert sim.brick_width() == w
+        sim.restore(snap)
+        sim.step(3)
+        out = [t.cpu().numpy() for t in sim.state()]
+        if ref is None:
+            ref = out
+        else:
+            for a, b in zip(out, ref):
+                np.testing.assert_array_equal(a, b, err_msg=f"brick {w}")
+    sim.restore(snap)
+    choice = autotune.autotune(sim, steps=1, use_cache=False)
+    assert choice["brick_width"] in autotune.BRICK_CANDIDATES and sim.brick_width() == choice["brick_width"]
+    x2, f2 = periodic_tg(40, "D2Q9", seed=7)
+    sim2 = _make("D2Q9", [{"dims": (40, 40)}], 1.0, 1.5, 1.0, precision, x2, f2)
+    sim2.lib.dbm_sim_set_option(sim2.handle, 2, 0)  # tiles off: the untiled kernels in 2D
+    snap2 = sim2.snapshot()
+    ref2 = None
+    for w in (8, 16, 64):
+        sim2.set_brick_width(w)
+        sim2.restore(snap2)
+        sim2.step(2)
+        out = [t.cpu().numpy() for t in sim2.state()]
+        if ref2 is None:
+            ref2 = out
+        else:
+            for a, b in zip(out, ref2):
+                np.testing.assert_array_equal(a, b, err_msg=f"2D brick {w}")
+    with pytest.raises(Exception):
+        sim2.set_brick_width(12)
