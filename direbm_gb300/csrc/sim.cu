@@ -1078,6 +1078,12 @@ struct SimImpl : SimBase {
   Tile2* d_tiles = nullptr;
   int ntiles = 0;
   int pgrid[3] = {1, 1, 1};  // persistent grids: thin+refine, weights, gather
+  // whole-cell displacements (FP32 store, R < 2 cells): the gather builds one window-row table per
+  // control point for all directions (k_gather_ts); geo_s is geo with that kernel's staging capacity
+  bool shift_ok = false;
+  int pgrid_s = 1, pgrid_rs = 1, pgrid_ws = 1;
+  TileGeo geo_s{};
+  size_t sm_gather_s = 0;
   int use_persistent = 0;
   TileGeo geo{};
   size_t sm_refine = 0, sm_weights = 0, sm_gather = 0;
@@ -1336,11 +1342,16 @@ struct SimImpl : SimBase {
       const size_t rh = geo.ty + geo.cp.yh - geo.cp.yl;
       return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4 * rs}, {(size_t)2 * geo.ty + 2, 4}, {ct, 4},
                           {ct, 2}, {ct, 2}, {ct, 2 * rs}});
-    } else {  // gather
+    } else if (kind == 2) {  // gather
       const size_t cells = (size_t)(geo.tx + geo.mom.xh - geo.mom.xl) * (geo.ty + geo.mom.yh - geo.mom.yl);
       const size_t rh = geo.ty + geo.mom.yh - geo.mom.yl;
       return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4}, {cp, 4 * rs}, {cp, rs}, {cp, 2 * rs},
                           {(size_t)2 * geo.ty + 2, 4}, {ct, 4}, {ct, 2}, {ct, 2}, {ct, 2 * rs}});
+    } else {  // gather with whole-cell displacements (FP32): 32-byte records
+      const size_t cells = (size_t)(geo.tx + geo.mom.xh - geo.mom.xl) * (geo.ty + geo.mom.yh - geo.mom.yl);
+      const size_t rh = geo.ty + geo.mom.yh - geo.mom.yl;
+      return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4}, {cp, 32}, {(size_t)2 * geo.ty + 2, 4},
+                          {ct, 4}, {ct, 2}, {ct, 2}, {ct, 8}});
     }
   }
   int pick_cap(int kind, int cells, size_t budget) const {
@@ -1389,6 +1400,18 @@ struct SimImpl : SimBase {
     sm_refine = smem_for(0, geo.cap_refine);
     sm_weights = smem_for(1, geo.cap_weights);
     sm_gather = smem_for(2, geo.cap_gather);
+    // whole-cell displacements: every c * dx / cell an integer (in FP64 and in its FP32 rounding)
+    shift_ok = std::is_same<P, PF32>::value && R < 1.99;
+    for (int k = 0; k < Q && shift_ok; ++k)
+      for (int a = 0; a < 2; ++a) {
+        const double cd64 = LH.c[k][a] * desc.dx / desc.cell;
+        shift_ok = shift_ok && cd64 == std::nearbyint(cd64) && (double)(float)cd64 == cd64 && std::fabs(cd64) <= 8.0;
+      }
+    geo_s = geo;
+    if (shift_ok) {
+      geo_s.cap_gather = pick_cap(3, mcells, budget);
+      sm_gather_s = smem_for(3, geo_s.cap_gather);
+    }
     std::vector<Tile2> tiles;
     for (int i = 0; i < (int)inst_h.size(); ++i)
       for (int y0 = 0; y0 < inst_h[i].dims[1]; y0 += geo.ty)
@@ -1412,6 +1435,25 @@ struct SimImpl : SimBase {
       DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[1], k_weights_t<Q, P>, 256, sm_weights));
       DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb[2], k_gather_t<Q, P>, 256, sm_gather));
       for (int i = 0; i < 3; ++i) pgrid[i] = std::max(1, std::min(ntiles, std::max(nb[i], 1) * sm_count()));
+      if constexpr (std::is_same<P, PF32>::value) {
+        if (shift_ok) {
+          DBM_CUDA(cudaFuncSetAttribute((const void*)k_gather_ts<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm_gather_s));
+          int nbs = 1;
+          DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbs, k_gather_ts<Q>, 256, sm_gather_s));
+          pgrid_s = std::max(1, std::min(ntiles, std::max(nbs, 1) * sm_count()));
+          DBM_CUDA(cudaFuncSetAttribute((const void*)k_thin_refine_t<Q, P, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_refine));
+          int nbr = 1;
+          DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbr, k_thin_refine_t<Q, P, true>, 256, sm_refine));
+          pgrid_rs = std::max(1, std::min(ntiles, std::max(nbr, 1) * sm_count()));
+          DBM_CUDA(cudaFuncSetAttribute((const void*)k_weights_t<Q, P, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_weights));
+          int nbw = 1;
+          DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbw, k_weights_t<Q, P, true>, 256, sm_weights));
+          pgrid_ws = std::max(1, std::min(ntiles, std::max(nbw, 1) * sm_count()));
+        }
+      }
     }
     tiled = true;
     return DBM_OK;
@@ -1565,9 +1607,20 @@ struct SimImpl : SimBase {
     mark(1, s);
     if (upto <= 1) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled_path())
-        k_thin_refine_t<Q, P><<<use_persistent ? pgrid[0] : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo, ntiles);
-      else k_thin_refine<Q, D, P><<<nbricks, 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
+      if (tiled_path()) {
+        bool shifted = false;
+        if constexpr (std::is_same<P, PF32>::value) {
+          if (shift_ok && use_shift) {
+            k_thin_refine_t<Q, P, true><<<use_persistent ? pgrid_rs : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo,
+                                                                                                  ntiles);
+            shifted = true;
+          }
+        }
+        if (!shifted)
+          k_thin_refine_t<Q, P><<<use_persistent ? pgrid[0] : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo, ntiles);
+      } else {
+        k_thin_refine<Q, D, P><<<nbricks, 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
+      }
     } else {
       k_thin_refine<Q, D, P><<<nbricks, 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     }
@@ -1609,9 +1662,20 @@ struct SimImpl : SimBase {
     mark(3, s);
     if (upto <= 3) return DBM_OK;
     if constexpr (D == 2) {
-      if (tiled_path())
-        k_weights_t<Q, P><<<use_persistent ? pgrid[1] : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo, ntiles);
-      else k_weights<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
+      if (tiled_path()) {
+        bool shifted = false;
+        if constexpr (std::is_same<P, PF32>::value) {
+          if (shift_ok && use_shift) {
+            k_weights_t<Q, P, true><<<use_persistent ? pgrid_ws : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo,
+                                                                                               ntiles);
+            shifted = true;
+          }
+        }
+        if (!shifted)
+          k_weights_t<Q, P><<<use_persistent ? pgrid[1] : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo, ntiles);
+      } else {
+        k_weights<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
+      }
     } else {
       k_weights<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     }
@@ -1620,9 +1684,19 @@ struct SimImpl : SimBase {
     if (upto <= 4) return DBM_OK;
     DBM_CUDA(cudaMemsetAsync(A.emask, 0, (size_t)ccap * 4, s));
     if constexpr (D == 2) {
-      if (tiled_path())
-        k_gather_t<Q, P><<<use_persistent ? pgrid[2] : ntiles, 256, sm_gather, s>>>(A, d_tiles, geo, ntiles);
-      else k_gather<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
+      if (tiled_path()) {
+        bool shifted = false;
+        if constexpr (std::is_same<P, PF32>::value) {
+          if (shift_ok && use_shift) {
+            k_gather_ts<Q><<<use_persistent ? pgrid_s : ntiles, 256, sm_gather_s, s>>>(A, d_tiles, geo_s, ntiles);
+            shifted = true;
+          }
+        }
+        if (!shifted)
+          k_gather_t<Q, P><<<use_persistent ? pgrid[2] : ntiles, 256, sm_gather, s>>>(A, d_tiles, geo, ntiles);
+      } else {
+        k_gather<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
+      }
     } else {
       k_gather<Q, D, P><<<dim3(nbricks, Q), 256, 0, s>>>(A, d_bricks, nbricks, bgeo);
     }
@@ -2101,6 +2175,8 @@ int dbm_sim_set_option(dbm_sim* s, int32_t option, int32_t value) {
     return s->impl->set_soft_spawn(value);
   } else if (option == DBM_OPT_BRICK_WIDTH) {
     return s->impl->set_brick(value);
+  } else if (option == DBM_OPT_SHIFTED_WINDOWS) {
+    s->impl->use_shift = value ? 1 : 0;
   } else {
     set_last_error("dbm_sim_set_option: unknown option %d", option);
     return DBM_ERR_INVALID;

@@ -345,6 +345,7 @@ struct SimBase {
   int kappa_soft = 0;  // soft-outer spawn threshold (0: off)
   int use_graphs = 1;
   int use_tiles = 1;
+  int use_shift = 1;  // DBM_OPT_SHIFTED_WINDOWS
   uint64_t version = 0;  // bumped by every change of the state (load, step, restore)
   int lattice = 0;
   int precision = 0;

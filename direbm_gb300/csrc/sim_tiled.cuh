@@ -348,7 +348,82 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
 // narrowing only drops cells with no hit, so sums (and their order) are those of the per-cell
 // loops.
 
-template <int Q, class P>
+// Rows of the whole-cell window tables: NR >= floor(2R + 2 tiny) + 2 (R < 2 cells).
+constexpr int kShiftRows = 5;
+
+template <int NR>
+struct WinRows {
+  int jlo, nr;
+  float cy[NR];
+  int a[NR], b[NR];
+};
+
+template <int NR, class ArgsT>
+__device__ __forceinline__ void win_rows(const ArgsT& A, Pair<float> p, WinRows<NR>& w) {
+  w.jlo = (int)floorf(p.y - A.R - A.tiny);
+  const int n = (int)floorf(p.y + A.R + A.tiny) - w.jlo + 1;
+  if (n > NR) atomicOr(A.status, ST_INTERNAL);  // the host sizes NR for R; never expected
+  w.nr = min(n, NR);
+#pragma unroll
+  for (int t = 0; t < NR; ++t) {
+    const float cy = rn_sub((float)(w.jlo + t), p.y);
+    const float hw = row_halfwidth<float>(A.R2, axis_lower<float>(cy));
+    w.cy[t] = cy;
+    const bool on = t < w.nr && hw >= 0.f;
+    w.a[t] = on ? (int)floorf(p.x - hw - A.tiny) : 1;
+    w.b[t] = on ? (int)floorf(p.x + hw + A.tiny) : 0;
+  }
+}
+
+// The refine sums of one centroid over the shifted windows of every direction (FP32 store): the
+// loop of thin_refine_rows with the row table built once.
+template <int Q, int NR>
+__device__ __forceinline__ void refine_shift(const Args<Q, 2, PF32>& A, int rw, int rh, const int* s_beg,
+                                             const int* s_end, const Item<float>* s_it, const float* s_w, int cap,
+                                             int bx, int by, Pair<float> c, uint32_t& mask, float& swf,
+                                             float (&sxf)[2]) {
+  WinRows<NR> w;
+  win_rows<NR>(A, c, w);
+  float2 sx = make_float2(sxf[0], sxf[1]);
+#pragma unroll 1
+  for (int k = 0; k < Q; ++k) {
+    const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
+    const float cxo = (float)(cdx - bx);
+    const float* wk = s_w + k * cap;
+    bool hit = false;
+#pragma unroll
+    for (int t = 0; t < NR; ++t) {
+      if (t >= w.nr) break;
+      const int ry = by + w.jlo + t - cdy;
+      const int lo = max(w.a[t] - cdx, -bx), hi = min(w.b[t] - cdx, rw - 1 - bx);
+      if (ry < 0 || ry >= rh || lo > hi) continue;
+      const int row = ry * rw + bx;
+      const int m1 = s_end[row + hi];
+      const float cy = w.cy[t];
+      for (int m = s_beg[row + lo]; m < m1; ++m) {
+        const Item<float> it = s_it[m];
+        const float cx = rn_sub(rn_add(it.rx, cxo), c.x);
+        const float2 e = __fadd2_rn(make_float2(it.ox, it.oy), make_float2(cx, cy));
+        const float2 e2 = __fmul2_rn(e, e);
+        if (rn_add(e2.x, e2.y) <= A.R2) {
+          hit = true;
+          const float wt = wk[m];
+          swf = __fadd_rn(swf, wt);
+          sx = __ffma2_rn(make_float2(wt, wt), e, sx);
+        }
+      }
+    }
+    if (hit) mask |= 1u << k;
+  }
+  sxf[0] = sx.x;
+  sxf[1] = sx.y;
+}
+
+
+// SHIFT (FP32 store, whole-cell displacements): the refine windows come from one row table of
+// the centroid, shifted per direction (see WinRows below); bit-identical to the per-direction
+// windows.
+template <int Q, class P, bool SHIFT = false>
 __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const InstK& I, const Tile2& T,
                                                  const TileGeo& G, int rw, int rh, const int* s_beg, const int* s_end,
                                                  const Item<typename P::real>* s_it, const typename P::real* s_w,
@@ -417,6 +492,10 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
   uint32_t mask = 0;
   double swd = 0, sxd[2] = {0, 0};
   float swf = 0.f, sxf[2] = {0.f, 0.f};
+  if constexpr (SHIFT) {
+    static_assert(!F64, "the shifted windows serve the FP32 store");
+    refine_shift<Q, kShiftRows>(A, rw, rh, s_beg, s_end, s_it, s_w, cap, bx, by, Pair<float>{cen[0], cen[1]}, mask, swf, sxf);
+  } else {
 #pragma unroll 1
   for (int k = 0; k < Q; ++k) {
     const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
@@ -452,6 +531,7 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
         }
       }
     }
+  }
   }
   const int kappa = __popc(mask);
   real np[2];
@@ -500,7 +580,7 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
 // blockIdx.x + gridDim.x, ...): launched with one block per tile they are ordinary kernels;
 // launched with fewer blocks (a few per SM) they are persistent.  Either way each tile is processed
 // by one block with the same per-thread loop order, so results do not depend on the launch.
-template <int Q, class P>
+template <int Q, class P, bool SHIFT = false>
 __global__ void __launch_bounds__(256) k_thin_refine_t(const __grid_constant__ Args<Q, 2, P> A,
                                                       const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
   using real = typename P::real;
@@ -523,7 +603,7 @@ __global__ void __launch_bounds__(256) k_thin_refine_t(const __grid_constant__ A
                  for (int k = 0; k < Q; ++k) s_w[k * cap + l] = exp(fstar_at<Q, 2, P>(A, (uint32_t)gm, k));
                });
   if (s_row[rh + 1]) {
-    thin_refine_rows<Q, P>(A, I, T, G, rw, rh, s_beg, s_end, s_it, s_w, cap);
+    thin_refine_rows<Q, P, SHIFT>(A, I, T, G, rw, rh, s_beg, s_end, s_it, s_w, cap);
   } else {
     thin_refine_body<Q, P, false>(A, I, T, G, rw, rh, s_beg, s_end, nullptr, nullptr, nullptr, 0);
   }
@@ -709,7 +789,79 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
   }
 }
 
-template <int Q, class P>
+// Weights with whole-cell displacements (FP32 store, shared-memory mode): one thread per moment,
+// all directions.  Component (m, k) sits at the moment's offset o plus cd_k; its control-point
+// window rows, relative to the component's cell, depend on o alone: row u (a control point row
+// gy = u + cd_k,y) has base_y = float(-u), the same lower bound on |e_y| and the same half-width,
+// and the column range [cd_k,x + a_u, cd_k,x + b_u].  One table per moment serves all
+// directions; the window margins are far above the rounding of o + cd, and each direction's
+// control points are visited in the same order, so sums are bit-identical to weights_rows.
+template <int Q, int NR>
+__device__ __forceinline__ void weights_rows_shift(const Args<Q, 2, PF32>& A, const InstK& I, const Tile2& T,
+                                                   const TileGeo& G, int rw, int rh, const int* s_beg,
+                                                   const int* s_end, const Item<float>* s_cit, int* s_tr, int* s_ij,
+                                                   short* s_bx, short* s_by, Pair<float>* s_mpos) {
+  const int cap_t = G.cap_tile;
+  for (int c0 = 0;; c0 += cap_t) {
+    const int n = tile_items<float>(I, T, G, G.cp, A.a.start, A.a.cell, A.a.off, A.mcap, c0, cap_t, s_tr, s_ij,
+                                    s_bx, s_by, s_mpos);
+    const int nc = min(cap_t, n - c0);
+    for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+      const int bx = s_bx[i], by = s_by[i];
+      const Pair<float> o = s_mpos[i];
+      // the row table of the moment: rows u in [ulo, ulo + nr)
+      const int ulo = (int)floorf(o.y - A.R - A.tiny);
+      const int nrow = (int)floorf(o.y + A.R + A.tiny) - ulo + 1;
+      if (nrow > NR) atomicOr(A.status, ST_INTERNAL);  // the host sizes NR for R; never expected
+      const int nr = min(nrow, NR);
+      float by_[NR];
+      int a_[NR], b_[NR];
+#pragma unroll
+      for (int t = 0; t < NR; ++t) {
+        const float basey = (float)(-(ulo + t));
+        const float ely = rn_add(o.y, rn_sub(basey, 1.f)), ehy = rn_add(o.y, basey);
+        const float lby = ely > 0.f ? ely : (ehy < 0.f ? -ehy : 0.f);
+        const float hw = row_halfwidth<float>(A.R2, lby);
+        by_[t] = basey;
+        const bool on = t < nr && hw >= 0.f;
+        a_[t] = on ? (int)floorf(o.x - hw - A.tiny) : 1;
+        b_[t] = on ? (int)floorf(o.x + hw + A.tiny) : 0;
+      }
+      const int j = s_ij[i];
+#pragma unroll 1
+      for (int k = 0; k < Q; ++k) {
+        const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
+        const float bxc = (float)(bx + cdx);  // base_x of a control point in region column rx = bxc - rx
+        CSum sws;
+#pragma unroll
+        for (int t = 0; t < NR; ++t) {
+          if (t >= nr) break;
+          const int ry = by + ulo + t + cdy;
+          const int lo = max(a_[t] + cdx, -bx), hi = min(b_[t] + cdx, rw - 1 - bx);
+          if (ry < 0 || ry >= rh || lo > hi) continue;
+          const int row = ry * rw + bx;
+          const int c1 = s_end[row + hi];
+          const float basey = by_[t];
+          for (int c = s_beg[row + lo]; c < c1; ++c) {
+            const Item<float> it = s_cit[c];
+            const float basex = rn_sub(bxc, it.rx);  // float(cd_x - dG_x), exact
+            const float2 q = __fadd2_rn(make_float2(basex, basey), make_float2(-it.ox, -it.oy));
+            const float2 e = __fadd2_rn(make_float2(o.x, o.y), q);
+            const float2 e2 = __fmul2_rn(e, e);
+            const float d2 = rn_add(e2.x, e2.y);
+            if (d2 <= A.R2) sws.add(A.R - rn_sqrt(d2));
+          }
+        }
+        const float sw = sws.value();
+        A.sw[(int64_t)k * A.mcap + j] = sw > 0.f ? 1.f / sw : 0.f;
+      }
+    }
+    if (c0 + cap_t >= n) break;
+    __syncthreads();
+  }
+}
+
+template <int Q, class P, bool SHIFT = false>
 __global__ void __launch_bounds__(256) k_weights_t(const __grid_constant__ Args<Q, 2, P> A,
                                                   const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
   using real = typename P::real;
@@ -733,7 +885,11 @@ __global__ void __launch_bounds__(256) k_weights_t(const __grid_constant__ Args<
                [&](int gc, int l, int rx) {
                  s_cit[l] = Item<real>{A.b.off[gc], A.b.off[A.ccap + gc], (real)rx, (real)0};
                });
-  if (s_row[rh + 1]) weights_rows<Q, P>(A, I, T, G, rw, rh, s_beg, s_end, s_cit, s_tr, s_ij, s_bx, s_by, s_mpos);
+  if (s_row[rh + 1]) {
+    if constexpr (SHIFT) weights_rows_shift<Q, kShiftRows>(A, I, T, G, rw, rh, s_beg, s_end, s_cit, s_tr, s_ij, s_bx,
+                                                           s_by, s_mpos);
+    else weights_rows<Q, P>(A, I, T, G, rw, rh, s_beg, s_end, s_cit, s_tr, s_ij, s_bx, s_by, s_mpos);
+  }
   else weights_body<Q, P, false>(A, I, T, G, rw, rh, s_beg, s_end, nullptr, s_tr, s_ij, s_bx, s_by, s_mpos);
   __syncthreads();
   }
@@ -922,6 +1078,157 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
       }
     }
     if (c0 + cap_t >= n) break;
+    __syncthreads();
+  }
+}
+
+// ---- whole-cell displacements: one window-row table per reference point ------------------------
+//
+// When every displacement cd_k is a whole number of cells (D2Q9 with dx = cell), the canonical
+// c = (float(dS) + cd_k) - p of a window cell is rn_sub(float(j), p) with j = dS + cd_k exact, so
+// direction k's window around a reference point p is the window of cd = 0 shifted by -cd_k:
+// component row j (relative to p's cell) has the same c_y, the same half-width bound and the
+// same column range [a_j, b_j] for every direction; only the moment row j - cd_k,y and the moment
+// columns [a_j - cd_k,x, b_j - cd_k,x] move.  The table of rows is built once per reference point
+// instead of once per (point, direction).  The window bounds keep their 1e-4 cell margin, which
+// is far above the rounding of p - cd, so every hit lies inside the shifted window and the hits
+// are visited in the same order (rows ascending, then the row's items): sums are bit-identical to
+// the per-direction windows.
+// A staged moment for the whole-cell gather: offsets, region column (exact small integer), rho,
+// then (1/sw, f*_k) of the direction being gathered, so a hit reads its operands at a fixed
+// offset from the candidate it just tested.
+struct alignas(16) GRec {
+  float ox, oy, rx, rho;
+  float inv, f, pad0, pad1;
+};
+
+// One control point, one direction (FP32 store): the gather_rows sum over the shifted rows.
+template <int Q, int NR>
+__device__ __forceinline__ void gather_cp_shift(const Args<Q, 2, PF32>& A, int k, int cdx, int cdy, int rw, int rh,
+                                                const int* s_beg, const int* s_end, const GRec* s_rec, int bx,
+                                                int by, Pair<float> pp, const WinRows<NR>& w, int j) {
+  const float cxo = (float)(cdx - bx);  // region column + cxo = float(dS_x + cd_x), exact
+  CSum sa;
+  float sb = 0.f;  // deviation part: plain FMA accumulation, as in gather_rows
+#pragma unroll
+  for (int t = 0; t < NR; ++t) {
+    if (t >= w.nr) break;
+    const int ry = by + w.jlo + t - cdy;
+    const int lo = max(w.a[t] - cdx, -bx), hi = min(w.b[t] - cdx, rw - 1 - bx);
+    if (ry < 0 || ry >= rh || lo > hi) continue;
+    const int row = ry * rw + bx;
+    const GRec* it = s_rec + s_beg[row + lo];
+    const GRec* const end = s_rec + s_end[row + hi];
+    const float cy = w.cy[t];
+    for (; it < end; ++it) {
+      const float4 a = *reinterpret_cast<const float4*>(it);
+      const float cx = rn_sub(rn_add(a.z, cxo), pp.x);
+      const float2 e = __fadd2_rn(make_float2(a.x, a.y), make_float2(cx, cy));
+      const float2 e2 = __fmul2_rn(e, e);
+      const float d2 = rn_add(e2.x, e2.y);
+      if (d2 <= A.R2) {
+        // A dropped component has 1/sw = 0: its weight is +0 and every sum below is unchanged
+        // (the sums are >= +0 and f is finite), so it needs no test of its own.
+        const float2 kv = *reinterpret_cast<const float2*>(&it->inv);
+        const float wgt = (A.R - rn_sqrt(d2)) * kv.x;
+        // CSum::add_prod(wgt, rho) and the deviation FMA, the two FMAs as one paired op
+        const float p = __fmul_rn(wgt, a.w);
+        const float2 r = __ffma2_rn(make_float2(wgt, wgt), make_float2(a.w, kv.y), make_float2(-p, sb));
+        sa.add(p);
+        sa.lo = __fadd_rn(sa.lo, r.x);
+        sb = r.y;
+      }
+    }
+  }
+  const DF Ad = df_norm(sa.hi, sa.lo);
+  const DF Fv = df_add(df_mul(DF{A.L.wf[k], A.L.wlo[k]}, Ad), DF{sb, 0.f});
+  A.cpfhi[(int64_t)k * A.ccap + j] = Fv.hi;
+  A.cpflo[(int64_t)k * A.ccap + j] = Fv.lo;
+  if (Fv.hi < A.eps) atomicOr(A.emask + j, 1u << k);
+}
+
+// Gather with whole-cell displacements (FP32 store, shared-memory mode).  Each thread keeps the
+// row table of its first control point in registers across the nine directions; a tile with more
+// control points than threads builds the extra points' tables per direction.
+template <int Q, int NR>
+__device__ __forceinline__ void gather_rows_shift(const Args<Q, 2, PF32>& A, const InstK& I, const Tile2& T,
+                                                  const TileGeo& G, int rw, int rh, const int* s_beg,
+                                                  const int* s_end, const int* s_gi, GRec* s_rec, int nstaged,
+                                                  int* s_tr, int* s_ij, short* s_bx, short* s_by,
+                                                  Pair<float>* s_cpos) {
+  const int cap_t = G.cap_tile;
+  for (int c0 = 0;; c0 += cap_t) {
+    const int n = tile_items<float>(I, T, G, G.mom, A.b.start, A.b.cell, A.b.off, A.ccap, c0, cap_t, s_tr, s_ij,
+                                    s_bx, s_by, s_cpos);
+    const int nc = min(cap_t, n - c0);
+    const int i0 = threadIdx.x;
+    const bool has0 = i0 < nc;
+    WinRows<NR> w0;
+    int bx0 = 0, by0 = 0, j0 = 0;
+    Pair<float> p0{0.f, 0.f};
+    if (has0) {
+      bx0 = s_bx[i0];
+      by0 = s_by[i0];
+      j0 = s_ij[i0];
+      p0 = s_cpos[i0];
+      win_rows<NR>(A, p0, w0);
+    }
+#pragma unroll 1
+    for (int k = 0; k < Q; ++k) {
+      const float* ginv = A.sw + (int64_t)k * A.mcap;
+      const float* gfk = A.a.dev + (int64_t)k * A.mcap;
+      __syncthreads();
+      for (int l = threadIdx.x; l < nstaged; l += blockDim.x) {
+        const int gm = s_gi[l];
+        *reinterpret_cast<float2*>(&s_rec[l].inv) = make_float2(ginv[gm], gfk[gm]);
+      }
+      __syncthreads();
+      const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
+      if (has0) gather_cp_shift<Q, NR>(A, k, cdx, cdy, rw, rh, s_beg, s_end, s_rec, bx0, by0, p0, w0, j0);
+      for (int i = i0 + blockDim.x; i < nc; i += blockDim.x) {
+        WinRows<NR> w;
+        const Pair<float> pp = s_cpos[i];
+        win_rows<NR>(A, pp, w);
+        gather_cp_shift<Q, NR>(A, k, cdx, cdy, rw, rh, s_beg, s_end, s_rec, s_bx[i], s_by[i], pp, w, s_ij[i]);
+      }
+    }
+    if (c0 + cap_t >= n) break;
+    __syncthreads();
+  }
+}
+
+template <int Q>
+__global__ void __launch_bounds__(256) k_gather_ts(const __grid_constant__ Args<Q, 2, PF32> A,
+                                                  const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const Tile2 T = tiles[tb];
+    const InstK I = A.inst[T.inst];
+    const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
+    const int cap = G.cap_gather, cap_t = G.cap_tile;
+    unsigned char* p = smem;
+    int* s_beg = carve<int>(p, rw * rh);
+    int* s_end = carve<int>(p, rw * rh);
+    int* s_row = carve<int>(p, rh + 2);
+    int* s_gi = carve<int>(p, cap);
+    GRec* s_rec = carve<GRec>(p, cap);
+    int* s_tr = carve<int>(p, 2 * G.ty + 2);
+    int* s_ij = carve<int>(p, cap_t);
+    short* s_bx = carve<short>(p, cap_t);
+    short* s_by = carve<short>(p, cap_t);
+    Pair<float>* s_cpos = carve<Pair<float>>(p, cap_t);
+    stage_region(I, T.x0 + G.mom.xl, T.y0 + G.mom.yl, rw, rh, A.a.start, cap, s_beg, s_end, s_row,
+                 [&](int gm, int l, int rx) {
+                   s_gi[l] = gm;
+                   *reinterpret_cast<float4*>(&s_rec[l]) =
+                       make_float4(A.a.off[gm], A.a.off[A.mcap + gm], (float)rx, A.a.rho[gm]);
+                 });
+    if (s_row[rh + 1])
+      gather_rows_shift<Q, kShiftRows>(A, I, T, G, rw, rh, s_beg, s_end, s_gi, s_rec, s_row[rh], s_tr, s_ij, s_bx,
+                                       s_by, s_cpos);
+    else
+      gather_body<Q, PF32, false>(A, I, T, G, rw, rh, s_beg, s_end, s_gi, nullptr, nullptr, nullptr, 0, s_tr, s_ij,
+                                  s_bx, s_by, s_cpos);
     __syncthreads();
   }
 }

@@ -271,7 +271,7 @@ class Simulation:
         self.instances[inst].inflow = (tuple(v), int(width)) if width > 0 else None
 
     # ---- launch configuration -------------------------------------------------------------------
-    OPT_TILE_WIDTH, OPT_PERSISTENT, OPT_KAPPA_SOFT, OPT_BRICK_WIDTH = 3, 4, 5, 6
+    OPT_TILE_WIDTH, OPT_PERSISTENT, OPT_KAPPA_SOFT, OPT_BRICK_WIDTH, OPT_SHIFTED_WINDOWS = 3, 4, 5, 6, 7
 
     def tiling(self) -> tuple:
         """(tile width in cells, persistent launches) of the 2D tiled kernels."""
@@ -288,6 +288,14 @@ class Simulation:
             if persistent is not None:
                 _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_PERSISTENT, 1 if persistent else 0),
                            "set persistent")
+
+    def set_shifted_windows(self, on: bool):
+        """2D FP32 store with whole-cell displacements (D2Q9, dx = cell) and r < 2 cells: build one
+        table of window rows per reference point and shift it per direction (default on).  Results
+        are bit-identical either way; only the speed changes."""
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_SHIFTED_WINDOWS, 1 if on else 0),
+                       "set shifted windows")
 
     def brick_width(self) -> int:
         """Cells along x of the 256-cell bricks the untiled window kernels give each block."""

@@ -185,6 +185,11 @@ int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
  * each block a brick of 256 cells, this many along x (a power of two, 4..32 in 3D, 8..64 in 2D;
  * default 8 in 3D, 16 in 2D); results do not depend on it.  direbm_gb300.autotune picks it. */
 #define DBM_OPT_BRICK_WIDTH 6
+/* DBM_OPT_SHIFTED_WINDOWS (2D, FP32 store): when every displacement c * dx / cell is a whole
+ * number of cells (D2Q9 with dx = cell) and r < 2 cells, the tiled kernels build one table of
+ * window rows per reference point and shift it for each direction instead of building a window
+ * per (point, direction) (default 1).  Results are bit-identical either way. */
+#define DBM_OPT_SHIFTED_WINDOWS 7
 int dbm_sim_get_brick_width(dbm_sim* sim, int32_t* brick_width);
 int dbm_sim_set_option(dbm_sim* sim, int32_t option, int32_t value);
 int dbm_sim_get_tiling(dbm_sim* sim, int32_t* tile_width, int32_t* persistent);

@@ -378,3 +378,42 @@ def test_tiled_kernels_bitwise_equal_untiled(precision, name):
         assert sim.status() == 0
     for a, b in zip(outs[0], outs[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["tg_d2q9_r15", "batch_uneven"])
+def test_shifted_windows_bitwise_equal(name):
+    """Whole-cell displacements (D2Q9, dx = cell, FP32 store): the kernels that shift one window-row
+    table per reference point give the same bits as the per-direction windows."""
+    from direbm_gb300.sim import Instance, Simulation
+    from oracle.lattices import D2Q9
+    from oracle.physics import equilibrium
+
+    if name in CASES:
+        lattice, insts, dx, r, cell, build = CASES[name]
+        x, f = build()
+        ib = None
+    else:
+        lattice, dx, r, cell = "D2Q9", 1.0, 1.5, 1.0
+        insts = [dict(dims=(n, n), periodic=True, tau=t) for n, t in ((70, 0.6), (23, 0.95), (41, 0.55))]
+        rng = np.random.default_rng(21)
+        xs, fs, bs = [], [], []
+        for b, ins in enumerate(insts):
+            n0, n1 = ins["dims"]
+            xx = np.stack(np.meshgrid(np.arange(n0) + 0.5, np.arange(n1) + 0.5), -1).reshape(-1, 2)
+            xx = np.mod(xx + rng.uniform(-0.25, 0.25, xx.shape), [n0, n1])
+            u = 0.03 * np.stack([np.sin(2 * np.pi * xx[:, 1] / n1), np.cos(2 * np.pi * xx[:, 0] / n0)], 1)
+            xs.append(xx)
+            fs.append(equilibrium(np.ones(len(xx)), u, D2Q9))
+            bs.append(np.full(len(xx), b))
+        x, f, ib = np.concatenate(xs), np.concatenate(fs), np.concatenate(bs)
+    outs = []
+    for on in (True, False):
+        sim = Simulation([Instance(**i) for i in insts], lattice=lattice, precision="fp32dev", dx=dx, r_res=r,
+                         cell=cell)
+        sim.set_shifted_windows(on)
+        sim.set_state(ib, x, f)
+        sim.step(4)
+        outs.append(sim.state_numpy())
+        assert sim.status() == 0
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
