@@ -51,14 +51,15 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
 
 // Global cell of unwrapped 2D coordinates for region staging.  A region may be wider than a small
 // periodic box (it then holds some cells twice, which is harmless: one window never spans a box),
-// so periodic coordinates are reduced with a true modulo rather than a single wrap.
+// so periodic coordinates are wrapped as often as needed (a region coordinate lies within a few
+// halo widths of the box, so this is at most a few steps and usually none, cheaper than a modulo).
 __device__ __forceinline__ bool region_cell(const InstK& I, int x, int y, uint32_t* g) {
   const int nx = I.dims[0], ny = I.dims[1];
   if (I.periodic) {
-    x %= nx;
-    if (x < 0) x += nx;
-    y %= ny;
-    if (y < 0) y += ny;
+    while (x < 0) x += nx;
+    while (x >= nx) x -= nx;
+    while (y < 0) y += ny;
+    while (y >= ny) y -= ny;
   } else if (x < 0 || x >= nx || y < 0 || y >= ny) {
     return false;
   }
@@ -646,8 +647,9 @@ __device__ __forceinline__ int tile_items(const InstK& I, const Tile2& T, const 
   const int nc = min(cap_t, n - c0);
   for (int i = threadIdx.x; i < nc; i += blockDim.x) {
     const int li = c0 + i;
-    int r = 0;
-    while (r + 1 < G.ty && s_tr[2 * (r + 1) + 1] <= li) ++r;
+    int r = 0;  // the last tile row whose first list entry is <= li (binary search; rows are sorted)
+    for (int step = 16; step > 0; step >>= 1)
+      if (r + step < G.ty && s_tr[2 * (r + step) + 1] <= li) r += step;
     const int j = s_tr[2 * r] + (li - s_tr[2 * r + 1]);
     const uint32_t lc = cellv[j] - I.base;
     s_ij[i] = j;
