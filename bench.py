@@ -65,10 +65,10 @@ KERNEL_BYTES = {
 }
 
 # DRAM bytes per input moment measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
-# one launch of k_gather_t on a 4.18 M-moment case of this workload (its first 64 members, 16x16
-# tiles): 436.4 MB read + 277.4 MB written.  Traffic grows with the moments, so a full launch's
-# traffic is this times M.
-KERNEL_TRAFFIC_PER_MOMENT = {"gather": 170.6}
+# one launch of k_gather_ts (the shifted-window gather this workload runs) on a 4.18 M-moment case
+# of this workload (its first 64 members, 16x16 tiles): 436.6 MB read + 281.3 MB written.  Traffic
+# grows with the moments, so a full launch's traffic is this times M.
+KERNEL_TRAFFIC_PER_MOMENT = {"gather": 171.6}
 
 # Per point-step byte model of the method (components materialised as 12-byte sort records):
 # B = M(Qs+b_p) + Nc k_b + 2 Nc k_b + 3(Nc k_b + M(Qs+b_p)) + 3 P b_p + P(Qs+b_p), with P ~ M,
@@ -222,7 +222,7 @@ def roofline_from_profile(sim, M, P, peak):
                       "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
                       "ms_per_launch": avg[dom], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
                       "traffic_source": ("ncu DRAM bytes of a 4.18 M-moment launch, scaled by moments "
-                                         "(profiles/gather_t_full_ensemble64.md)") if per_m else None}
+                                         "(profiles/gather_ts_full_ensemble64.md)") if per_m else None}
 
 
 def velocity_l2(f, lat):
