@@ -48,8 +48,19 @@ class Tape:
             _lib.check(self.lib.dbm_tape_create(sim.handle, ctypes.byref(h)), "dbm_tape_create")
         self._h = h
         self._counts = []
+        self._twin = None
+
+    def twin(self) -> "Tape":
+        """A second tape of the same simulator (created once, kept with this one): the rollout's
+        backward records one segment on one tape while the other tape's segment runs its VJPs."""
+        if self._twin is None:
+            self._twin = Tape(self.sim)
+        return self._twin
 
     def close(self):
+        if getattr(self, "_twin", None) is not None:
+            self._twin.close()
+            self._twin = None
         if getattr(self, "_h", None):
             self.lib.dbm_tape_destroy(self._h)
             self._h = None
@@ -176,7 +187,7 @@ class Tape:
 
 class _Rollout(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, pos, f, tau, sim, tape, inst, steps, every):
+    def forward(ctx, pos, f, tau, sim, tape, inst, steps, every, overlap):
         taus = tau.detach().to("cpu", torch.float64).numpy()
         sim.set_tau(taus)
         sim.set_state(inst, pos.detach(), f.detach())
@@ -188,7 +199,7 @@ class _Rollout(torch.autograd.Function):
             sim.step(1)
         final = sim.snapshot()
         inst_t, pos_t, f_t = sim.state()
-        ctx.sim, ctx.tape, ctx.steps, ctx.every = sim, tape, steps, every
+        ctx.sim, ctx.tape, ctx.steps, ctx.every, ctx.overlap = sim, tape, steps, every, overlap
         ctx.snaps, ctx.final, ctx.taus = snaps, final, taus
         ctx.save_for_backward(order)
         ctx.mark_non_differentiable(inst_t)
@@ -206,34 +217,57 @@ class _Rollout(torch.autograd.Function):
         g_tau = torch.zeros(len(sim.instances), dtype=torch.float64, device=dev)
         sim.set_tau(ctx.taus)
         nseg = len(ctx.snaps)
-        for seg in reversed(range(nseg)):
+        # Two tapes, two streams: segment s is recorded (with one host synchronisation per step)
+        # on the simulator's stream while the VJPs of segment s + 1 run from the other tape on a
+        # second stream, so the VJP kernels fill the recording's gaps.  Each tape's VJPs read only
+        # that tape, and a tape is cleared for its next segment only after its VJPs have finished;
+        # the arithmetic is the same as one tape on one stream, bit for bit.
+        overlap = ctx.overlap and nseg > 1
+        tapes = [tape, tape.twin()] if overlap else [tape]
+        main = torch.cuda.current_stream(dev)
+        vjp = torch.cuda.Stream(device=dev) if overlap else main
+        vjp.wait_stream(main)  # the output cotangents and g_tau
+        free = [None] * len(tapes)  # per tape: event after its last VJP launch
+        for i, seg in enumerate(reversed(range(nseg))):
             s0 = seg * ctx.every
             s1 = min(s0 + ctx.every, ctx.steps)
+            slot = i % len(tapes)
+            t = tapes[slot]
+            if free[slot] is not None:
+                main.wait_event(free[slot])
             for attempt in range(3):
                 sim.restore(ctx.snaps[seg], s0)
-                tape.clear()
+                t.clear()
                 try:
-                    tape.record(s1 - s0)
-                    g_off, g_f = tape.backward_all(g_off, g_f, g_tau)
+                    t.record(s1 - s0)
+                    vjp.wait_stream(main)
+                    with torch.cuda.stream(vjp):
+                        g_off, g_f = t.backward_all(g_off, g_f, g_tau)
+                    if overlap:
+                        free[slot] = torch.cuda.Event()
+                        free[slot].record(vjp)
                     break
                 except TapeOverflow:
                     if attempt == 2:
                         raise
-        tape.clear()
+        main.wait_stream(vjp)
+        for t in tapes:
+            t.clear()
         sim.restore(ctx.final, ctx.steps)
         g_pos_in = torch.empty_like(g_off)
         g_f_in = torch.empty_like(g_f)
         g_pos_in[order] = g_off / sim.cell
         g_f_in[order] = g_f
-        return g_pos_in, g_f_in, g_tau, None, None, None, None, None
+        return g_pos_in, g_f_in, g_tau, None, None, None, None, None, None
 
 
 def rollout(sim: Simulation, inst, pos: torch.Tensor, f: torch.Tensor, tau: torch.Tensor, steps: int,
-            checkpoint_every: int = 10, tape: Tape | None = None):
+            checkpoint_every: int = 10, tape: Tape | None = None, overlap: bool = True):
     """Differentiable ``steps``-step rollout of ``sim`` from moments (inst (M,), world positions
     pos (M, D), f (M, Q)) with per-instance ``tau`` (n_inst,).  Returns (inst, pos, f) of the final
     state in its sorted order; gradients flow to pos, f and tau.  The simulator is left at the
-    final state."""
+    final state.  ``overlap`` records one segment while the previous one runs its VJPs, on a
+    second tape (``tape.twin()``, twice the tape memory); the gradients are the same either way."""
     if steps < 1 or checkpoint_every < 1:
         raise ValueError("steps and checkpoint_every must be >= 1")
     dev = sim.device
@@ -244,7 +278,7 @@ def rollout(sim: Simulation, inst, pos: torch.Tensor, f: torch.Tensor, tau: torc
         inst = torch.zeros(pos.shape[0], dtype=torch.int32, device=dev)
     inst = torch.as_tensor(inst, dtype=torch.int32, device=dev)
     tape = tape if tape is not None else Tape(sim)
-    return _Rollout.apply(pos, f, tau, sim, tape, inst, int(steps), int(checkpoint_every))
+    return _Rollout.apply(pos, f, tau, sim, tape, inst, int(steps), int(checkpoint_every), bool(overlap))
 
 
 # ---- the inverse-problem workload: initial velocity from Fourier-mode coefficients ---------------
@@ -297,11 +331,12 @@ def velocity(f: torch.Tensor, lattice) -> torch.Tensor:
 
 
 def inverse_problem_loss(sim: Simulation, x0: torch.Tensor, field: ModeField, coeffs: torch.Tensor, tau: torch.Tensor,
-                         target: ModeField, steps: int, checkpoint_every: int = 10, tape: Tape | None = None):
+                         target: ModeField, steps: int, checkpoint_every: int = 10, tape: Tape | None = None,
+                         overlap: bool = True):
     """L = mean over final moments of |u(f_T) - u*(x_T)|^2, u* the target field at the final
     positions; the initial moments sit at x0 with unit density and velocity field(x0; coeffs)."""
     rho0 = torch.ones(x0.shape[0], dtype=torch.float64, device=x0.device)
     f0 = equilibrium(rho0, field(x0, coeffs), sim.lattice)
-    _, pos, f = rollout(sim, None, x0, f0, tau, steps, checkpoint_every, tape)
+    _, pos, f = rollout(sim, None, x0, f0, tau, steps, checkpoint_every, tape, overlap)
     du = velocity(f, sim.lattice) - target(pos, target.coeffs)
     return (du * du).sum(1).mean()
