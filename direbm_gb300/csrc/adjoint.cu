@@ -221,6 +221,162 @@ __global__ void k_rec_inst_start(const __grid_constant__ Args<Q, D, P> A, uint32
 // Each enumeration visits one row's pairs with exactly the arithmetic of the forward decision it
 // restates (canonical displacement, inclusive radius test) and calls emit(other end, e) per pair.
 
+// ---- 2D row runs -----------------------------------------------------------------------------
+//
+// The same enumerations in 2D with fewer dependent loads: a window row's candidate cells form at
+// most two runs of consecutive cells (split at a periodic seam), so a row reads its item range
+// with two loads instead of two per cell, and the row's x range is narrowed by its lower bound on
+// |e_y| (row_halfwidth2 drops only cells that hold no hit).  Candidates are visited in the
+// per-cell loops' order (rows ascending, x ascending, items in cell order), so every list is
+// identical, pair for pair.  Windows are at most kListRows rows (R < 2 cells); taller ones use the
+// per-cell loops.
+constexpr int kListRows = 5;
+
+struct RowRuns2 {
+  int n;             // runs, 0..2, in x order
+  uint32_t g0[2], g1[2];  // first and last cell of each run
+  int sx0[2];        // window-relative x of the run's first cell
+};
+
+// Runs of one window row: grid row Gy + sy, unwrapped cells [Gx + lo, Gx + hi] (windows are
+// narrower than every box, so a row wraps at most once).
+__device__ __forceinline__ RowRuns2 row_runs2(const InstK& I, int Gx, int Gy, int sy, int lo, int hi) {
+  RowRuns2 R;
+  R.n = 0;
+  const int nx = I.dims[0], ny = I.dims[1];
+  int y = Gy + sy;
+  if (I.periodic) y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+  else if (y < 0 || y >= ny) return R;
+  const uint32_t row = I.base + (uint32_t)nx * (uint32_t)y;
+  int a = Gx + lo, b = Gx + hi;
+  if (!I.periodic) {
+    a = max(a, 0);
+    b = min(b, nx - 1);
+    lo = a - Gx;
+  }
+  if (a > b) return R;
+  if (I.periodic && a < 0) {  // cells a + nx .. nx - 1, then 0 .. b
+    R.g0[0] = row + (uint32_t)(a + nx);
+    R.g1[0] = row + (uint32_t)(nx - 1);
+    R.sx0[0] = lo;
+    R.n = 1;
+    if (b >= 0) {
+      R.g0[1] = row;
+      R.g1[1] = row + (uint32_t)b;
+      R.sx0[1] = -Gx;
+      R.n = 2;
+    }
+  } else if (I.periodic && b >= nx) {  // cells a .. nx - 1, then 0 .. b - nx
+    if (a <= nx - 1) {
+      R.g0[0] = row + (uint32_t)a;
+      R.g1[0] = row + (uint32_t)(nx - 1);
+      R.sx0[0] = lo;
+      R.g0[1] = row;
+      R.g1[1] = row + (uint32_t)(b - nx);
+      R.sx0[1] = nx - Gx;
+      R.n = 2;
+    } else {
+      R.g0[0] = row;
+      R.g1[0] = row + (uint32_t)(b - nx);
+      R.sx0[0] = nx - Gx;
+      R.n = 1;
+    }
+  } else {
+    R.g0[0] = row + (uint32_t)a;
+    R.g1[0] = row + (uint32_t)b;
+    R.sx0[0] = lo;
+    R.n = 1;
+  }
+  return R;
+}
+
+// CP side (refine: reference = centroid, resampling: reference = control point), candidates the
+// moments of A.a: emit(m * Q + k, e) for every component (m, k) within r of the reference p
+// (offsets in the reference's cell Gc).  Returns the pair count, or -1 if the window is too tall.
+template <int Q, class P, class Emit>
+__device__ __forceinline__ int enum_cp_rows2(const Args<Q, 2, P>& A, const InstK& I, const int (&Gc)[3],
+                                             typename P::real px, typename P::real py, int k, Emit&& emit) {
+  using real = typename P::real;
+  const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
+  const real bxr = px - cdx, byr = py - cdy;
+  const int ylo = (int)floor(byr - A.R - A.tiny), yhi = (int)floor(byr + A.R + A.tiny);
+  if (yhi - ylo + 1 > kListRows) return -1;
+  int cnt = 0;
+#pragma unroll 1
+  for (int sy = ylo; sy <= yhi; ++sy) {
+    const real cy = canon_c<real>(sy, cdy, py);
+    const real lb = axis_lb<real>(cy);
+    const real hw = row_halfwidth2<real>(A.R2, rn_mul(lb, lb));
+    if (hw < (real)0) continue;
+    const RowRuns2 R = row_runs2(I, Gc[0], Gc[1], sy, (int)floor(bxr - hw - A.tiny), (int)floor(bxr + hw + A.tiny));
+    uint32_t mb[2], me[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      mb[q] = q < R.n ? A.a.start[R.g0[q]] : 0u;
+      me[q] = q < R.n ? A.a.start[R.g1[q] + 1] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q >= R.n) break;
+      for (uint32_t m = mb[q]; m < me[q]; ++m) {
+        const real o[3] = {A.a.off[m], A.a.off[A.mcap + m], 0};
+        const int sx = R.sx0[q] + (int)(A.a.cell[m] - R.g0[q]);
+        const real c[3] = {canon_c<real>(sx, cdx, px), cy, 0};
+        real e[3];
+        if (canon_d2<2, real>(o, c, e) <= A.R2) {
+          emit(m * (uint32_t)Q + (uint32_t)k, e);
+          ++cnt;
+        }
+      }
+    }
+  }
+  return cnt;
+}
+
+// Resampling, component side (row = component (m, k)), candidates the output control points; e in
+// the CP side's operation order.  Returns the pair count, or -1 if the window is too tall.
+template <int Q, class P, class Emit>
+__device__ __forceinline__ int enum_comp_rows2(const Args<Q, 2, P>& A, const InstK& I, const int (&Sc)[3], uint32_t m,
+                                               int k, Emit&& emit) {
+  using real = typename P::real;
+  const real o[3] = {A.a.off[m], A.a.off[A.mcap + m], 0};
+  const real cdx = A.L.template cd_as<real>(k, 0), cdy = A.L.template cd_as<real>(k, 1);
+  const real tx = rn_add(o[0], cdx), ty = rn_add(o[1], cdy);
+  const int ylo = (int)floor(ty - A.R - A.tiny), yhi = (int)floor(ty + A.R + A.tiny);
+  if (yhi - ylo + 1 > kListRows) return -1;
+  int cnt = 0;
+#pragma unroll 1
+  for (int gy = ylo; gy <= yhi; ++gy) {
+    // candidates have e_y in [fl(o_y + fl(base_y - 1)), fl(o_y + base_y)] (offsets in [0, 1))
+    const real basey = rn_add((real)(-gy), cdy);
+    const real ely = rn_add(o[1], rn_sub(basey, (real)1)), ehy = rn_add(o[1], basey);
+    const real lb = ely > (real)0 ? ely : (ehy < (real)0 ? -ehy : (real)0);
+    const real hw = row_halfwidth2<real>(A.R2, rn_mul(lb, lb));
+    if (hw < (real)0) continue;
+    const RowRuns2 R = row_runs2(I, Sc[0], Sc[1], gy, (int)floor(tx - hw - A.tiny), (int)floor(tx + hw + A.tiny));
+    uint32_t cb[2], ce[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      cb[q] = q < R.n ? A.b.start[R.g0[q]] : 0u;
+      ce[q] = q < R.n ? A.b.start[R.g1[q] + 1] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q >= R.n) break;
+      for (uint32_t c = cb[q]; c < ce[q]; ++c) {
+        const int gx = R.sx0[q] + (int)(A.b.cell[c] - R.g0[q]);
+        const real cc[3] = {canon_c<real>(-gx, cdx, A.b.off[c]), canon_c<real>(-gy, cdy, A.b.off[A.ccap + c]), 0};
+        real e[3];
+        if (canon_d2<2, real>(o, cc, e) <= A.R2) {
+          emit(c, e);
+          ++cnt;
+        }
+      }
+    }
+  }
+  return cnt;
+}
+
 // Refine, CP side, row (CP j, direction k): the components of direction k within r of the centroid
 // of moved CP j (the forward refine's window around the thin cell).
 template <int Q, int D, class P, class Emit>
@@ -232,6 +388,10 @@ __device__ __forceinline__ uint32_t enum_refine_cp(const Args<Q, D, P>& A, const
   const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, F)];
   int Fc[3];
   decode_cell<D>(I, F, Fc);
+  if constexpr (D == 2) {
+    const int n = enum_cp_rows2<Q, P>(A, I, Fc, r.cp_cen[j], r.cp_cen[r.P + j], k, emit);
+    if (n >= 0) return (uint32_t)n;
+  }
   real cen[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
@@ -279,6 +439,10 @@ __device__ __forceinline__ uint32_t enum_resample_cp(const Args<Q, D, P>& A, int
   const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
   int Gc[3];
   decode_cell<D>(I, G, Gc);
+  if constexpr (D == 2) {
+    const int n = enum_cp_rows2<Q, P>(A, I, Gc, A.b.off[j], A.b.off[A.ccap + j], k, emit);
+    if (n >= 0) return (uint32_t)n;
+  }
   real p[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
@@ -329,6 +493,10 @@ __device__ __forceinline__ uint32_t enum_comp(const Args<Q, D, P>& A, const Step
   const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, g)];
   int Sc[3];
   decode_cell<D>(I, g, Sc);
+  if constexpr (D == 2 && !REFINE) {  // (the refine side reads one centroid per cell: no item runs)
+    const int n = enum_comp_rows2<Q, P>(A, I, Sc, m, k, emit);
+    if (n >= 0) return (uint32_t)n;
+  }
   real o[3] = {0, 0, 0}, cdk[3] = {0, 0, 0};
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
