@@ -116,6 +116,13 @@ struct StepRec {
   PairCSR<real, D> ref, res, gap;
 };
 
+// Per component (m, k), from the gather's VJP to the control-point rows: f*·(1/sw) (0 for a
+// dropped component) and G = sum over its pairs of a_ij fbar_jk.
+template <class real>
+struct alignas(2 * sizeof(real)) FsG {
+  real fsi, g;
+};
+
 // Everything a backward kernel reads, by value.
 template <int Q, int D, class P>
 struct RecK {
@@ -815,7 +822,7 @@ template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK<Q, D, P> K,
                                                     const typename P::real* __restrict__ fbarG,
                                                     typename P::real* __restrict__ fsbar, typename P::real* __restrict__ ybar,
-                                                    typename P::real* __restrict__ Gc, typename P::real* __restrict__ wexp) {
+                                                    FsG<typename P::real>* __restrict__ fg, typename P::real* __restrict__ wexp) {
   using real = typename P::real;
   const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
   const auto& L = K.r.res.t;
@@ -834,10 +841,10 @@ __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK
       }
     }
     fsbar[t] = G;
-    Gc[t] = G;
     const real fst = rec_fstar<Q, D, P>(K, m, k);
     wexp[t] = exp(fst);  // the refine weight, kept for the refine kernels
     const real fsi = fst * inv;
+    fg[t] = FsG<real>{inv > (real)0 ? fsi : (real)0, G};
     real y[3] = {0, 0, 0};
     for (uint32_t q = q0; q < q1; ++q) {
       const auto pr = L.rec[q];
@@ -857,7 +864,7 @@ __global__ void __launch_bounds__(256) k_bwd_gather(const __grid_constant__ RecK
 // the row's part of W = sum w and sum w e over its refine pairs (w = exp(f*)).
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_rows(const __grid_constant__ RecK<Q, D, P> K,
-                                                  const typename P::real* __restrict__ Gc,
+                                                  const FsG<typename P::real>* __restrict__ fg,
                                                   const typename P::real* __restrict__ wexp,
                                                   const typename P::real* __restrict__ fbarG,
                                                   typename P::real* __restrict__ xrow, typename P::real* __restrict__ Wrow,
@@ -875,8 +882,10 @@ __global__ void __launch_bounds__(256) k_bwd_rows(const __grid_constant__ RecK<Q
       real u[3];
       unit_of<D, real>(pr, u);
       const int64_t m = pr.item / Q;
-      const real inv = K.r.inv_sw[(int64_t)k * M + m];
-      const real wb = inv > (real)0 ? rec_fstar<Q, D, P>(K, m, k) * inv * (fb - Gc[(int64_t)k * M + m]) : (real)0;
+      // f*·(1/sw)·(fbar − G), the product formed in k_bwd_gather (0 for a dropped component: the
+      // pair then adds ±0, which leaves x unchanged)
+      const FsG<real> v = fg[(int64_t)k * M + m];
+      const real wb = v.fsi * (fb - v.g);
 #pragma unroll
       for (int a = 0; a < D; ++a) x[a] += wb * u[a];
     }
@@ -1501,14 +1510,15 @@ struct TapeImpl : TapeBase, StepHook {
     }
     DBM_CUDA(cudaStreamWaitEvent(s, done, 0));  // the previous call's scratch is free
     bwd_mem.reset();
-    real *xbarP, *fbarG, *sbarG, *fsbar, *ybar, *Gc, *wexp, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
+    real *xbarP, *fbarG, *sbarG, *fsbar, *ybar, *wexp, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
+    FsG<real>* fg;
     double *taupart, *blocksum;
     DBM_TRY(bwd_mem.get(&xbarP, (int64_t)D * Pn));
     DBM_TRY(bwd_mem.get(&fbarG, (int64_t)Q * Pn));
     DBM_TRY(bwd_mem.get(&sbarG, (int64_t)Q * Pn));
     DBM_TRY(bwd_mem.get(&fsbar, QM));
     DBM_TRY(bwd_mem.get(&ybar, (int64_t)D * QM));
-    DBM_TRY(bwd_mem.get(&Gc, QM));
+    DBM_TRY(bwd_mem.get(&fg, QM));
     DBM_TRY(bwd_mem.get(&wexp, QM));
     DBM_TRY(bwd_mem.get(&xrow, (int64_t)D * PQ));
     DBM_TRY(bwd_mem.get(&Wrow, PQ));
@@ -1529,11 +1539,11 @@ struct TapeImpl : TapeBase, StepHook {
       }
     }
     if (M > 0) {
-      k_bwd_gather<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, fbarG, fsbar, ybar, Gc, wexp);
+      k_bwd_gather<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, fbarG, fsbar, ybar, fg, wexp);
       DBM_LAUNCH_CHECK();
     }
     if (Pn > 0) {
-      k_bwd_rows<Q, D, P><<<grid_for(PQ), 256, 0, s>>>(K, Gc, wexp, fbarG, xrow, Wrow, sxrow);
+      k_bwd_rows<Q, D, P><<<grid_for(PQ), 256, 0, s>>>(K, fg, wexp, fbarG, xrow, Wrow, sxrow);
       DBM_LAUNCH_CHECK();
       k_bwd_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xrow, Wrow, sxrow, xbarP, Wj, sj, cenbar, ncells);
       DBM_LAUNCH_CHECK();
