@@ -1347,10 +1347,10 @@ struct SimImpl : SimBase {
       const size_t rh = geo.ty + geo.mom.yh - geo.mom.yl;
       return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4}, {cp, 4 * rs}, {cp, rs}, {cp, 2 * rs},
                           {(size_t)2 * geo.ty + 2, 4}, {ct, 4}, {ct, 2}, {ct, 2}, {ct, 2 * rs}});
-    } else {  // gather with whole-cell displacements (FP32): 32-byte records
+    } else {  // gather with whole-cell displacements (FP32): GRec records
       const size_t cells = (size_t)(geo.tx + geo.mom.xh - geo.mom.xl) * (geo.ty + geo.mom.yh - geo.mom.yl);
       const size_t rh = geo.ty + geo.mom.yh - geo.mom.yl;
-      return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4}, {cp, 32}, {(size_t)2 * geo.ty + 2, 4},
+      return carve_bytes({{cells, 4}, {cells, 4}, {rh + 2, 4}, {cp, 4}, {cp, sizeof(GRec)}, {(size_t)2 * geo.ty + 2, 4},
                           {ct, 4}, {ct, 2}, {ct, 2}, {ct, 8}});
     }
   }

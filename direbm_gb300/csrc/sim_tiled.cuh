@@ -1097,18 +1097,20 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
 // are visited in the same order (rows ascending, then the row's items): sums are bit-identical to
 // the per-direction windows.
 // A staged moment for the whole-cell gather: offsets, region column (exact small integer), rho,
-// then (1/sw, f*_k) of the direction being gathered, so a hit reads its operands at a fixed
-// offset from the candidate it just tested.
+// then (1/sw, f*_k) of the kGatherGroup directions staged together, so a hit reads its operands
+// at a fixed offset from the candidate it just tested.
+constexpr int kGatherGroup = 3;
 struct alignas(16) GRec {
   float ox, oy, rx, rho;
-  float inv, f, pad0, pad1;
+  float kv[2 * kGatherGroup];  // (1/sw, f*) of each staged direction
+  float pad[(4 - (2 * kGatherGroup) % 4) % 4];
 };
 
 // One control point, one direction (FP32 store): the gather_rows sum over the shifted rows.
 template <int Q, int NR>
-__device__ __forceinline__ void gather_cp_shift(const Args<Q, 2, PF32>& A, int k, int cdx, int cdy, int rw, int rh,
-                                                const int* s_beg, const int* s_end, const GRec* s_rec, int bx,
-                                                int by, Pair<float> pp, const WinRows<NR>& w, int j) {
+__device__ __forceinline__ void gather_cp_shift(const Args<Q, 2, PF32>& A, int k, int slot, int cdx, int cdy, int rw,
+                                                int rh, const int* s_beg, const int* s_end, const GRec* s_rec,
+                                                int bx, int by, Pair<float> pp, const WinRows<NR>& w, int j) {
   const float cxo = (float)(cdx - bx);  // region column + cxo = float(dS_x + cd_x), exact
   CSum sa;
   float sb = 0.f;  // deviation part: plain FMA accumulation, as in gather_rows
@@ -1131,7 +1133,7 @@ __device__ __forceinline__ void gather_cp_shift(const Args<Q, 2, PF32>& A, int k
       if (d2 <= A.R2) {
         // A dropped component has 1/sw = 0: its weight is +0 and every sum below is unchanged
         // (the sums are >= +0 and f is finite), so it needs no test of its own.
-        const float2 kv = *reinterpret_cast<const float2*>(&it->inv);
+        const float2 kv = *reinterpret_cast<const float2*>(&it->kv[2 * slot]);
         const float wgt = (A.R - rn_sqrt(d2)) * kv.x;
         // CSum::add_prod(wgt, rho) and the deviation FMA, the two FMAs as one paired op
         const float p = __fmul_rn(wgt, a.w);
@@ -1175,23 +1177,29 @@ __device__ __forceinline__ void gather_rows_shift(const Args<Q, 2, PF32>& A, con
       p0 = s_cpos[i0];
       win_rows<NR>(A, p0, w0);
     }
+    // directions in groups of kGatherGroup: one staging pass (two barriers) per group
 #pragma unroll 1
-    for (int k = 0; k < Q; ++k) {
-      const float* ginv = A.sw + (int64_t)k * A.mcap;
-      const float* gfk = A.a.dev + (int64_t)k * A.mcap;
+    for (int k0 = 0; k0 < Q; k0 += kGatherGroup) {
+      const int ng = min(kGatherGroup, Q - k0);
       __syncthreads();
       for (int l = threadIdx.x; l < nstaged; l += blockDim.x) {
         const int gm = s_gi[l];
-        *reinterpret_cast<float2*>(&s_rec[l].inv) = make_float2(ginv[gm], gfk[gm]);
+        for (int q = 0; q < ng; ++q)
+          *reinterpret_cast<float2*>(&s_rec[l].kv[2 * q]) =
+              make_float2(A.sw[(int64_t)(k0 + q) * A.mcap + gm], A.a.dev[(int64_t)(k0 + q) * A.mcap + gm]);
       }
       __syncthreads();
-      const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
-      if (has0) gather_cp_shift<Q, NR>(A, k, cdx, cdy, rw, rh, s_beg, s_end, s_rec, bx0, by0, p0, w0, j0);
-      for (int i = i0 + blockDim.x; i < nc; i += blockDim.x) {
-        WinRows<NR> w;
-        const Pair<float> pp = s_cpos[i];
-        win_rows<NR>(A, pp, w);
-        gather_cp_shift<Q, NR>(A, k, cdx, cdy, rw, rh, s_beg, s_end, s_rec, s_bx[i], s_by[i], pp, w, s_ij[i]);
+#pragma unroll 1
+      for (int q = 0; q < ng; ++q) {
+        const int k = k0 + q;
+        const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
+        if (has0) gather_cp_shift<Q, NR>(A, k, q, cdx, cdy, rw, rh, s_beg, s_end, s_rec, bx0, by0, p0, w0, j0);
+        for (int i = i0 + blockDim.x; i < nc; i += blockDim.x) {
+          WinRows<NR> w;
+          const Pair<float> pp = s_cpos[i];
+          win_rows<NR>(A, pp, w);
+          gather_cp_shift<Q, NR>(A, k, q, cdx, cdy, rw, rh, s_beg, s_end, s_rec, s_bx[i], s_by[i], pp, w, s_ij[i]);
+        }
       }
     }
     if (c0 + cap_t >= n) break;
