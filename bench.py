@@ -368,14 +368,17 @@ def e2e_leg(sim, ib, x, f, steps=8, warmup=1):
     ms = e0.elapsed_time(e1)
     serial = {"value": points / (ms * 1e-3), "ms_per_step": ms / steps, "wall_s": wall}
     piped = _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, (o_inst, o_pos, o_f, m2))
-    return {"value": piped["value"], "unit": "point-steps/s", "h2d_bytes_per_step": int(h2d // steps),
-            "d2h_bytes_per_step": int(d2h // steps), "ms_per_step": piped["ms_per_step"], "wall_s": piped["wall_s"],
+    serial["h2d_bytes_per_step"], serial["d2h_bytes_per_step"] = int(h2d // steps), int(d2h // steps)
+    return {"value": piped["value"], "unit": "point-steps/s", "h2d_bytes_per_step": int(piped["h2d_bytes_per_step"]),
+            "d2h_bytes_per_step": int(piped["d2h_bytes_per_step"]), "ms_per_step": piped["ms_per_step"],
+            "wall_s": piped["wall_s"],
             "steps": steps, "warmup": warmup, "copy_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs}, "serial": serial,
             "result_equals_serial": piped["result_equals_serial"],
             "repetitions_ms_per_step": piped["repetitions_ms_per_step"], "statistic": "median of 3 repetitions",
-            "path": "Simulation.set_state/step/state(out=) (C ABI dbm_sim_*) with pinned host buffers; each step's "
-                    "host-to-device copy on its own stream overlaps the previous step, each step's device-to-host "
-                    "copy on a third stream overlaps the next (two buffer slots each way)"}
+            "path": "Simulation.set_state(check=False)/step/state_into (C ABI dbm_sim_*) with pinned host buffers and "
+                    "no host wait inside a step; each step's host-to-device copy on its own stream overlaps the "
+                    "previous step, each step's device-to-host copy of the whole output buffers (capacity rows) on a "
+                    "third stream overlaps the next (two buffer slots each way); status and count read after the run"}
 
 
 def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out):
@@ -415,19 +418,18 @@ def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out):
             if i + 1 < n:
                 upload(1 - sl)
             main.wait_event(ev["in"][sl])
-            sim.set_state(*din[sl])
+            sim.set_state(*din[sl], check=False)  # the bad-input bit is checked after the run
             ev["used"][sl].record(main)
             sim.step(1)
             main.wait_event(ev["down"][sl])  # this slot's previous result has left the device
-            gi, gp, gf = sim.state(out=dout[sl])
-            m2 = gi.shape[0]
+            sim.state_into(dout[sl])  # no host wait: the whole buffers go down, count() read after
             ev["out"][sl].record(main)
             with torch.cuda.stream(s_down):
                 s_down.wait_event(ev["out"][sl])
-                for h, d in zip(hout[sl], (gi, gp, gf)):
-                    h[:m2].copy_(d, non_blocking=True)
+                for h, d in zip(hout[sl], dout[sl]):
+                    h.copy_(d, non_blocking=True)
                 ev["down"][sl].record(s_down)
-            last.update(slot=sl, m=m2)
+            last.update(slot=sl)
         main.wait_stream(s_down)
         main.wait_stream(s_up)
 
@@ -445,14 +447,17 @@ def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out):
         torch.cuda.synchronize()
         reps.append((e0.elapsed_time(e1), time.perf_counter() - t0))
     ms, wall = sorted(reps)[1]
+    sim.check_status()  # set_state's deferred bad-input check, and every step's status bits
     # same input every step and deterministic kernels: the last result equals the serial path's
     oi, op, of, m_serial = serial_out
     hi, hp, hf = hout[last["slot"]]
+    m2 = sim.count()
     n = min(m_serial, 1 << 20)
-    same = (last["m"] == m_serial and torch.equal(hi[:n], oi[:n]) and torch.equal(hp[:n], op[:n])
+    same = (m2 == m_serial and torch.equal(hi[:n], oi[:n]) and torch.equal(hp[:n], op[:n])
             and torch.equal(hf[:n], of[:n]))
     return {"value": M * steps / (ms * 1e-3), "ms_per_step": ms / steps, "wall_s": wall,
-            "result_equals_serial": bool(same), "repetitions_ms_per_step": [r[0] / steps for r in reps]}
+            "result_equals_serial": bool(same), "repetitions_ms_per_step": [r[0] / steps for r in reps],
+            "h2d_bytes_per_step": M * (4 + 16 + 72), "d2h_bytes_per_step": cap * (4 + 16 + 72)}
 
 
 def adjoint_leg(n=256, steps=100, every=10, tau=0.6, precisions=("fp32dev", "fp64")):

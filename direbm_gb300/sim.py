@@ -88,6 +88,7 @@ class Simulation:
         self.kappa_soft = int(kappa_soft)
         if self.kappa_soft > 0:  # up to one spawned control point per thinning cell
             moment_capacity = max(int(moment_capacity), 2 * self.ncells)
+        self.capacity = max(int(moment_capacity), self.ncells)  # rows of each state buffer
         desc = _lib.SimDesc(
             lattice=self.lattice.id, precision=_PREC[precision], dx=self.dx, r_res=self.r_res,
             cell=self.cell, kappa_hard=self.kappa_hard, eps=self.eps, moment_capacity=int(moment_capacity),
@@ -140,8 +141,11 @@ class Simulation:
         return int(self.lib.dbm_sim_device_bytes(self._h))
 
     # ---- state ----------------------------------------------------------------------------------
-    def set_state(self, inst, pos, f):
-        """Load moments: instance index (M,), world positions (M, D), distributions (M, Q)."""
+    def set_state(self, inst, pos, f, check: bool = True):
+        """Load moments: instance index (M,), world positions (M, D), distributions (M, Q).  With
+        ``check=False`` the call does not wait for the load to finish: a moment outside its box then
+        leaves the bad-input bit in ``status()`` (``check_status()`` raises on it) instead of raising
+        here, so a caller that pipelines loads and steps keeps the device busy."""
         dev = self.device
         pos = torch.as_tensor(pos, dtype=torch.float64, device=dev).contiguous()
         f = torch.as_tensor(f, dtype=torch.float64, device=dev).contiguous()
@@ -154,7 +158,7 @@ class Simulation:
         with torch.cuda.device(dev):
             _lib.check(self.lib.dbm_sim_set_state(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), M, _stream()),
                        "dbm_sim_set_state")
-            st = self.status(clear=True)
+            st = self.status(clear=True) if check else 0
         if st & _lib.ST_BAD_INPUT:
             raise _lib.DbmError("set_state: a moment lies outside its instance box")
         self.iteration = 0
@@ -216,6 +220,24 @@ class Simulation:
     def state_numpy(self):
         inst, pos, f = self.state()
         return inst.cpu().numpy(), pos.cpu().numpy(), f.cpu().numpy()
+
+    def state_into(self, out):
+        """Write the state into ``out`` = (inst, pos, f): contiguous CUDA int32 (>= capacity,),
+        fp64 (>= capacity, D) and fp64 (>= capacity, Q) buffers.  Unlike ``state()`` this does not
+        wait for the step to finish (it needs no row count on the host): once the caller's stream
+        reaches this point, rows [0, count()) hold the state, in its sorted order."""
+        oi, op, of = out
+        D, Q, C = self.lattice.D, self.lattice.Q, self.capacity
+        ok = (oi.is_cuda and op.is_cuda and of.is_cuda and oi.dtype == torch.int32 and op.dtype == torch.float64
+              and of.dtype == torch.float64 and oi.is_contiguous() and op.is_contiguous() and of.is_contiguous()
+              and oi.shape[0] >= C and op.shape[0] >= C and of.shape[0] >= C and tuple(op.shape[1:]) == (D,)
+              and tuple(of.shape[1:]) == (Q,))
+        if not ok:
+            raise ValueError(f"state_into: need contiguous CUDA int32 (>= {C},), fp64 (>= {C}, {D}), fp64 (>= {C}, {Q})")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_get_state(self._h, oi.data_ptr(), op.data_ptr(), of.data_ptr(), _stream()),
+                       "dbm_sim_get_state")
+        return out
 
     def status(self, clear: bool = False) -> int:
         v = ctypes.c_uint32()

@@ -138,3 +138,34 @@ def test_state_into_caller_buffers_and_status_reads_on_busy_copy_streams():
         sim.state(out=(out[0][: n - 1], out[1], out[2]))
     with pytest.raises(ValueError):
         sim.state(out=(out[0], out[1].float(), out[2]))
+
+
+def test_pipelined_load_and_export_without_host_waits():
+    """set_state(check=False) defers the bad-input check to status(), and state_into writes the
+    same rows as state() into capacity-sized buffers without reading the count on the host."""
+    import torch
+
+    from direbm_gb300._lib import ST_BAD_INPUT, DbmError
+
+    x, f = periodic_tg(24, "D2Q9", seed=6)
+    sim = _sim([dict(dims=(24, 24), tau=0.7)], "fp32dev")
+    sim.set_state(None, x, f, check=False)
+    sim.step(2)
+    C = sim.capacity
+    out = (torch.full((C,), -1, dtype=torch.int32, device="cuda"),
+           torch.full((C, 2), -1.0, dtype=torch.float64, device="cuda"),
+           torch.full((C, 9), -1.0, dtype=torch.float64, device="cuda"))
+    assert sim.state_into(out) is out
+    ref = sim.state()
+    n = sim.count()
+    for o, r in zip(out, ref):
+        assert torch.equal(o[:n], r)
+    assert sim.status() == 0
+    with pytest.raises(ValueError):
+        sim.state_into((out[0][: C - 1], out[1], out[2]))
+    # a moment outside its bounded box: no error at the load, the bit waits in the status word
+    sim = _sim([dict(dims=(16, 16), periodic=False)])
+    sim.set_state(None, np.array([[20.0, 3.0]]), np.ones((1, 9)) / 9, check=False)
+    assert sim.status() & ST_BAD_INPUT
+    with pytest.raises(DbmError):
+        sim.check_status()
