@@ -99,6 +99,7 @@ template <class real, int D>
 struct StepRec {
   int64_t M = 0, P = 0;
   uint32_t* in_cell = nullptr;    // [M]
+  uint32_t* in_start = nullptr;   // [ncells + 1] the input state's cell ranges (read by the lists)
   real* in_off = nullptr;         // [D][M]
   real* in_f = nullptr;           // FP64: f [Q][M]; FP32DEV: dev [Q][M]
   float* in_rho = nullptr;        // FP32DEV: rho [M]
@@ -1193,13 +1194,24 @@ struct TapeImpl : TapeBase, StepHook {
   double* io[1] = {nullptr};     // intermediate cotangents of backward_all
   int64_t io_cap = 0;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // The six lists of a recorded step run on two streams of their own (side: component side and gap
+  // fill, side2: control-point side) and read only the tape and the step's output state, so they
+  // overlap the simulator's next step.  Whatever reads their counters or lists, or could overwrite
+  // what they read, first waits on lists_done.
+  cudaStream_t side2 = nullptr;
+  cudaEvent_t ev_join2 = nullptr, lists_done = nullptr;
+  bool lists_pending = false;
 
   explicit TapeImpl(SimBase* s) : sim(s) {}
   ~TapeImpl() override {
+    if (lists_pending) cudaEventSynchronize(lists_done);
     if (io[0]) cudaFree(io[0]);
     if (side) cudaStreamDestroy(side);
+    if (side2) cudaStreamDestroy(side2);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_join2) cudaEventDestroy(ev_join2);
+    if (lists_done) cudaEventDestroy(lists_done);
     if (done) cudaEventDestroy(done);
     if (hbuf) cudaFreeHost(hbuf);
     if (d_count) cudaFree(d_count);
@@ -1210,6 +1222,9 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     DBM_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    DBM_CUDA(cudaStreamCreateWithFlags(&side2, cudaStreamNonBlocking));
+    DBM_CUDA(cudaEventCreateWithFlags(&ev_join2, cudaEventDisableTiming));
+    DBM_CUDA(cudaEventCreateWithFlags(&lists_done, cudaEventDisableTiming));
     DBM_CUDA(cudaHostAlloc(&hbuf, 64, cudaHostAllocMapped));
     DBM_CUDA(cudaHostGetDevicePointer(&hbuf_dev, hbuf, 0));
     DBM_CUDA(cudaMalloc(&d_count, 6 * 4));
@@ -1218,6 +1233,8 @@ struct TapeImpl : TapeBase, StepHook {
   }
 
   int clear() override {
+    if (lists_pending) DBM_CUDA(cudaEventSynchronize(lists_done));  // their memory is about to be reused
+    lists_pending = false;
     steps.clear();
     pending = -1;
     invalid = false;
@@ -1292,6 +1309,8 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_TRY(rec_mem.get(&r.thin_cell, (int64_t)Q * M));
     DBM_TRY(rec_mem.get(&r.inv_sw, (int64_t)Q * M));
     DBM_TRY(rec_mem.get(&r.inst_start, n_inst + 1));
+    DBM_TRY(rec_mem.get(&r.in_start, ncells + 1));
+    DBM_CUDA(cudaMemcpyAsync(r.in_start, A.a.start, (size_t)(ncells + 1) * 4, cudaMemcpyDeviceToDevice, s));
     if (M == 0) return DBM_OK;
     DBM_CUDA(cudaMemcpyAsync(r.in_cell, A.a.cell, (size_t)M * 4, cudaMemcpyDeviceToDevice, s));
     DBM_CUDA(cudaMemcpy2DAsync(r.in_off, (size_t)M * sizeof(real), A.a.off, (size_t)A.mcap * sizeof(real),
@@ -1366,6 +1385,10 @@ struct TapeImpl : TapeBase, StepHook {
     tmp_mem.reset();
     rec_stream = s;
     if (invalid) return DBM_ERR_CAPACITY;
+    if (lists_pending) {  // the previous step's lists ran beside this step: wait for their counters
+      DBM_CUDA(cudaStreamWaitEvent(s, lists_done, 0));
+      lists_pending = false;
+    }
     if (pending >= 0) {  // one synchronisation: this step's count and the previous step's counters
       const uint32_t* src[8] = {A.status, A.d_P, pending_counts, pending_counts + 1, pending_counts + 2,
                                 pending_counts + 3, pending_counts + 4, pending_counts + 5};
@@ -1409,8 +1432,8 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_TRY(rec_mem.get(&r.out_cell, Pn));
     DBM_TRY(rec_mem.get(&r.out_off, (int64_t)D * Pn));
     DBM_TRY(rec_mem.get(&r.emask, Pn));
-    uint32_t* cp_of_cell;
-    DBM_TRY(tmp_mem.get(&cp_of_cell, ncells));
+    uint32_t* cp_of_cell;  // kept with the step: its lists may still run during the next step
+    DBM_TRY(rec_mem.get(&cp_of_cell, ncells));
     DBM_CUDA(cudaMemsetAsync(cp_of_cell, 0xff, (size_t)ncells * 4, s));
     if (Pn > 0) {
       k_rec_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(A, r, cp_of_cell);
@@ -1422,15 +1445,28 @@ struct TapeImpl : TapeBase, StepHook {
       const int64_t cap = (int64_t)(per_row[kind] * 1.25 * (double)rows[kind]) + 1024;
       DBM_TRY(alloc_list(list_of(r, kind), rows[kind], cap, kind == kGapCP));
     }
-    // CP-side lists on s, component-side and gap lists on a second stream: they are independent
+    // The lists read the input moments from the tape's copies (the next step overwrites the
+    // simulator's input buffer), the emptiness masks from the tape, and the output state, which
+    // the next step only reads (its collision changes f, which no list reads).  So they run on two
+    // streams of their own beside the next step: control-point side on side2, component side and
+    // gap fill on side.
+    Args<Q, D, P> AL = A;
+    AL.a.start = r.in_start;
+    AL.a.cell = r.in_cell;
+    AL.a.off = r.in_off;
+    AL.mcap = M;
+    AL.emask = r.emask;
     DBM_CUDA(cudaEventRecord(ev_fork, s));
     DBM_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
-    for (int kind : {kRefineCP, kResCP}) DBM_TRY(launch_list(A, r, kind, cp_of_cell, s));
-    for (int kind : {kRefineComp, kResComp, kGapCP, kGapNb}) DBM_TRY(launch_list(A, r, kind, cp_of_cell, side));
-    DBM_CUDA(cudaEventRecord(ev_join, side));
-    DBM_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
-    // the slot counters are read at the next synchronisation (see settle): no wait here
-    DBM_CUDA(cudaMemcpyAsync(r_counts_dev(), d_count, 6 * 4, cudaMemcpyDeviceToDevice, s));
+    DBM_CUDA(cudaStreamWaitEvent(side2, ev_fork, 0));
+    for (int kind : {kRefineCP, kResCP}) DBM_TRY(launch_list(AL, r, kind, cp_of_cell, side2));
+    for (int kind : {kRefineComp, kResComp, kGapCP, kGapNb}) DBM_TRY(launch_list(AL, r, kind, cp_of_cell, side));
+    DBM_CUDA(cudaEventRecord(ev_join2, side2));
+    DBM_CUDA(cudaStreamWaitEvent(side, ev_join2, 0));
+    // the slot counters are read at the next synchronisation (see settle), after lists_done
+    DBM_CUDA(cudaMemcpyAsync(r_counts_dev(), d_count, 6 * 4, cudaMemcpyDeviceToDevice, side));
+    DBM_CUDA(cudaEventRecord(lists_done, side));
+    lists_pending = true;
     pending = (int)steps.size();  // this step's index once step() appends it
     pending_counts = cur_counts;
     return DBM_OK;
@@ -1479,6 +1515,10 @@ struct TapeImpl : TapeBase, StepHook {
     if (invalid) return DBM_ERR_CAPACITY;
     if (pending < 0) return DBM_OK;
     cudaStream_t s = rec_stream;
+    if (lists_pending) {
+      DBM_CUDA(cudaStreamWaitEvent(s, lists_done, 0));
+      lists_pending = false;
+    }
     const uint32_t* src[6] = {pending_counts, pending_counts + 1, pending_counts + 2, pending_counts + 3,
                               pending_counts + 4, pending_counts + 5};
     DBM_TRY(fetch(src, 6, s));

@@ -380,7 +380,7 @@ def test_tiled_kernels_bitwise_equal_untiled(precision, name):
         np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("name", ["tg_d2q9_r15", "batch_uneven"])
+@pytest.mark.parametrize("name", ["tg_d2q9_r15", "batch_uneven", "bounded_pulse_d2q9"])
 def test_shifted_windows_bitwise_equal(name):
     """Whole-cell displacements (D2Q9, dx = cell, FP32 store): the kernels that shift one window-row
     table per reference point give the same bits as the per-direction windows."""
@@ -391,6 +391,12 @@ def test_shifted_windows_bitwise_equal(name):
     if name in CASES:
         lattice, insts, dx, r, cell, build = CASES[name]
         x, f = build()
+        ib = None
+    elif name == "bounded_pulse_d2q9":  # points on cell corners (offsets exactly 0), bounded box
+        lattice, dx, r, cell = "D2Q9", 1.0, 1.5, 1.0
+        x, f = rest_pulse(6, "D2Q9")
+        dims, origin = bounded_box(x, 1.0, 8.0)
+        insts = [dict(dims=dims, origin=origin, periodic=False, tau=0.6)]
         ib = None
     else:
         lattice, dx, r, cell = "D2Q9", 1.0, 1.5, 1.0
