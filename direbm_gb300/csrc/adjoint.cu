@@ -151,11 +151,21 @@ __device__ __forceinline__ real unit_of(const PairRec<real, D>& pr, real (&u)[3]
     u[a] = pr.e[a];
     d2 += u[a] * u[a];
   }
-  const real d = sqrt(d2);
-  const real inv = d > (real)0 ? (real)1 / d : (real)0;
+  if constexpr (std::is_same<real, float>::value) {
+    // FP32 store: the hardware reciprocal square root (a few ulp), far inside the 2e-4 the FP32
+    // backward is held to against the FP64 reference; one instruction instead of a correctly
+    // rounded square root and a division
+    const float r = d2 > 0.f ? rsqrtf(d2) : 0.f;
 #pragma unroll
-  for (int a = 0; a < D; ++a) u[a] *= inv;
-  return d;
+    for (int a = 0; a < D; ++a) u[a] *= r;
+    return d2 * r;
+  } else {
+    const real d = sqrt(d2);
+    const real inv = d > (real)0 ? (real)1 / d : (real)0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) u[a] *= inv;
+    return d;
+  }
 }
 
 template <int D, class real>
