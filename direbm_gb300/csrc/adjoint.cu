@@ -1192,7 +1192,8 @@ struct TapeImpl : TapeBase, StepHook {
   int n_inst = 0;
   real R = 0;
   int64_t ncells = 0;
-  double* wk = nullptr;        // W_k in FP64 (export of FP32DEV f)
+  double* wk = nullptr;        // W_k in FP64 (export of FP32DEV f); written once, at the first step
+  bool wk_set = false;
   uint32_t* hbuf = nullptr;    // mapped pinned host words read back while recording
   uint32_t* hbuf_dev = nullptr;  // the same words as seen from the device
   uint32_t* d_count = nullptr; // slot counters of the six lists
@@ -1225,6 +1226,7 @@ struct TapeImpl : TapeBase, StepHook {
     if (done) cudaEventDestroy(done);
     if (hbuf) cudaFreeHost(hbuf);
     if (d_count) cudaFree(d_count);
+    if (wk) cudaFree(wk);
   }
 
   int init() {
@@ -1238,7 +1240,7 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_CUDA(cudaHostAlloc(&hbuf, 64, cudaHostAllocMapped));
     DBM_CUDA(cudaHostGetDevicePointer(&hbuf_dev, hbuf, 0));
     DBM_CUDA(cudaMalloc(&d_count, 6 * 4));
-    DBM_TRY(rec_mem.get(&wk, Q));
+    DBM_CUDA(cudaMalloc(&wk, sizeof(double) * Q));
     return DBM_OK;
   }
 
@@ -1249,8 +1251,6 @@ struct TapeImpl : TapeBase, StepHook {
     pending = -1;
     invalid = false;
     rec_mem.reset();
-    wk = nullptr;
-    DBM_TRY(rec_mem.get(&wk, Q));
     return DBM_OK;
   }
   int length() const override { return (int)steps.size(); }
@@ -1309,7 +1309,10 @@ struct TapeImpl : TapeBase, StepHook {
       DBM_TRY(fetch(src, 1, s));
       M = hbuf[0];
     }
-    if (wk) DBM_CUDA(cudaMemcpyAsync(wk, L.w, sizeof(double) * Q, cudaMemcpyHostToDevice, s));
+    if (!wk_set) {  // a copy from pageable memory waits for the stream: once, not at every step
+      DBM_CUDA(cudaMemcpyAsync(wk, L.w, sizeof(double) * Q, cudaMemcpyHostToDevice, s));
+      wk_set = true;
+    }
     StepRec<real, D>& r = cur;
     r.M = M;
     DBM_TRY(rec_mem.get(&r.in_cell, M));
