@@ -342,12 +342,18 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
   }
 }
 
-// Row-segment versions of the three bodies (shared-memory mode).  A window row's cells are
-// consecutive columns of one region row, whose items were staged contiguously in column order, so
-// the row is one item range [s_beg[first], s_end[last]) with no per-cell bookkeeping.  Each row's
-// column range is narrowed to the cells that can hold a hit given the row's smallest |e_y|; the
-// narrowing only drops cells with no hit, so sums (and their order) are those of the per-cell
-// loops.
+// ---- whole-cell displacements: one window-row table per reference point ------------------------
+//
+// When every displacement cd_k is a whole number of cells (D2Q9 with dx = cell), the canonical
+// c = (float(dS) + cd_k) - p of a window cell is rn_sub(float(j), p) with j = dS + cd_k exact, so
+// direction k's window around a reference point p is the window of cd = 0 shifted by -cd_k:
+// component row j (relative to p's cell) has the same c_y, the same half-width bound and the
+// same column range [a_j, b_j] for every direction; only the moment row j - cd_k,y and the moment
+// columns [a_j - cd_k,x, b_j - cd_k,x] move.  The table of rows is built once per reference point
+// instead of once per (point, direction).  The window bounds keep their 1e-4 cell margin, which
+// is far above the rounding of p - cd, so every hit lies inside the shifted window and the hits
+// are visited in the same order (rows ascending, then the row's items): sums are bit-identical to
+// the per-direction windows.
 
 // Rows of the whole-cell window tables: NR >= floor(2R + 2 tiny) + 2 (R < 2 cells).
 constexpr int kShiftRows = 5;
@@ -420,9 +426,15 @@ __device__ __forceinline__ void refine_shift(const Args<Q, 2, PF32>& A, int rw, 
   sxf[1] = sx.y;
 }
 
+// Row-segment versions of the three bodies (shared-memory mode).  A window row's cells are
+// consecutive columns of one region row, whose items were staged contiguously in column order, so
+// the row is one item range [s_beg[first], s_end[last]) with no per-cell bookkeeping.  Each row's
+// column range is narrowed to the cells that can hold a hit given the row's smallest |e_y|; the
+// narrowing only drops cells with no hit, so sums (and their order) are those of the per-cell
+// loops.
 
 // SHIFT (FP32 store, whole-cell displacements): the refine windows come from one row table of
-// the centroid, shifted per direction (see WinRows below); bit-identical to the per-direction
+// the centroid, shifted per direction (refine_shift above); bit-identical to the per-direction
 // windows.
 template <int Q, class P, bool SHIFT = false>
 __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const InstK& I, const Tile2& T,
@@ -1084,18 +1096,6 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
   }
 }
 
-// ---- whole-cell displacements: one window-row table per reference point ------------------------
-//
-// When every displacement cd_k is a whole number of cells (D2Q9 with dx = cell), the canonical
-// c = (float(dS) + cd_k) - p of a window cell is rn_sub(float(j), p) with j = dS + cd_k exact, so
-// direction k's window around a reference point p is the window of cd = 0 shifted by -cd_k:
-// component row j (relative to p's cell) has the same c_y, the same half-width bound and the
-// same column range [a_j, b_j] for every direction; only the moment row j - cd_k,y and the moment
-// columns [a_j - cd_k,x, b_j - cd_k,x] move.  The table of rows is built once per reference point
-// instead of once per (point, direction).  The window bounds keep their 1e-4 cell margin, which
-// is far above the rounding of p - cd, so every hit lies inside the shifted window and the hits
-// are visited in the same order (rows ascending, then the row's items): sums are bit-identical to
-// the per-direction windows.
 // A staged moment for the whole-cell gather: offsets, region column (exact small integer), rho,
 // then (1/sw, f*_k) of the kGatherGroup directions staged together, so a hit reads its operands
 // at a fixed offset from the candidate it just tested.
