@@ -124,6 +124,17 @@ struct alignas(2 * sizeof(real)) FsG {
   real fsi, g;
 };
 
+// Per moved control point, from its VJP to the component side's refine pairs: W = sum of the
+// refine weights, the position cotangent and the move s, in one record (one pair reads it with
+// two vector loads instead of five scalar ones).
+template <class real>
+struct alignas(16) CPBar {
+  real W;
+  real xb[3];
+  real s[3];
+  real pad;
+};
+
 // Everything a backward kernel reads, by value.
 template <int Q, int D, class P>
 struct RecK {
@@ -925,7 +936,7 @@ template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_cp(const __grid_constant__ RecK<Q, D, P> K,
                                                 const typename P::real* __restrict__ xrow, const typename P::real* __restrict__ Wrow,
                                                 const typename P::real* __restrict__ sxrow, typename P::real* __restrict__ xbarP,
-                                                typename P::real* __restrict__ Wj, typename P::real* __restrict__ sj,
+                                                CPBar<typename P::real>* __restrict__ cpb,
                                                 typename P::real* __restrict__ cenbar, int64_t ncells) {
   using real = typename P::real;
   const int64_t Pn = K.r.P, PQ = Pn * Q;
@@ -947,9 +958,14 @@ __global__ void __launch_bounds__(256) k_bwd_cp(const __grid_constant__ RecK<Q, 
 #pragma unroll
         for (int a = 0; a < D; ++a) sx[a] += sxrow[(int64_t)a * PQ + j * Q + k];
       }
-      Wj[j] = W;
+      CPBar<real> c{};
+      c.W = W;
 #pragma unroll
-      for (int a = 0; a < D; ++a) sj[(int64_t)a * Pn + j] = W > (real)0 ? sx[a] / W : (real)0;
+      for (int a = 0; a < D; ++a) {
+        c.xb[a] = x[a];
+        c.s[a] = W > (real)0 ? sx[a] / W : (real)0;
+      }
+      cpb[j] = c;
     } else {
       const uint32_t F = K.r.cp_thin[j];
       const real invn = (real)1 / (real)K.r.cp_n[j];
@@ -964,17 +980,14 @@ __global__ void __launch_bounds__(256) k_bwd_cp(const __grid_constant__ RecK<Q, 
 //   ybar_i += cenbar[thin cell of i]                                        (thinning)
 template <int Q, int D, class P>
 __global__ void __launch_bounds__(256) k_bwd_comp(const __grid_constant__ RecK<Q, D, P> K,
-                                                  const typename P::real* __restrict__ xbarP,
-                                                  const typename P::real* __restrict__ Wj, const typename P::real* __restrict__ sj,
+                                                  const CPBar<typename P::real>* __restrict__ cpb,
                                                   const typename P::real* __restrict__ cenbar, int64_t ncells,
                                                   const typename P::real* __restrict__ wexp,
                                                   typename P::real* __restrict__ fsbar, typename P::real* __restrict__ ybar) {
   using real = typename P::real;
-  const int64_t M = K.r.M, Pn = K.r.P, QM = (int64_t)Q * M;
+  const int64_t QM = (int64_t)Q * K.r.M;
   const auto& L = K.r.ref.t;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < QM; t += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(t / M);
-    const int64_t m = t - (int64_t)k * M;
     real y[3] = {0, 0, 0};
 #pragma unroll
     for (int a = 0; a < D; ++a) y[a] = ybar[(int64_t)a * QM + t];
@@ -989,14 +1002,14 @@ __global__ void __launch_bounds__(256) k_bwd_comp(const __grid_constant__ RecK<Q
       const real w = wexp[t];
       for (uint32_t q = q0; q < q1; ++q) {
         const auto pr = L.rec[q];
-        const uint32_t j = pr.row;
-        const real wW = w / Wj[j];
+        const CPBar<real> c = cpb[pr.row];  // a refine pair's control point has moved
+        const real wW = w / c.W;
         real dot = 0;
 #pragma unroll
         for (int a = 0; a < D; ++a) {
-          const real pb = xbarP[(int64_t)a * Pn + j];
+          const real pb = c.xb[a];
           y[a] += wW * pb;
-          dot += (pr.e[a] - sj[(int64_t)a * Pn + j]) * pb;
+          dot += (pr.e[a] - c.s[a]) * pb;
         }
         g += wW * dot;
       }
@@ -1563,7 +1576,8 @@ struct TapeImpl : TapeBase, StepHook {
     }
     DBM_CUDA(cudaStreamWaitEvent(s, done, 0));  // the previous call's scratch is free
     bwd_mem.reset();
-    real *xbarP, *fbarG, *sbarG, *fsbar, *ybar, *wexp, *xrow, *Wrow, *sxrow, *Wj, *sj, *cenbar;
+    real *xbarP, *fbarG, *sbarG, *fsbar, *ybar, *wexp, *xrow, *Wrow, *sxrow, *cenbar;
+    CPBar<real>* cpb;
     FsG<real>* fg;
     double *taupart, *blocksum;
     DBM_TRY(bwd_mem.get(&xbarP, (int64_t)D * Pn));
@@ -1576,8 +1590,7 @@ struct TapeImpl : TapeBase, StepHook {
     DBM_TRY(bwd_mem.get(&xrow, (int64_t)D * PQ));
     DBM_TRY(bwd_mem.get(&Wrow, PQ));
     DBM_TRY(bwd_mem.get(&sxrow, (int64_t)D * PQ));
-    DBM_TRY(bwd_mem.get(&Wj, Pn));
-    DBM_TRY(bwd_mem.get(&sj, (int64_t)D * Pn));
+    DBM_TRY(bwd_mem.get(&cpb, Pn));
     DBM_TRY(bwd_mem.get(&cenbar, (int64_t)D * ncells));
     DBM_TRY(bwd_mem.get(&taupart, M));
     DBM_TRY(bwd_mem.get(&blocksum, (int64_t)n_inst * kTauSplit));
@@ -1598,11 +1611,11 @@ struct TapeImpl : TapeBase, StepHook {
     if (Pn > 0) {
       k_bwd_rows<Q, D, P><<<grid_for(PQ), 256, 0, s>>>(K, fg, wexp, fbarG, xrow, Wrow, sxrow);
       DBM_LAUNCH_CHECK();
-      k_bwd_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xrow, Wrow, sxrow, xbarP, Wj, sj, cenbar, ncells);
+      k_bwd_cp<Q, D, P><<<grid_for(Pn), 256, 0, s>>>(K, xrow, Wrow, sxrow, xbarP, cpb, cenbar, ncells);
       DBM_LAUNCH_CHECK();
     }
     if (M > 0) {
-      k_bwd_comp<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, xbarP, Wj, sj, cenbar, ncells, wexp, fsbar, ybar);
+      k_bwd_comp<Q, D, P><<<grid_for(QM), 256, 0, s>>>(K, cpb, cenbar, ncells, wexp, fsbar, ybar);
       DBM_LAUNCH_CHECK();
       k_bwd_moment<Q, D, P><<<grid_for(M), 256, 0, s>>>(K, fsbar, ybar, goff_in, gf_in, taupart);
       DBM_LAUNCH_CHECK();
