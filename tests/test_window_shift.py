@@ -94,3 +94,54 @@ def test_shifted_windows_visit_the_same_hits_in_the_same_order():
                 off[key] = (f32(0), f32(edges[t % len(edges)]))
         for cdx, cdy in CD:
             assert _per_direction(p, off, cdx, cdy) == _shifted(p, off, cdx, cdy), (p, cdx, cdy)
+
+
+def _lb_row(o_y, basey):
+    ely, ehy = f32(o_y + f32(basey - f32(1))), f32(o_y + basey)
+    return ely if ely > 0 else (-ehy if ehy < 0 else f32(0))
+
+
+def _cp_hits(o, cps, rows):
+    """Weights-side hits of component (moment offset o, direction cd): rows = [(gy, basey, lo, hi,
+    cdx)] in control-point cell coordinates relative to the moment's cell; e = o + (base - p)."""
+    out = []
+    for gy, basey, lo, hi, cdx in rows:
+        for gx in range(lo, hi + 1):
+            p = cps.get((gx, gy))
+            if p is None:
+                continue
+            basex = f32(f32(-gx) + f32(cdx))
+            ex, ey = f32(o[0] + f32(basex - p[0])), f32(o[1] + f32(basey - p[1]))
+            if f32(f32(ex * ex) + f32(ey * ey)) <= R2:
+                out.append((gx, gy))
+    return out
+
+
+def test_shifted_weights_windows_visit_the_same_control_points():
+    """The weights kernel's form: a component's control-point window rows depend on its moment's
+    offset alone, shifted by cd_k (weights_rows_shift against weights_rows)."""
+    rng = np.random.default_rng(12)
+    edges = np.array([0.0, 0.5, 1 - 2 ** -24, 2 ** -24, 0.25], dtype=np.float32)
+    offsets = [rng.random(2).astype(np.float32) for _ in range(300)]
+    offsets += [np.array([a, b], dtype=np.float32) for a in edges for b in edges]
+    for o in offsets:
+        cps = {(gx, gy): rng.random(2).astype(np.float32) for gx in range(-4, 5) for gy in range(-4, 5)}
+        for cdx, cdy in CD:
+            tx, ty = f32(o[0] + f32(cdx)), f32(o[1] + f32(cdy))
+            rows_a = []
+            for gy in range(int(np.floor(f32(f32(ty - R) - TINY))), int(np.floor(f32(f32(ty + R) + TINY))) + 1):
+                basey = f32(f32(-gy) + f32(cdy))
+                hw = _halfwidth(_lb_row(o[1], basey))
+                if hw >= 0:
+                    rows_a.append((gy, basey, int(np.floor(f32(f32(tx - hw) - TINY))),
+                                   int(np.floor(f32(f32(tx + hw) + TINY))), cdx))
+            rows_b = []
+            ulo, uhi = int(np.floor(f32(f32(o[1] - R) - TINY))), int(np.floor(f32(f32(o[1] + R) + TINY)))
+            assert uhi - ulo + 1 <= 5
+            for u in range(ulo, uhi + 1):
+                basey = f32(-u)
+                hw = _halfwidth(_lb_row(o[1], basey))
+                if hw >= 0:
+                    a, b = int(np.floor(f32(f32(o[0] - hw) - TINY))), int(np.floor(f32(f32(o[0] + hw) + TINY)))
+                    rows_b.append((u + cdy, basey, a + cdx, b + cdx, cdx))
+            assert _cp_hits(o, cps, rows_a) == _cp_hits(o, cps, rows_b), (o, cdx, cdy)
