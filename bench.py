@@ -221,8 +221,8 @@ def roofline_from_profile(sim, M, P, peak):
     return dom, avg, {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                       "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
                       "ms_per_launch": avg[dom], "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
-                      "traffic_source": ("ncu DRAM bytes of a 4.18 M-moment launch, scaled by moments "
-                                         "(profiles/gather_ts_full_ensemble64.md)") if per_m else None}
+                      "traffic_source": "ncu DRAM bytes of a 4.18 M-moment launch, scaled by moments"
+                      if per_m else None}
 
 
 def velocity_l2(f, lat):

@@ -251,6 +251,12 @@ class _Rollout(torch.autograd.Function):
                     if attempt == 2:
                         raise
         main.wait_stream(vjp)
+        if vjp is not main:
+            # g_off and g_f were allocated on the VJP stream and are read below on the main
+            # stream: tell the caching allocator, so their blocks are not handed to a later
+            # allocation on the VJP stream before the main stream's reads have run
+            g_off.record_stream(main)
+            g_f.record_stream(main)
         for t in tapes:
             t.clear()
         sim.restore(ctx.final, ctx.steps)

@@ -12,7 +12,10 @@
 //  * at most DBM_NOALLOC_SORT_MAX_PAIRS pairs per call; larger requests are rejected with
 //    DBM_ERR_CAPACITY before any work is queued;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress, with
-//    that device current) and caches it; make that first call before any stream capture;
+//    that device current) and caches it; make that first call before any stream capture.  The
+//    cached address is valid only while the device's primary context lives: after a
+//    cudaDeviceReset in the same process it would point at freed memory, so such a process must
+//    not call this entry point again;
 //  * all calls share the one array: two calls whose work overlaps on the GPU (different streams,
 //    no ordering between them) race and corrupt each other's results; order them on one stream
 //    or with events;

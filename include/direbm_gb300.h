@@ -72,8 +72,10 @@ int dbm_radix_sort_pairs_u64(uint64_t* d_keys, uint32_t* d_vals, int64_t n, int 
  * array compiled into the library instead (about 2.2 MB held on every GPU that loads it until the
  * process exits) and never allocates or frees.  At most DBM_NOALLOC_SORT_MAX_PAIRS pairs per
  * call (larger n returns DBM_ERR_CAPACITY).  The first call on each device looks up the scratch
- * address; make it before any stream capture.  Calls share the scratch: calls that overlap on
- * the GPU race, so order them on one stream. */
+ * address; make it before any stream capture.  That address is cached for the life of the
+ * process and stays valid only while the device's context does: after cudaDeviceReset (or any
+ * teardown of the primary context) do not call this entry point again in the same process.
+ * Calls share the scratch: calls that overlap on the GPU race, so order them on one stream. */
 #define DBM_NOALLOC_SORT_MAX_PAIRS 262144
 int dbm_radix_sort_pairs_u32_noalloc(uint32_t* d_keys, uint32_t* d_vals, int64_t n, int key_bits, void* stream);
 

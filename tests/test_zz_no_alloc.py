@@ -50,7 +50,11 @@ def test_noalloc_sort_matches_caller_scratch_sort_on_consecutive_calls():
     lib, L = _lib()
     # two calls in a row that share the static scratch: a full-size one, then a smaller one with
     # different data (stale contents of the first call must not leak into the second)
-    for seed, n, bits in ((1, MAX_PAIRS, 24), (2, 100_003, 17)):
+    # 24 and 17 key bits take three 8-bit passes (the result lands in the static alternate buffers
+    # and is copied back); 32 and 16 bits take an even number of passes (the result ends in the
+    # caller's buffers and the static scratch only ping-pongs); the 32-bit case spans the full key
+    # range at the size limit
+    for seed, n, bits in ((1, MAX_PAIRS, 24), (2, 100_003, 17), (3, MAX_PAIRS, 32), (4, 65_537, 16)):
         rng = np.random.default_rng(seed)
         keys = rng.integers(0, 1 << bits, size=n, dtype=np.uint64).astype(np.uint32)
         keys[: n // 4] = keys[0]  # long runs of equal keys: the sort must stay stable
@@ -67,10 +71,14 @@ def test_noalloc_sort_matches_caller_scratch_sort_on_consecutive_calls():
 def test_noalloc_sort_rejects_sizes_beyond_its_scratch():
     lib, L = _lib()
     n = MAX_PAIRS + 1
-    k = torch.zeros(n, dtype=torch.int32, device="cuda")
+    # descending 8-bit keys: any sort that ran would reorder both arrays
+    keys = (255 - (np.arange(n, dtype=np.int64) * 256) // n).astype(np.int32)
+    k = torch.tensor(keys, device="cuda")
     v = torch.arange(n, dtype=torch.int32, device="cuda")
     rc = lib.dbm_radix_sort_pairs_u32_noalloc(k.data_ptr(), v.data_ptr(), n, 8, _stream())
     assert rc == 3  # DBM_ERR_CAPACITY
     assert b"static scratch limit" in lib.dbm_last_error()
     torch.cuda.synchronize()
-    assert torch.equal(v, torch.arange(n, dtype=torch.int32, device="cuda"))  # nothing was queued
+    # nothing was queued: keys and values are exactly as they went in
+    assert torch.equal(k, torch.tensor(keys, device="cuda"))
+    assert torch.equal(v, torch.arange(n, dtype=torch.int32, device="cuda"))
