@@ -1010,7 +1010,7 @@ __global__ void __launch_bounds__(256) k_conservation(const __grid_constant__ Ar
 
 }  // namespace dbm
 
-#include "sim_tiled.cuh"
+#include "sim_dense.cuh"
 
 namespace dbm {
 
@@ -1084,6 +1084,11 @@ struct SimImpl : SimBase {
   int pgrid_s = 1, pgrid_rs = 1, pgrid_ws = 1;
   TileGeo geo_s{};
   size_t sm_gather_s = 0;
+  // dense-stencil kernels (k_*_ds, shared memory = the dense layout) and the list of tiles they
+  // defer to the row-segment code: d_fb[0..2] the per-stage counts, d_fb + 4 the tile indices
+  size_t sm_ds[3] = {0, 0, 0};  // thin+refine, weights, gather
+  int pgrid_ds[3] = {1, 1, 1};
+  int* d_fb = nullptr;
   int use_persistent = 0;
   TileGeo geo{};
   size_t sm_refine = 0, sm_weights = 0, sm_gather = 0;
@@ -1411,6 +1416,9 @@ struct SimImpl : SimBase {
     if (shift_ok) {
       geo_s.cap_gather = pick_cap(3, mcells, budget);
       sm_gather_s = smem_for(3, geo_s.cap_gather);
+      sm_ds[0] = ds_bytes_refine(Q, mcells);
+      sm_ds[1] = ds_bytes_weights(ccells);
+      sm_ds[2] = ds_bytes_gather(Q, mcells);
     }
     std::vector<Tile2> tiles;
     for (int i = 0; i < (int)inst_h.size(); ++i)
@@ -1423,6 +1431,14 @@ struct SimImpl : SimBase {
     }
     DBM_TRY(alloc(&d_tiles, ntiles));
     DBM_CUDA(cudaMemcpy(d_tiles, tiles.data(), sizeof(Tile2) * ntiles, cudaMemcpyHostToDevice));
+    if (d_fb) {
+      release(d_fb);
+      d_fb = nullptr;
+    }
+    if (shift_ok) {
+      DBM_TRY(alloc(&d_fb, (int64_t)ntiles + 4));
+      DBM_CUDA(cudaMemset(d_fb, 0, ((size_t)ntiles + 4) * sizeof(int)));
+    }
     if constexpr (D == 2) {
       DBM_CUDA(cudaFuncSetAttribute((const void*)k_thin_refine_t<Q, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)sm_refine));
@@ -1452,6 +1468,20 @@ struct SimImpl : SimBase {
           int nbw = 1;
           DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbw, k_weights_t<Q, P, true>, 256, sm_weights));
           pgrid_ws = std::max(1, std::min(ntiles, std::max(nbw, 1) * sm_count()));
+          const void* kds[3] = {(const void*)k_thin_refine_ds<Q>, (const void*)k_weights_ds<Q>,
+                                (const void*)k_gather_ds<Q>};
+          for (int i = 0; i < 3; ++i) {
+            DBM_CUDA(cudaFuncSetAttribute(kds[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_ds[i]));
+            int nbd = 1;
+            DBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbd, kds[i], 256, sm_ds[i]));
+            pgrid_ds[i] = std::max(1, std::min(ntiles, std::max(nbd, 1) * sm_count()));
+          }
+          DBM_CUDA(cudaFuncSetAttribute((const void*)k_dense_fallback<Q, 0>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_refine));
+          DBM_CUDA(cudaFuncSetAttribute((const void*)k_dense_fallback<Q, 1>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_weights));
+          DBM_CUDA(cudaFuncSetAttribute((const void*)k_dense_fallback<Q, 2>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_gather_s));
         }
       }
     }
@@ -1610,7 +1640,14 @@ struct SimImpl : SimBase {
       if (tiled_path()) {
         bool shifted = false;
         if constexpr (std::is_same<P, PF32>::value) {
-          if (shift_ok && use_shift) {
+          if (shift_ok && use_shift && use_dense) {
+            DBM_CUDA(cudaMemsetAsync(d_fb, 0, 3 * sizeof(int), s));  // the three stages' fallback counts
+            k_thin_refine_ds<Q><<<use_persistent ? pgrid_ds[0] : ntiles, 256, sm_ds[0], s>>>(A, d_tiles, geo, ntiles,
+                                                                                            d_fb + 4, d_fb + 0);
+            DBM_LAUNCH_CHECK();
+            k_dense_fallback<Q, 0><<<pgrid_rs, 256, sm_refine, s>>>(A, d_tiles, geo, d_fb + 4, d_fb + 0);
+            shifted = true;
+          } else if (shift_ok && use_shift) {
             k_thin_refine_t<Q, P, true><<<use_persistent ? pgrid_rs : ntiles, 256, sm_refine, s>>>(A, d_tiles, geo,
                                                                                                   ntiles);
             shifted = true;
@@ -1665,7 +1702,13 @@ struct SimImpl : SimBase {
       if (tiled_path()) {
         bool shifted = false;
         if constexpr (std::is_same<P, PF32>::value) {
-          if (shift_ok && use_shift) {
+          if (shift_ok && use_shift && use_dense) {
+            k_weights_ds<Q><<<use_persistent ? pgrid_ds[1] : ntiles, 256, sm_ds[1], s>>>(A, d_tiles, geo, ntiles,
+                                                                                        d_fb + 4, d_fb + 1);
+            DBM_LAUNCH_CHECK();
+            k_dense_fallback<Q, 1><<<pgrid_ws, 256, sm_weights, s>>>(A, d_tiles, geo, d_fb + 4, d_fb + 1);
+            shifted = true;
+          } else if (shift_ok && use_shift) {
             k_weights_t<Q, P, true><<<use_persistent ? pgrid_ws : ntiles, 256, sm_weights, s>>>(A, d_tiles, geo,
                                                                                                ntiles);
             shifted = true;
@@ -1687,7 +1730,13 @@ struct SimImpl : SimBase {
       if (tiled_path()) {
         bool shifted = false;
         if constexpr (std::is_same<P, PF32>::value) {
-          if (shift_ok && use_shift) {
+          if (shift_ok && use_shift && use_dense) {
+            k_gather_ds<Q><<<use_persistent ? pgrid_ds[2] : ntiles, 256, sm_ds[2], s>>>(A, d_tiles, geo_s, ntiles,
+                                                                                       d_fb + 4, d_fb + 2);
+            DBM_LAUNCH_CHECK();
+            k_dense_fallback<Q, 2><<<pgrid_s, 256, sm_gather_s, s>>>(A, d_tiles, geo_s, d_fb + 4, d_fb + 2);
+            shifted = true;
+          } else if (shift_ok && use_shift) {
             k_gather_ts<Q><<<use_persistent ? pgrid_s : ntiles, 256, sm_gather_s, s>>>(A, d_tiles, geo_s, ntiles);
             shifted = true;
           }
@@ -2177,6 +2226,8 @@ int dbm_sim_set_option(dbm_sim* s, int32_t option, int32_t value) {
     return s->impl->set_brick(value);
   } else if (option == DBM_OPT_SHIFTED_WINDOWS) {
     s->impl->use_shift = value ? 1 : 0;
+  } else if (option == DBM_OPT_DENSE_STENCIL) {
+    s->impl->use_dense = value ? 1 : 0;
   } else {
     set_last_error("dbm_sim_set_option: unknown option %d", option);
     return DBM_ERR_INVALID;

@@ -346,6 +346,7 @@ struct SimBase {
   int use_graphs = 1;
   int use_tiles = 1;
   int use_shift = 1;  // DBM_OPT_SHIFTED_WINDOWS
+  int use_dense = 1;  // DBM_OPT_DENSE_STENCIL
   uint64_t version = 0;  // bumped by every change of the state (load, step, restore)
   int lattice = 0;
   int precision = 0;

@@ -593,14 +593,11 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
 // blockIdx.x + gridDim.x, ...): launched with one block per tile they are ordinary kernels;
 // launched with fewer blocks (a few per SM) they are persistent.  Either way each tile is processed
 // by one block with the same per-thread loop order, so results do not depend on the launch.
-template <int Q, class P, bool SHIFT = false>
-__global__ void __launch_bounds__(256) k_thin_refine_t(const __grid_constant__ Args<Q, 2, P> A,
-                                                      const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
+// One tile of thinning + refine, staged through `smem` (the block's dynamic shared memory).
+template <int Q, class P, bool SHIFT>
+__device__ __forceinline__ void thin_refine_tile(const Args<Q, 2, P>& A, const Tile2& T, const InstK& I,
+                                                 const TileGeo& G, unsigned char* smem) {
   using real = typename P::real;
-  extern __shared__ __align__(16) unsigned char smem[];
-  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
-  const Tile2 T = tiles[tb];
-  const InstK I = A.inst[T.inst];
   const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
   const int cap = G.cap_refine;
   unsigned char* p = smem;
@@ -620,7 +617,17 @@ __global__ void __launch_bounds__(256) k_thin_refine_t(const __grid_constant__ A
   } else {
     thin_refine_body<Q, P, false>(A, I, T, G, rw, rh, s_beg, s_end, nullptr, nullptr, nullptr, 0);
   }
-  __syncthreads();  // shared memory is restaged for the next tile
+}
+
+template <int Q, class P, bool SHIFT = false>
+__global__ void __launch_bounds__(256) k_thin_refine_t(const __grid_constant__ Args<Q, 2, P> A,
+                                                      const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const Tile2 T = tiles[tb];
+    const InstK I = A.inst[T.inst];
+    thin_refine_tile<Q, P, SHIFT>(A, T, I, G, smem);
+    __syncthreads();  // shared memory is restaged for the next tile
   }
 }
 
@@ -875,14 +882,11 @@ __device__ __forceinline__ void weights_rows_shift(const Args<Q, 2, PF32>& A, co
   }
 }
 
-template <int Q, class P, bool SHIFT = false>
-__global__ void __launch_bounds__(256) k_weights_t(const __grid_constant__ Args<Q, 2, P> A,
-                                                  const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
+// One tile of the weights kernel, staged through `smem`.
+template <int Q, class P, bool SHIFT>
+__device__ __forceinline__ void weights_tile(const Args<Q, 2, P>& A, const Tile2& T, const InstK& I,
+                                             const TileGeo& G, unsigned char* smem) {
   using real = typename P::real;
-  extern __shared__ __align__(16) unsigned char smem[];
-  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
-  const Tile2 T = tiles[tb];
-  const InstK I = A.inst[T.inst];
   const int rw = G.tx + G.cp.xh - G.cp.xl, rh = G.ty + G.cp.yh - G.cp.yl;
   const int cap = G.cap_weights, cap_t = G.cap_tile;
   unsigned char* p = smem;
@@ -905,7 +909,17 @@ __global__ void __launch_bounds__(256) k_weights_t(const __grid_constant__ Args<
     else weights_rows<Q, P>(A, I, T, G, rw, rh, s_beg, s_end, s_cit, s_tr, s_ij, s_bx, s_by, s_mpos);
   }
   else weights_body<Q, P, false>(A, I, T, G, rw, rh, s_beg, s_end, nullptr, s_tr, s_ij, s_bx, s_by, s_mpos);
-  __syncthreads();
+}
+
+template <int Q, class P, bool SHIFT = false>
+__global__ void __launch_bounds__(256) k_weights_t(const __grid_constant__ Args<Q, 2, P> A,
+                                                  const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const Tile2 T = tiles[tb];
+    const InstK I = A.inst[T.inst];
+    weights_tile<Q, P, SHIFT>(A, T, I, G, smem);
+    __syncthreads();
   }
 }
 
@@ -1207,6 +1221,37 @@ __device__ __forceinline__ void gather_rows_shift(const Args<Q, 2, PF32>& A, con
   }
 }
 
+// One tile of the whole-cell gather, staged through `smem`.
+template <int Q>
+__device__ __forceinline__ void gather_ts_tile(const Args<Q, 2, PF32>& A, const Tile2& T, const InstK& I,
+                                               const TileGeo& G, unsigned char* smem) {
+  const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
+  const int cap = G.cap_gather, cap_t = G.cap_tile;
+  unsigned char* p = smem;
+  int* s_beg = carve<int>(p, rw * rh);
+  int* s_end = carve<int>(p, rw * rh);
+  int* s_row = carve<int>(p, rh + 2);
+  int* s_gi = carve<int>(p, cap);
+  GRec* s_rec = carve<GRec>(p, cap);
+  int* s_tr = carve<int>(p, 2 * G.ty + 2);
+  int* s_ij = carve<int>(p, cap_t);
+  short* s_bx = carve<short>(p, cap_t);
+  short* s_by = carve<short>(p, cap_t);
+  Pair<float>* s_cpos = carve<Pair<float>>(p, cap_t);
+  stage_region(I, T.x0 + G.mom.xl, T.y0 + G.mom.yl, rw, rh, A.a.start, cap, s_beg, s_end, s_row,
+               [&](int gm, int l, int rx) {
+                 s_gi[l] = gm;
+                 *reinterpret_cast<float4*>(&s_rec[l]) =
+                     make_float4(A.a.off[gm], A.a.off[A.mcap + gm], (float)rx, A.a.rho[gm]);
+               });
+  if (s_row[rh + 1])
+    gather_rows_shift<Q, kShiftRows>(A, I, T, G, rw, rh, s_beg, s_end, s_gi, s_rec, s_row[rh], s_tr, s_ij, s_bx,
+                                     s_by, s_cpos);
+  else
+    gather_body<Q, PF32, false>(A, I, T, G, rw, rh, s_beg, s_end, s_gi, nullptr, nullptr, nullptr, 0, s_tr, s_ij,
+                                s_bx, s_by, s_cpos);
+}
+
 template <int Q>
 __global__ void __launch_bounds__(256) k_gather_ts(const __grid_constant__ Args<Q, 2, PF32> A,
                                                   const Tile2* __restrict__ tiles, const TileGeo G, int ntiles) {
@@ -1214,31 +1259,7 @@ __global__ void __launch_bounds__(256) k_gather_ts(const __grid_constant__ Args<
   for (int tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
     const Tile2 T = tiles[tb];
     const InstK I = A.inst[T.inst];
-    const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
-    const int cap = G.cap_gather, cap_t = G.cap_tile;
-    unsigned char* p = smem;
-    int* s_beg = carve<int>(p, rw * rh);
-    int* s_end = carve<int>(p, rw * rh);
-    int* s_row = carve<int>(p, rh + 2);
-    int* s_gi = carve<int>(p, cap);
-    GRec* s_rec = carve<GRec>(p, cap);
-    int* s_tr = carve<int>(p, 2 * G.ty + 2);
-    int* s_ij = carve<int>(p, cap_t);
-    short* s_bx = carve<short>(p, cap_t);
-    short* s_by = carve<short>(p, cap_t);
-    Pair<float>* s_cpos = carve<Pair<float>>(p, cap_t);
-    stage_region(I, T.x0 + G.mom.xl, T.y0 + G.mom.yl, rw, rh, A.a.start, cap, s_beg, s_end, s_row,
-                 [&](int gm, int l, int rx) {
-                   s_gi[l] = gm;
-                   *reinterpret_cast<float4*>(&s_rec[l]) =
-                       make_float4(A.a.off[gm], A.a.off[A.mcap + gm], (float)rx, A.a.rho[gm]);
-                 });
-    if (s_row[rh + 1])
-      gather_rows_shift<Q, kShiftRows>(A, I, T, G, rw, rh, s_beg, s_end, s_gi, s_rec, s_row[rh], s_tr, s_ij, s_bx,
-                                       s_by, s_cpos);
-    else
-      gather_body<Q, PF32, false>(A, I, T, G, rw, rh, s_beg, s_end, s_gi, nullptr, nullptr, nullptr, 0, s_tr, s_ij,
-                                  s_bx, s_by, s_cpos);
+    gather_ts_tile<Q>(A, T, I, G, smem);
     __syncthreads();
   }
 }

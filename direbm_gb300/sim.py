@@ -294,6 +294,7 @@ class Simulation:
 
     # ---- launch configuration -------------------------------------------------------------------
     OPT_TILE_WIDTH, OPT_PERSISTENT, OPT_KAPPA_SOFT, OPT_BRICK_WIDTH, OPT_SHIFTED_WINDOWS = 3, 4, 5, 6, 7
+    OPT_DENSE_STENCIL = 8
 
     def tiling(self) -> tuple:
         """(tile width in cells, persistent launches) of the 2D tiled kernels."""
@@ -318,6 +319,14 @@ class Simulation:
         with torch.cuda.device(self.device):
             _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_SHIFTED_WINDOWS, 1 if on else 0),
                        "set shifted windows")
+
+    def set_dense_stencil(self, on: bool):
+        """With the shifted windows: stage a tile whose cells each hold at most one moment and one
+        control point as a dense grid and run every window as a fixed 4 x 4 block of cells (default
+        on); other tiles take the row-segment loops.  Results are bit-identical either way."""
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.dbm_sim_set_option(self._h, self.OPT_DENSE_STENCIL, 1 if on else 0),
+                       "set dense stencil")
 
     def brick_width(self) -> int:
         """Cells along x of the 256-cell bricks the untiled window kernels give each block."""

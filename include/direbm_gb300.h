@@ -192,6 +192,12 @@ int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
  * window rows per reference point and shift it for each direction instead of building a window
  * per (point, direction) (default 1).  Results are bit-identical either way. */
 #define DBM_OPT_SHIFTED_WINDOWS 7
+/* DBM_OPT_DENSE_STENCIL (2D, FP32 store, with the shifted windows): a tile whose cells each hold at
+ * most one moment and one control point (in D2Q9 runs with dx = cell, every cell holds exactly
+ * one) is staged as a dense grid and every window becomes a fixed 4 x 4 block of cells; other
+ * tiles take the row-segment loops in the same launch (default 1).  Results are bit-identical
+ * either way. */
+#define DBM_OPT_DENSE_STENCIL 8
 int dbm_sim_get_brick_width(dbm_sim* sim, int32_t* brick_width);
 int dbm_sim_set_option(dbm_sim* sim, int32_t option, int32_t value);
 int dbm_sim_get_tiling(dbm_sim* sim, int32_t* tile_width, int32_t* persistent);

@@ -423,3 +423,65 @@ def test_shifted_windows_bitwise_equal(name):
         assert sim.status() == 0
     for a, b in zip(outs[0], outs[1]):
         np.testing.assert_array_equal(a, b)
+
+
+def _d2q9_field(xx, n0, n1, amp=0.03):
+    from oracle.lattices import D2Q9
+    from oracle.physics import equilibrium
+
+    u = amp * np.stack([np.sin(2 * np.pi * xx[:, 1] / n1), np.cos(2 * np.pi * xx[:, 0] / n0)], 1)
+    return equilibrium(np.ones(len(xx)), u, D2Q9)
+
+
+@pytest.mark.parametrize("name", ["batch_uneven", "mixed_density", "cell_centres", "bounded_pulse_d2q9"])
+def test_dense_stencil_bitwise_equal(name):
+    """The dense-stencil kernels (one item per cell, fixed 4 x 4 windows) give the same bits as the
+    row-segment shifted windows.  Cases: a batch of jittered grids (dense everywhere); a box whose
+    right half holds uniformly random points (cells with two or more moments send their tiles to the
+    row-segment fallback in the first step, and empty cells take the empty-slot path); points at the
+    exact cell centres (every reference offset is 1/2, where the stencil is five cells wide); and a
+    bounded box around a pulse (empty cells outside the material, offsets exactly 0)."""
+    from direbm_gb300.sim import Instance, Simulation
+
+    lattice, dx, r, cell = "D2Q9", 1.0, 1.5, 1.0
+    rng = np.random.default_rng(33)
+    ib = None
+    if name == "batch_uneven":
+        insts = [dict(dims=(n, n), periodic=True, tau=t) for n, t in ((70, 0.6), (23, 0.95), (41, 0.55))]
+        xs, fs, bs = [], [], []
+        for b, ins in enumerate(insts):
+            n0, n1 = ins["dims"]
+            xx = np.stack(np.meshgrid(np.arange(n0) + 0.5, np.arange(n1) + 0.5), -1).reshape(-1, 2)
+            xx = np.mod(xx + rng.uniform(-0.25, 0.25, xx.shape), [n0, n1])
+            xs.append(xx)
+            fs.append(_d2q9_field(xx, n0, n1))
+            bs.append(np.full(len(xx), b))
+        x, f, ib = np.concatenate(xs), np.concatenate(fs), np.concatenate(bs)
+    elif name == "mixed_density":
+        n0, n1 = 64, 48
+        insts = [dict(dims=(n0, n1), periodic=True, tau=0.7)]
+        xx = np.stack(np.meshgrid(np.arange(n0 // 2) + 0.5, np.arange(n1) + 0.5), -1).reshape(-1, 2)
+        xx = xx + rng.uniform(-0.25, 0.25, xx.shape)
+        xr = np.stack([rng.uniform(n0 // 2, n0, xx.shape[0]), rng.uniform(0, n1, xx.shape[0])], 1)
+        x = np.mod(np.concatenate([xx, xr]), [n0, n1])
+        f = _d2q9_field(x, n0, n1)
+    elif name == "cell_centres":
+        n0, n1 = 40, 36
+        insts = [dict(dims=(n0, n1), periodic=True, tau=0.8)]
+        x = np.stack(np.meshgrid(np.arange(n0) + 0.5, np.arange(n1) + 0.5), -1).reshape(-1, 2)
+        f = _d2q9_field(x, n0, n1)
+    else:
+        x, f = rest_pulse(6, "D2Q9")
+        dims, origin = bounded_box(x, 1.0, 8.0)
+        insts = [dict(dims=dims, origin=origin, periodic=False, tau=0.6)]
+    outs = []
+    for on in (True, False):
+        sim = Simulation([Instance(**i) for i in insts], lattice=lattice, precision="fp32dev", dx=dx, r_res=r,
+                         cell=cell)
+        sim.set_dense_stencil(on)
+        sim.set_state(ib, x, f)
+        sim.step(4)
+        outs.append(sim.state_numpy())
+        assert sim.status() == 0
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
