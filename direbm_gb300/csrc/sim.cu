@@ -503,21 +503,25 @@ __global__ void __launch_bounds__(256) k_place(const __grid_constant__ Args<Q, D
   for (uint32_t F = blockIdx.x * blockDim.x + threadIdx.x; F < A.ncells; F += gridDim.x * blockDim.x) {
     if (!A.occ[F]) continue;
     const uint32_t G = A.fkey[F];
-    const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
-    int Gc[3];
-    decode_cell<D>(I, G, Gc);
-    uint32_t rank = 0, all = 0;
-    for (int dy = -H; dy <= H; ++dy)
-      for (int dx = -H; dx <= H; ++dx) {
-        uint32_t Fp;
-        if (!cell_at<D>(I, Gc[0] + dx, Gc[1] + dy, 0, &Fp)) continue;
-        const uint32_t hit = A.fkey[Fp] == G ? 1u : 0u;  // fkey is all ones where no control point was made
-        all += hit;
-        rank += Fp < F ? hit : 0u;
-      }
-    // every control point of G comes from this neighbourhood (the move bound): check it
-    if (all != A.b.start[G + 1] - A.b.start[G]) atomicOr(A.status, ST_INTERNAL);
-    const uint32_t j = A.b.start[G] + rank;
+    const uint32_t g0 = A.b.start[G], ng = A.b.start[G + 1] - g0;
+    uint32_t rank = 0;
+    if (ng != 1u) {  // a cell with one control point needs no rank (the common case: one per cell)
+      const InstK I = A.inst[find_instance(A.inst_base, A.n_inst, G)];
+      int Gc[3];
+      decode_cell<D>(I, G, Gc);
+      uint32_t all = 0;
+      for (int dy = -H; dy <= H; ++dy)
+        for (int dx = -H; dx <= H; ++dx) {
+          uint32_t Fp;
+          if (!cell_at<D>(I, Gc[0] + dx, Gc[1] + dy, 0, &Fp)) continue;
+          const uint32_t hit = A.fkey[Fp] == G ? 1u : 0u;  // fkey is all ones where no control point was made
+          all += hit;
+          rank += Fp < F ? hit : 0u;
+        }
+      // every control point of G comes from this neighbourhood (the move bound): check it
+      if (all != ng) atomicOr(A.status, ST_INTERNAL);
+    }
+    const uint32_t j = g0 + rank;
     keys[j] = G;
     vals[j] = F;
     A.b.cell[j] = G;

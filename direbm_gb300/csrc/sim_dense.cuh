@@ -384,12 +384,24 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
 // own.  The order of the fallback list is arbitrary, which changes no result: tiles write
 // disjoint outputs.
 
+// Resident blocks per SM the dense kernels are compiled for (register budgets 48, 36 and 64;
+// chosen by timing the ensemble step on GB300).
+#ifndef DBM_DS_BLOCKS_THIN
+#define DBM_DS_BLOCKS_THIN 5
+#endif
+#ifndef DBM_DS_BLOCKS_WEIGHTS
+#define DBM_DS_BLOCKS_WEIGHTS 7
+#endif
+#ifndef DBM_DS_BLOCKS_GATHER
+#define DBM_DS_BLOCKS_GATHER 4
+#endif
+
 __device__ __forceinline__ void defer_tile(int tb, int* fb_tiles, int* fb_count) {
   if (threadIdx.x == 0) fb_tiles[atomicAdd(fb_count, 1)] = tb;
 }
 
 template <int Q>
-__global__ void __launch_bounds__(256, 5) k_thin_refine_ds(const __grid_constant__ Args<Q, 2, PF32> A,
+__global__ void __launch_bounds__(256, DBM_DS_BLOCKS_THIN) k_thin_refine_ds(const __grid_constant__ Args<Q, 2, PF32> A,
                                                           const Tile2* __restrict__ tiles, const TileGeo G, int ntiles,
                                                           int* fb_tiles, int* fb_count) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -402,7 +414,7 @@ __global__ void __launch_bounds__(256, 5) k_thin_refine_ds(const __grid_constant
 }
 
 template <int Q>
-__global__ void __launch_bounds__(256, 6) k_weights_ds(const __grid_constant__ Args<Q, 2, PF32> A,
+__global__ void __launch_bounds__(256, DBM_DS_BLOCKS_WEIGHTS) k_weights_ds(const __grid_constant__ Args<Q, 2, PF32> A,
                                                       const Tile2* __restrict__ tiles, const TileGeo G, int ntiles,
                                                       int* fb_tiles, int* fb_count) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -415,7 +427,7 @@ __global__ void __launch_bounds__(256, 6) k_weights_ds(const __grid_constant__ A
 }
 
 template <int Q>
-__global__ void __launch_bounds__(256, 4) k_gather_ds(const __grid_constant__ Args<Q, 2, PF32> A,
+__global__ void __launch_bounds__(256, DBM_DS_BLOCKS_GATHER) k_gather_ds(const __grid_constant__ Args<Q, 2, PF32> A,
                                                      const Tile2* __restrict__ tiles, const TileGeo G, int ntiles,
                                                      int* fb_tiles, int* fb_count) {
   extern __shared__ __align__(16) unsigned char smem[];
