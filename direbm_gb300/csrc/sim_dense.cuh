@@ -1,23 +1,25 @@
 // Dense-stencil variants of the three whole-cell window kernels (2D, FP32 store).
 //
 // With whole-cell displacements (every cd_k an integer, D2Q9 with dx = cell) and R < 2 cells, the
-// thinning cell holds at most one control point, and in the ensemble and inverse-problem
-// workloads every cell of the grid holds exactly one moment at every step (the refine move stays
-// inside its cell).  A tile whose region satisfies "at most one item per cell" is staged as a
-// dense grid -- one slot per region cell, an empty cell holding an offset far outside every
-// window -- and each reference point's window for direction k becomes a fixed 4 x 4 block of
-// cells: the component-cell offsets j with e = off + (j - p) in reach of R are
-// floor(p - R - tiny) .. floor(p + R + tiny), four values per axis at R = 1.5 except within tiny
-// of p = 1/2 (five).  A point whose range is not four wide takes a loop over its exact range, so
-// no access leaves the cells the region stages (its halo covers the exact ranges for any R < 2).  Every thread then runs the same
-// unrolled stencil, without the per-row bookkeeping and the uneven loop trips of the row-segment
-// loops, and the canonical c = rn(float(j) - p) of the stencil's four columns and rows is
-// computed once per point.
+// thinning cell holds at most one control point, so in the ensemble and inverse-problem workloads
+// almost every cell holds exactly one moment: all of them at first, and after some steps all but
+// ~1 % (a refine move occasionally crosses a cell face, leaving a cell with two items and another
+// empty).  A tile's region is therefore staged as a dense grid -- one record per region cell, an
+// empty cell holding an offset far outside every window, a cell with two items naming the slot of
+// its second item in a small per-tile overflow list -- and each reference point's window for
+// direction k becomes a fixed 4 x 4 block of cells: the component-cell offsets j with
+// e = off + (j - p) in reach of R are floor(p - R - tiny) .. floor(p + R + tiny), four values per
+// axis at R = 1.5 except within tiny of p = 1/2 (five).  A point whose range is not four wide takes
+// a loop over its exact range, so no access leaves the staged region (its halo covers the exact
+// ranges for any R < 2).  Every thread runs the same unrolled stencil, without the per-row
+// bookkeeping and the uneven loop trips of the row-segment loops, and the canonical
+// c = rn(float(j) - p) of the stencil's four columns and rows is computed once per point.
 //
 // Results are bit-identical to the row-segment kernels: each sum visits the same hits in the same
-// order (window rows ascending, then columns ascending, one item per cell) with the same
-// operations.  A tile whose region (or own cells) holds a cell with two or more items is handed to
-// the row-segment code (a second, normally empty, launch over the deferred tiles).
+// order (window rows ascending, then columns ascending, then the items of a cell in order) with the
+// same operations.  A tile whose region holds a cell with three or more items, or more two-item
+// cells than the overflow list takes, is handed to the row-segment code (a second, normally empty,
+// launch over the deferred tiles).
 #pragma once
 
 #include "sim_tiled.cuh"
@@ -26,24 +28,94 @@ namespace dbm {
 
 // Offset stored for an empty cell: every displacement from it is ~1e4 cells, far outside R.
 constexpr float kEmptyOff = 1.0e4f;
+// Second items of a tile's region (cells holding two items): at most this many per tile.  A cell
+// with three or more items, or more two-item cells than this, sends the tile to the fallback.
+constexpr int kOvf = 32;
 
-// Bytes of dynamic shared memory of the dense layouts (region of rw x rh cells).
+// Dynamic shared memory of the dense layouts (region of `cells` cells): per cell a float4 record
+// {offset x, offset y, overflow slot of the cell's second item (-1: none), rho or 0} plus per
+// direction data, the same for the kOvf overflow items, and the overflow counter.
 __host__ __device__ inline size_t dense_off(size_t n) { return (n + 15) & ~(size_t)15; }
-__host__ __device__ inline size_t ds_bytes_refine(int Q, int cells) {
-  return dense_off((size_t)cells * 8) + dense_off((size_t)Q * cells * 4);
+// Byte offsets of the cell records, their data, the overflow records and their data; returns the
+// total including the counter.
+__host__ __device__ inline size_t ds_layout(int cells, size_t per_cell, size_t* offs) {
+  const int n[2] = {cells, kOvf};
+  size_t o = 0;
+  for (int b = 0; b < 2; ++b) {
+    offs[2 * b] = o;
+    o += dense_off((size_t)n[b] * 16);
+    offs[2 * b + 1] = o;
+    o += dense_off((size_t)n[b] * per_cell);
+  }
+  return o + 16;  // + the overflow counter
 }
-__host__ __device__ inline size_t ds_bytes_weights(int cells) { return dense_off((size_t)cells * 8); }
-__host__ __device__ inline size_t ds_bytes_gather(int Q, int cells) {
-  return dense_off((size_t)cells * 8) + dense_off((size_t)cells * 4) + dense_off((size_t)Q * cells * 8);
+__host__ __device__ inline size_t ds_bytes(int cells, size_t per_cell) {
+  size_t offs[4];
+  return ds_layout(cells, per_cell, offs);
+}
+// per-direction bytes per item: thin + refine exp(f*) (4 Q), weights none, gather (1/sw, f*) (8 Q)
+__host__ __device__ inline size_t ds_bytes_refine(int Q, int cells) { return ds_bytes(cells, (size_t)4 * Q); }
+__host__ __device__ inline size_t ds_bytes_weights(int cells) { return ds_bytes(cells, 0); }
+__host__ __device__ inline size_t ds_bytes_gather(int Q, int cells) { return ds_bytes(cells, (size_t)8 * Q); }
+
+struct DenseSmem {
+  float4* rec;          // [cells]
+  unsigned char* dat;   // per-direction data of the cells' first items
+  float4* orec;         // [kOvf]
+  unsigned char* odat;  // per-direction data of the overflow items
+  int* novf;            // overflow counter
+};
+__device__ __forceinline__ DenseSmem dense_smem(unsigned char* smem, int cells, size_t per_cell) {
+  size_t offs[4];
+  const size_t total = ds_layout(cells, per_cell, offs);
+  return DenseSmem{reinterpret_cast<float4*>(smem + offs[0]), smem + offs[1], reinterpret_cast<float4*>(smem + offs[2]),
+                   smem + offs[3], reinterpret_cast<int*>(smem + total - 16)};
 }
 
-// The single item of global cell g in a state's sorted ranges: its index, -1 if the cell is
-// empty; sets *many if the cell holds two or more items.
-__device__ __forceinline__ int single_item(const uint32_t* __restrict__ start, uint32_t g, int* many) {
-  const uint32_t b = start[g], e = start[g + 1];
-  if (e - b == 1u) return (int)b;
-  if (e != b) *many = 1;
-  return -1;
+// Item range of global cell g: at most two items, else *many is set.
+__device__ __forceinline__ void cell_items(const uint32_t* __restrict__ start, uint32_t g, int* b, int* e, int* many) {
+  const uint32_t b0 = start[g], e0 = start[g + 1];
+  if (e0 - b0 > 2u) {
+    *many = 1;
+    *b = *e = (int)b0;
+  } else {
+    *b = (int)b0;
+    *e = (int)e0;
+  }
+}
+
+// Dense staging of region cells [xr0, xr0 + rw) x [yr0, yr0 + rh) of a state's sorted ranges
+// `start`: put(record, per-direction data, stride, slot, item, nxt) fills the record of one item
+// (its per-direction data goes to data[k * stride + slot]); the record of an empty cell gets the
+// empty offset.  A cell's second item goes to the next overflow slot.  Returns false, the same in
+// every thread, when the tile must be deferred (`many` from the caller, a cell with three or more
+// items, or a full overflow list).
+template <class Put>
+__device__ __forceinline__ bool stage_dense(const InstK& I, int xr0, int yr0, int rw, int rh,
+                                            const uint32_t* __restrict__ start, const DenseSmem& S, int many,
+                                            Put&& put) {
+  const int cells = rw * rh;
+  if (threadIdx.x == 0) *S.novf = 0;
+  __syncthreads();
+  for (int ci = threadIdx.x; ci < cells; ci += blockDim.x) {
+    const int ry = ci / rw, rx = ci - ry * rw;
+    uint32_t g;
+    int b = 0, e = 0;
+    if (region_cell(I, xr0 + rx, yr0 + ry, &g)) cell_items(start, g, &b, &e, &many);
+    float nxt = -1.f;
+    if (e - b == 2) {
+      const int q = atomicAdd(S.novf, 1);
+      if (q < kOvf) {
+        put(S.orec + q, S.odat, kOvf, q, b + 1, -1.f);
+        nxt = (float)q;
+      } else {
+        many = 1;
+      }
+    }
+    if (e > b) put(S.rec + ci, S.dat, cells, ci, b, nxt);
+    else S.rec[ci] = make_float4(kEmptyOff, kEmptyOff, -1.f, 0.f);
+  }
+  return !__syncthreads_or(many);
 }
 
 // Stencil origin and width along one axis for reference offset p: j in [lo, lo + n).
@@ -53,29 +125,25 @@ __device__ __forceinline__ void stencil_axis(float p, float R, float tiny, int* 
 }
 
 // ---- thinning + refine --------------------------------------------------------------------------
+// Per-direction data: exp(f*_k) of each item, direction-major ([k][cells] and [k][kOvf]).
 
 template <int Q>
 __device__ __forceinline__ bool thin_refine_ds_tile(const Args<Q, 2, PF32>& A, const Tile2& T, const InstK& I,
                                                     const TileGeo& G, unsigned char* smem) {
   const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
   const int cells = rw * rh;
-  float2* s_off = reinterpret_cast<float2*>(smem);
-  float* s_w = reinterpret_cast<float*>(smem + dense_off((size_t)cells * 8));  // exp(f*) [Q][cells]
-  int many = 0;
-  const int xr0 = T.x0 + G.mom.xl, yr0 = T.y0 + G.mom.yl;
-  for (int ci = threadIdx.x; ci < cells; ci += blockDim.x) {
-    const int ry = ci / rw, rx = ci - ry * rw;
-    uint32_t g;
-    const int m = region_cell(I, xr0 + rx, yr0 + ry, &g) ? single_item(A.a.start, g, &many) : -1;
-    if (m >= 0) {
-      s_off[ci] = make_float2(A.a.off[m], A.a.off[A.mcap + m]);
+  const DenseSmem S = dense_smem(smem, cells, (size_t)4 * Q);
+  float* s_w = reinterpret_cast<float*>(S.dat);
+  float* s_ow = reinterpret_cast<float*>(S.odat);
+  const bool dense = stage_dense(I, T.x0 + G.mom.xl, T.y0 + G.mom.yl, rw, rh, A.a.start, S, 0,
+                                 [&](float4* r, unsigned char* dat, int stride, int slot, int m, float nxt) {
+                                   *r = make_float4(A.a.off[m], A.a.off[A.mcap + m], nxt, 0.f);
+                                   float* w = reinterpret_cast<float*>(dat);
 #pragma unroll
-      for (int k = 0; k < Q; ++k) s_w[k * cells + ci] = exp(fstar_at<Q, 2, PF32>(A, (uint32_t)m, k));
-    } else {
-      s_off[ci] = make_float2(kEmptyOff, kEmptyOff);
-    }
-  }
-  if (__syncthreads_or(many)) return false;
+                                   for (int k = 0; k < Q; ++k)
+                                     w[k * stride + slot] = exp(fstar_at<Q, 2, PF32>(A, (uint32_t)m, k));
+                                 });
+  if (!dense) return false;
 
   const int lx = threadIdx.x % G.tx, ly = threadIdx.x / G.tx;
   const int Fx = T.x0 + lx, Fy = T.y0 + ly;
@@ -99,14 +167,18 @@ __device__ __forceinline__ bool thin_refine_ds_tile(const Args<Q, 2, PF32>& A, c
 #pragma unroll 1
       for (int ox = 0; ox < nx; ++ox) {
         const int sox = lox + ox;
-        const float2 o = s_off[(by + soy) * rw + (bx + sox)];
-        const float tx = rn_add(o.x, cdx), ty = rn_add(o.y, cdy);
         const float sxf = (float)sox;
-        if (tx >= -sxf && tx < 1.f - sxf && ty >= fy0 && ty < fy0 + 1.f) {
-          ++cnt;
-          csum[0].add(rn_add(sxf, tx));
-          csum[1].add(rn_add(sy, ty));
-        }
+        auto land = [&](float4 o) {
+          const float tx = rn_add(o.x, cdx), ty = rn_add(o.y, cdy);
+          if (tx >= -sxf && tx < 1.f - sxf && ty >= fy0 && ty < fy0 + 1.f) {
+            ++cnt;
+            csum[0].add(rn_add(sxf, tx));
+            csum[1].add(rn_add(sy, ty));
+          }
+        };
+        const float4 o = S.rec[(by + soy) * rw + (bx + sox)];
+        land(o);
+        if (o.z >= 0.f) land(S.orec[(int)o.z]);
       }
     }
   }
@@ -139,16 +211,24 @@ __device__ __forceinline__ bool thin_refine_ds_tile(const Args<Q, 2, PF32>& A, c
     const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
     const int c0 = (by + jly - cdy) * rw + (bx + jlx - cdx);
     const float* wk = s_w + k * cells;
+    const float* owk = s_ow + k * kOvf;
     bool hit = false;
-    auto visit = [&](int ci, float ex0, float ey0) {
-      const float2 o = s_off[ci];
-      const float2 e = __fadd2_rn(o, make_float2(ex0, ey0));
+    auto one = [&](float4 o, const float* wp, float ex0, float ey0) {
+      const float2 e = __fadd2_rn(make_float2(o.x, o.y), make_float2(ex0, ey0));
       const float2 e2 = __fmul2_rn(e, e);
       if (rn_add(e2.x, e2.y) <= A.R2) {
         hit = true;
-        const float wt = wk[ci];
+        const float wt = *wp;
         swf = __fadd_rn(swf, wt);
         sx = __ffma2_rn(make_float2(wt, wt), e, sx);
+      }
+    };
+    auto visit = [&](int ci, float ex0, float ey0) {
+      const float4 o = S.rec[ci];
+      one(o, wk + ci, ex0, ey0);
+      if (o.z >= 0.f) {
+        const int q = (int)o.z;
+        one(S.orec[q], owk + q, ex0, ey0);
       }
     };
     if (!wide) {
@@ -218,160 +298,166 @@ __device__ __forceinline__ bool weights_ds_tile(const Args<Q, 2, PF32>& A, const
                                                 const TileGeo& G, unsigned char* smem) {
   const int rw = G.tx + G.cp.xh - G.cp.xl, rh = G.ty + G.cp.yh - G.cp.yl;
   const int cells = rw * rh;
-  float2* s_cp = reinterpret_cast<float2*>(smem);  // control-point offsets
-  int many = 0;
-  const int xr0 = T.x0 + G.cp.xl, yr0 = T.y0 + G.cp.yl;
-  for (int ci = threadIdx.x; ci < cells; ci += blockDim.x) {
-    const int ry = ci / rw, rx = ci - ry * rw;
-    uint32_t g;
-    const int c = region_cell(I, xr0 + rx, yr0 + ry, &g) ? single_item(A.b.start, g, &many) : -1;
-    s_cp[ci] = c >= 0 ? make_float2(A.b.off[c], A.b.off[A.ccap + c]) : make_float2(kEmptyOff, kEmptyOff);
-  }
-  // the tile's own moment (one per cell at most)
+  const DenseSmem S = dense_smem(smem, cells, 0);
+  // the tile's own moments (at most two per cell)
   const int lx = threadIdx.x % G.tx, ly = threadIdx.x / G.tx;
   const int Sx = T.x0 + lx, Sy = T.y0 + ly;
-  int m = -1;
+  int m0 = 0, m1 = 0, many = 0;
   if (ly < G.ty && Sx < I.dims[0] && Sy < I.dims[1])
-    m = single_item(A.a.start, I.base + (uint32_t)Sx + (uint32_t)I.dims[0] * (uint32_t)Sy, &many);
-  if (__syncthreads_or(many)) return false;
-  if (m < 0) return true;
+    cell_items(A.a.start, I.base + (uint32_t)Sx + (uint32_t)I.dims[0] * (uint32_t)Sy, &m0, &m1, &many);
+  const bool dense = stage_dense(I, T.x0 + G.cp.xl, T.y0 + G.cp.yl, rw, rh, A.b.start, S, many,
+                                 [&](float4* r, unsigned char*, int, int, int c, float nxt) {
+                                   *r = make_float4(A.b.off[c], A.b.off[A.ccap + c], nxt, 0.f);
+                                 });
+  if (!dense) return false;
 
-  const float2 o = make_float2(A.a.off[m], A.a.off[A.mcap + m]);
-  const int bx = lx - G.cp.xl, by = ly - G.cp.yl;  // region coordinates of the moment's cell
-  // control-point offsets u (relative to the component's cell) with a possible hit
-  int ulx, nxs, uly, nys;
-  stencil_axis(o.x, A.R, A.tiny, &ulx, &nxs);
-  stencil_axis(o.y, A.R, A.tiny, &uly, &nys);
-  const bool wide = nxs != 4 || nys != 4;  // exact-range loops otherwise
-  float bxv[4], byv[4];  // base = float(cd - dG) = float(-u), exact
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    bxv[a] = (float)(-(ulx + a));
-    byv[a] = (float)(-(uly + a));
-  }
+  const int bx = lx - G.cp.xl, by = ly - G.cp.yl;  // region coordinates of the moments' cell
 #pragma unroll 1
-  for (int k = 0; k < Q; ++k) {
-    const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
-    const int c0 = (by + uly + cdy) * rw + (bx + ulx + cdx);
-    CSum sws;
-    auto visit = [&](int ci, float basex, float basey) {
-      const float2 pc = s_cp[ci];
-      const float2 q = __fadd2_rn(make_float2(basex, basey), make_float2(-pc.x, -pc.y));
-      const float2 e = __fadd2_rn(o, q);
-      const float2 e2 = __fmul2_rn(e, e);
-      const float d2 = rn_add(e2.x, e2.y);
-      if (d2 <= A.R2) sws.add(A.R - rn_sqrt(d2));
-    };
-    if (!wide) {
+  for (int m = m0; m < m1; ++m) {
+    const float2 o = make_float2(A.a.off[m], A.a.off[A.mcap + m]);
+    // control-point offsets u (relative to the component's cell) with a possible hit
+    int ulx, nxs, uly, nys;
+    stencil_axis(o.x, A.R, A.tiny, &ulx, &nxs);
+    stencil_axis(o.y, A.R, A.tiny, &uly, &nys);
+    const bool wide = nxs != 4 || nys != 4;  // exact-range loops otherwise
+    float bxv[4], byv[4];  // base = float(cd - dG) = float(-u), exact
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
-#pragma unroll
-        for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, bxv[a], byv[b]);
-    } else {
-#pragma unroll 1
-      for (int b = 0; b < nys; ++b)
-#pragma unroll 1
-        for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, (float)(-(ulx + a)), (float)(-(uly + b)));
+    for (int a = 0; a < 4; ++a) {
+      bxv[a] = (float)(-(ulx + a));
+      byv[a] = (float)(-(uly + a));
     }
-    const float sw = sws.value();
-    A.sw[(int64_t)k * A.mcap + m] = sw > 0.f ? 1.f / sw : 0.f;
+#pragma unroll 1
+    for (int k = 0; k < Q; ++k) {
+      const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
+      const int c0 = (by + uly + cdy) * rw + (bx + ulx + cdx);
+      CSum sws;
+      auto one = [&](float4 pc, float basex, float basey) {
+        const float2 q = __fadd2_rn(make_float2(basex, basey), make_float2(-pc.x, -pc.y));
+        const float2 e = __fadd2_rn(o, q);
+        const float2 e2 = __fmul2_rn(e, e);
+        const float d2 = rn_add(e2.x, e2.y);
+        if (d2 <= A.R2) sws.add(A.R - rn_sqrt(d2));
+      };
+      auto visit = [&](int ci, float basex, float basey) {
+        const float4 pc = S.rec[ci];
+        one(pc, basex, basey);
+        if (pc.z >= 0.f) one(S.orec[(int)pc.z], basex, basey);
+      };
+      if (!wide) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+          for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, bxv[a], byv[b]);
+      } else {
+#pragma unroll 1
+        for (int b = 0; b < nys; ++b)
+#pragma unroll 1
+          for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, (float)(-(ulx + a)), (float)(-(uly + b)));
+      }
+      const float sw = sws.value();
+      A.sw[(int64_t)k * A.mcap + m] = sw > 0.f ? 1.f / sw : 0.f;
+    }
   }
   return true;
 }
 
 // ---- gather: per control point and direction ------------------------------------------------------
+// Per-direction data: (1/sw, f*_k) of each item, direction-major.
 
 template <int Q>
 __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const Tile2& T, const InstK& I,
                                                const TileGeo& G, unsigned char* smem) {
   const int rw = G.tx + G.mom.xh - G.mom.xl, rh = G.ty + G.mom.yh - G.mom.yl;
   const int cells = rw * rh;
-  float2* s_off = reinterpret_cast<float2*>(smem);
-  float* s_rho = reinterpret_cast<float*>(smem + dense_off((size_t)cells * 8));
-  float2* s_kv = reinterpret_cast<float2*>(smem + dense_off((size_t)cells * 8) + dense_off((size_t)cells * 4));
-  int many = 0;
-  const int xr0 = T.x0 + G.mom.xl, yr0 = T.y0 + G.mom.yl;
-  for (int ci = threadIdx.x; ci < cells; ci += blockDim.x) {
-    const int ry = ci / rw, rx = ci - ry * rw;
-    uint32_t g;
-    const int m = region_cell(I, xr0 + rx, yr0 + ry, &g) ? single_item(A.a.start, g, &many) : -1;
-    if (m >= 0) {
-      s_off[ci] = make_float2(A.a.off[m], A.a.off[A.mcap + m]);
-      s_rho[ci] = A.a.rho[m];
-#pragma unroll
-      for (int k = 0; k < Q; ++k)
-        s_kv[k * cells + ci] = make_float2(A.sw[(int64_t)k * A.mcap + m], A.a.dev[(int64_t)k * A.mcap + m]);
-    } else {
-      s_off[ci] = make_float2(kEmptyOff, kEmptyOff);
-    }
-  }
-  // the tile's own control point (one per cell at most)
+  const DenseSmem S = dense_smem(smem, cells, (size_t)8 * Q);
+  const float2* s_kv = reinterpret_cast<const float2*>(S.dat);
+  const float2* s_okv = reinterpret_cast<const float2*>(S.odat);
+  // the tile's own control points (at most two per cell)
   const int lx = threadIdx.x % G.tx, ly = threadIdx.x / G.tx;
   const int Fx = T.x0 + lx, Fy = T.y0 + ly;
-  int j = -1;
+  int j0 = 0, j1 = 0, many = 0;
   if (ly < G.ty && Fx < I.dims[0] && Fy < I.dims[1])
-    j = single_item(A.b.start, I.base + (uint32_t)Fx + (uint32_t)I.dims[0] * (uint32_t)Fy, &many);
-  if (__syncthreads_or(many)) return false;
-  if (j < 0) return true;
+    cell_items(A.b.start, I.base + (uint32_t)Fx + (uint32_t)I.dims[0] * (uint32_t)Fy, &j0, &j1, &many);
+  const bool dense = stage_dense(I, T.x0 + G.mom.xl, T.y0 + G.mom.yl, rw, rh, A.a.start, S, many,
+                                 [&](float4* r, unsigned char* dat, int stride, int slot, int m, float nxt) {
+                                   *r = make_float4(A.a.off[m], A.a.off[A.mcap + m], nxt, A.a.rho[m]);
+                                   float2* kv = reinterpret_cast<float2*>(dat);
+#pragma unroll
+                                   for (int k = 0; k < Q; ++k)
+                                     kv[k * stride + slot] = make_float2(A.sw[(int64_t)k * A.mcap + m],
+                                                                         A.a.dev[(int64_t)k * A.mcap + m]);
+                                 });
+  if (!dense) return false;
 
-  const float2 pp = make_float2(A.b.off[j], A.b.off[A.ccap + j]);
-  const int bx = lx - G.mom.xl, by = ly - G.mom.yl;  // region coordinates of the CP's cell
-  int jlx, nxs, jly, nys;
-  stencil_axis(pp.x, A.R, A.tiny, &jlx, &nxs);
-  stencil_axis(pp.y, A.R, A.tiny, &jly, &nys);
-  const bool wide = nxs != 4 || nys != 4;  // exact-range loops otherwise
-  float cx[4], cy[4];
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    cx[a] = rn_sub((float)(jlx + a), pp.x);
-    cy[a] = rn_sub((float)(jly + a), pp.y);
-  }
-  uint32_t empty = 0;
+  const int bx = lx - G.mom.xl, by = ly - G.mom.yl;  // region coordinates of the control points' cell
 #pragma unroll 1
-  for (int k = 0; k < Q; ++k) {
-    const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
-    const int c0 = (by + jly - cdy) * rw + (bx + jlx - cdx);
-    const float2* kvk = s_kv + k * cells;
-    CSum sa;
-    float sb = 0.f;  // deviation part: plain FMA accumulation, as in the row-segment gathers
-    auto visit = [&](int ci, float ex0, float ey0) {
-      const float2 o = s_off[ci];
-      const float2 e = __fadd2_rn(o, make_float2(ex0, ey0));
-      const float2 e2 = __fmul2_rn(e, e);
-      const float d2 = rn_add(e2.x, e2.y);
-      if (d2 <= A.R2) {
-        // a dropped component has 1/sw = 0: its weight is +0 and leaves every sum unchanged
-        const float2 kv = kvk[ci];
-        const float rho = s_rho[ci];
-        const float wgt = (A.R - rn_sqrt(d2)) * kv.x;
-        const float p = __fmul_rn(wgt, rho);
-        const float2 r = __ffma2_rn(make_float2(wgt, wgt), make_float2(rho, kv.y), make_float2(-p, sb));
-        sa.add(p);
-        sa.lo = __fadd_rn(sa.lo, r.x);
-        sb = r.y;
-      }
-    };
-    if (!wide) {
+  for (int j = j0; j < j1; ++j) {
+    const float2 pp = make_float2(A.b.off[j], A.b.off[A.ccap + j]);
+    int jlx, nxs, jly, nys;
+    stencil_axis(pp.x, A.R, A.tiny, &jlx, &nxs);
+    stencil_axis(pp.y, A.R, A.tiny, &jly, &nys);
+    const bool wide = nxs != 4 || nys != 4;  // exact-range loops otherwise
+    float cx[4], cy[4];
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
-#pragma unroll
-        for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, cx[a], cy[b]);
-    } else {
-#pragma unroll 1
-      for (int b = 0; b < nys; ++b) {
-        const float cyb = rn_sub((float)(jly + b), pp.y);
-#pragma unroll 1
-        for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, rn_sub((float)(jlx + a), pp.x), cyb);
-      }
+    for (int a = 0; a < 4; ++a) {
+      cx[a] = rn_sub((float)(jlx + a), pp.x);
+      cy[a] = rn_sub((float)(jly + a), pp.y);
     }
-    const DF Ad = df_norm(sa.hi, sa.lo);
-    const DF Fv = df_add(df_mul(DF{A.L.wf[k], A.L.wlo[k]}, Ad), DF{sb, 0.f});
-    A.cpfhi[(int64_t)k * A.ccap + j] = Fv.hi;
-    A.cpflo[(int64_t)k * A.ccap + j] = Fv.lo;
-    if (Fv.hi < A.eps) empty |= 1u << k;
+    uint32_t empty = 0;
+#pragma unroll 1
+    for (int k = 0; k < Q; ++k) {
+      const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
+      const int c0 = (by + jly - cdy) * rw + (bx + jlx - cdx);
+      const float2* kvk = s_kv + k * cells;
+      const float2* okvk = s_okv + k * kOvf;
+      CSum sa;
+      float sb = 0.f;  // deviation part: plain FMA accumulation, as in the row-segment gathers
+      auto one = [&](float4 o, const float2* kvp, float ex0, float ey0) {
+        const float2 e = __fadd2_rn(make_float2(o.x, o.y), make_float2(ex0, ey0));
+        const float2 e2 = __fmul2_rn(e, e);
+        const float d2 = rn_add(e2.x, e2.y);
+        if (d2 <= A.R2) {
+          // a dropped component has 1/sw = 0: its weight is +0 and leaves every sum unchanged
+          const float2 kv = *kvp;
+          const float rho = o.w;
+          const float wgt = (A.R - rn_sqrt(d2)) * kv.x;
+          const float p = __fmul_rn(wgt, rho);
+          const float2 r = __ffma2_rn(make_float2(wgt, wgt), make_float2(rho, kv.y), make_float2(-p, sb));
+          sa.add(p);
+          sa.lo = __fadd_rn(sa.lo, r.x);
+          sb = r.y;
+        }
+      };
+      auto visit = [&](int ci, float ex0, float ey0) {
+        const float4 o = S.rec[ci];
+        one(o, kvk + ci, ex0, ey0);
+        if (o.z >= 0.f) {
+          const int q = (int)o.z;
+          one(S.orec[q], okvk + q, ex0, ey0);
+        }
+      };
+      if (!wide) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+          for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, cx[a], cy[b]);
+      } else {
+#pragma unroll 1
+        for (int b = 0; b < nys; ++b) {
+          const float cyb = rn_sub((float)(jly + b), pp.y);
+#pragma unroll 1
+          for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, rn_sub((float)(jlx + a), pp.x), cyb);
+        }
+      }
+      const DF Ad = df_norm(sa.hi, sa.lo);
+      const DF Fv = df_add(df_mul(DF{A.L.wf[k], A.L.wlo[k]}, Ad), DF{sb, 0.f});
+      A.cpfhi[(int64_t)k * A.ccap + j] = Fv.hi;
+      A.cpflo[(int64_t)k * A.ccap + j] = Fv.lo;
+      if (Fv.hi < A.eps) empty |= 1u << k;
+    }
+    // this thread is the only writer of its control point's mask (cleared before the launch)
+    if (empty) A.emask[j] = empty;
   }
-  // this thread is the only writer of its control point's mask (cleared before the launch)
-  if (empty) A.emask[j] = empty;
   return true;
 }
 
@@ -384,13 +470,13 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
 // own.  The order of the fallback list is arbitrary, which changes no result: tiles write
 // disjoint outputs.
 
-// Resident blocks per SM the dense kernels are compiled for (register budgets 48, 36 and 64;
+// Resident blocks per SM the dense kernels are compiled for (register budgets 48, 40 and 64;
 // chosen by timing the ensemble step on GB300).
 #ifndef DBM_DS_BLOCKS_THIN
 #define DBM_DS_BLOCKS_THIN 5
 #endif
 #ifndef DBM_DS_BLOCKS_WEIGHTS
-#define DBM_DS_BLOCKS_WEIGHTS 7
+#define DBM_DS_BLOCKS_WEIGHTS 6
 #endif
 #ifndef DBM_DS_BLOCKS_GATHER
 #define DBM_DS_BLOCKS_GATHER 4

@@ -433,14 +433,18 @@ def _d2q9_field(xx, n0, n1, amp=0.03):
     return equilibrium(np.ones(len(xx)), u, D2Q9)
 
 
-@pytest.mark.parametrize("name", ["batch_uneven", "mixed_density", "cell_centres", "bounded_pulse_d2q9"])
+@pytest.mark.parametrize("name", ["batch_uneven", "mixed_density", "cell_centres", "bounded_pulse_d2q9",
+                                  "pairs_sparse", "pairs_frequent", "long_run"])
 def test_dense_stencil_bitwise_equal(name):
-    """The dense-stencil kernels (one item per cell, fixed 4 x 4 windows) give the same bits as the
-    row-segment shifted windows.  Cases: a batch of jittered grids (dense everywhere); a box whose
-    right half holds uniformly random points (cells with two or more moments send their tiles to the
-    row-segment fallback in the first step, and empty cells take the empty-slot path); points at the
-    exact cell centres (every reference offset is 1/2, where the stencil is five cells wide); and a
-    bounded box around a pulse (empty cells outside the material, offsets exactly 0)."""
+    """The dense-stencil kernels (fixed 4 x 4 windows over a dense staging of each tile) give the same
+    bits as the row-segment shifted windows.  Cases: a batch of jittered grids (one item per cell);
+    a box whose right half holds uniformly random points (cells with three or more moments send their
+    tiles to the row-segment fallback in the first step, empty cells take the empty-slot path);
+    points at the exact cell centres (every reference offset is 1/2, where the stencil is five cells
+    wide); a bounded box around a pulse (empty cells outside the material, offsets exactly 0); a grid
+    with an extra point in 2 % of the cells (two-item cells through the overflow list) and in 30 %
+    of them (more two-item cells than the list takes: fallback); and a long run, over which refine
+    moves leave some cells with two moments."""
     from direbm_gb300.sim import Instance, Simulation
 
     lattice, dx, r, cell = "D2Q9", 1.0, 1.5, 1.0
@@ -470,17 +474,30 @@ def test_dense_stencil_bitwise_equal(name):
         insts = [dict(dims=(n0, n1), periodic=True, tau=0.8)]
         x = np.stack(np.meshgrid(np.arange(n0) + 0.5, np.arange(n1) + 0.5), -1).reshape(-1, 2)
         f = _d2q9_field(x, n0, n1)
+    elif name in ("pairs_sparse", "pairs_frequent", "long_run"):
+        n0, n1 = 72, 56
+        insts = [dict(dims=(n0, n1), periodic=True, tau=0.75)]
+        x = np.stack(np.meshgrid(np.arange(n0) + 0.5, np.arange(n1) + 0.5), -1).reshape(-1, 2)
+        x = x + rng.uniform(-0.25, 0.25, x.shape)
+        if name != "long_run":
+            frac = 0.02 if name == "pairs_sparse" else 0.3
+            pick = rng.random(len(x)) < frac
+            extra = np.floor(x[pick]) + rng.uniform(0.05, 0.95, (int(pick.sum()), 2))
+            x = np.concatenate([x, extra])
+        x = np.mod(x, [n0, n1])
+        f = _d2q9_field(x, n0, n1, amp=0.05)
     else:
         x, f = rest_pulse(6, "D2Q9")
         dims, origin = bounded_box(x, 1.0, 8.0)
         insts = [dict(dims=dims, origin=origin, periodic=False, tau=0.6)]
+    steps = 40 if name == "long_run" else 4
     outs = []
     for on in (True, False):
         sim = Simulation([Instance(**i) for i in insts], lattice=lattice, precision="fp32dev", dx=dx, r_res=r,
-                         cell=cell)
+                         cell=cell, moment_capacity=len(x))
         sim.set_dense_stencil(on)
         sim.set_state(ib, x, f)
-        sim.step(4)
+        sim.step(steps)
         outs.append(sim.state_numpy())
         assert sim.status() == 0
     for a, b in zip(outs[0], outs[1]):
