@@ -11,13 +11,16 @@ so L2 is not flushed between steps.
 Keys beyond the base contract:
   roofline      dominant kernel's algorithmic bytes / its CUDA-event duration vs measured HBM peak
   step_roofline the whole step against the per-point-step byte model of the method
-  fp64          the same workload in the FP64 store (fewer steps: GB300 FP64 is slow)
-  accuracy      velocity L2 error vs the FP64 oracle on a 4096-point instance
+  fp64          the same workload in the FP64 store (5 timed steps: GB300 FP64 is slow)
+  accuracy      velocity L2 error vs the FP64 oracle on a 4096-point instance, and against the
+                FP64 GPU step after 1/10/50/200 steps beside FP64 from the FP32-rounded start
+  accuracy_ensemble  FP32DEV vs FP64 on the whole ensemble after 10 steps (same comparison)
   lbm           hexagonal D2Q7 shear wave 1024x1024 (FP32DEV and FP64), node-steps/s
   adjoint       inverse problem on 64k points, 100 steps, checkpoint every 10: adjoint steps/s, its
                 cost relative to the forward step, FP32DEV gradient error vs FP64
   sphere        3D flow past a bounce-back sphere (D3Q19, ~2 M points, inflow), FP32DEV and FP64
-  cpu_baseline  the CPU oracle (numpy restatement of the reference step) on the host cores
+  cpu_baseline  the CPU oracle (numpy restatement of the reference step) on the host cores, and
+                the reference's own CPU simulator (one process and one per core)
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -65,10 +68,10 @@ KERNEL_BYTES = {
 }
 
 # DRAM bytes per input moment measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum) for
-# one launch of k_gather_ts (the shifted-window gather this workload runs) on a 4.18 M-moment case
-# of this workload (its first 64 members, 16x16 tiles): 436.6 MB read + 281.3 MB written.  Traffic
+# one launch of k_gather_ds (the dense-stencil gather this workload runs) on a 4.18 M-moment case
+# of this workload (its first 64 members, 16x16 tiles): 419.6 MB read + 267.4 MB written.  Traffic
 # grows with the moments, so a full launch's traffic is this times M.
-KERNEL_TRAFFIC_PER_MOMENT = {"gather": 171.6}
+KERNEL_TRAFFIC_PER_MOMENT = {"gather": 164.2}
 
 # Per point-step byte model of the method (components materialised as 12-byte sort records):
 # B = M(Qs+b_p) + Nc k_b + 2 Nc k_b + 3(Nc k_b + M(Qs+b_p)) + 3 P b_p + P(Qs+b_p), with P ~ M,
@@ -230,8 +233,22 @@ def velocity_l2(f, lat):
     return (f @ lat.C) / rho[:, None]
 
 
-def accuracy_leg(steps=10):
-    """FP32DEV and FP64 GPU vs the FP64 oracle on one 64x64 instance (the smallest ensemble size)."""
+def fp32_rounded(x, f, lat, rho_rest=1.0):
+    """The state as the FP32-deviation store holds it: positions as integer cell + FP32 offset, f as
+    the rest equilibrium plus an FP32 deviation.  An FP64 run from this state differs from the FP64
+    run from (x, f) only by the input rounding of the FP32 store."""
+    c = np.floor(x)
+    xr = c + (x - c).astype(np.float32).astype(np.float64)
+    rest = rho_rest * lat.W[None, :]
+    fr = rest + (f - rest).astype(np.float32).astype(np.float64)
+    return xr, fr
+
+
+def accuracy_leg(steps=10, table=(1, 10, 50, 200)):
+    """FP32DEV and FP64 GPU vs the FP64 oracle on one 64x64 instance (the smallest ensemble size)
+    after `steps` steps; then, after each step count of `table`, FP32DEV against the FP64 GPU step
+    (itself within 1e-12 of the oracle) beside the FP64 step started from the FP32-rounded state
+    against the same FP64 step (the method's own response to the FP32 store's input rounding)."""
     from oracle import grid_step
     from oracle.lattices import D2Q9 as OD2Q9
 
@@ -261,10 +278,121 @@ def accuracy_leg(steps=10):
         out[prec] = {"velocity_l2_rel": err, "points_match": bool(same), "moments": int(len(xg)),
                      "max_pos_err": float(np.abs(xg - xo).max()) if len(xg) == len(xo) else None}
         sim.close()
+    # error against step count
+    xr, fr = fp32_rounded(x, f, D2Q9)
+    starts = {"fp32dev": (x, f), "fp64": (x, f), "fp64_rounded_start": (xr, fr)}
+    sims = {k: make_sim([n], [0.8], "fp32dev" if k == "fp32dev" else "fp64", 0) for k in starts}
+    for k, sm in sims.items():
+        sm.set_state(None, *starts[k])
+    rows, done = [], 0
+    for t in table:
+        for sm in sims.values():
+            sm.step(t - done)
+        done = t
+        st_ = {k: sm.state_numpy() for k, sm in sims.items()}
+        row = {"steps": t}
+        for k in ("fp32dev", "fp64_rounded_start"):
+            row[k + "_vs_fp64"] = compare_states(st_[k], st_["fp64"], [n], D2Q9)
+        rows.append(row)
+    for sm in sims.values():
+        sm.close()
+    out["vs_fp64_gpu_by_steps"] = rows
     return out
 
 
-def lbm_leg(steps=100, warmup=5):
+def _cell_keys(inst, xp, sides):
+    """Global cell index of each point (instance-major, row-major inside a square instance)."""
+    side = np.asarray(sides, dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(side * side)])
+    c = np.floor(xp).astype(np.int64)
+    return offs[inst] + c[:, 0] + side[inst] * c[:, 1]
+
+
+def _binned_velocity(inst, xp, fp, sides, lat, b):
+    """Mass-weighted velocity of each b x b block of cells: sum f c / sum f over its points."""
+    side = np.asarray(sides, dtype=np.int64)
+    nb = -(-side // b)
+    offs = np.concatenate([[0], np.cumsum(nb * nb)])
+    c = np.floor(xp).astype(np.int64) // b
+    key = offs[inst] + c[:, 0] + nb[inst] * c[:, 1]
+    nbin = int(offs[-1])
+    mass = np.bincount(key, weights=fp.sum(1), minlength=nbin)
+    mom = fp @ lat.C
+    u = np.stack([np.bincount(key, weights=mom[:, a], minlength=nbin) for a in range(mom.shape[1])], 1)
+    return u / np.maximum(mass, 1e-300)[:, None]
+
+
+def compare_states(a, b, sides, lat, bins=4):
+    """State a against state b (each (inst, pos, f) of one ensemble).
+
+    Per point: velocity L2 over the cells where each holds exactly one point (the point sets can
+    differ where a near-tie decision went the other way), and over the subset whose points also
+    agree in position to 1e-5 cells.  Per field: the L2 of the mass-weighted velocity of each
+    bins x bins block of cells (the macroscopic field, which does not depend on which of two
+    nearly equal decisions a point took)."""
+    (ia_, xa, fa), (ib_, xb, fb) = a, b
+    ia_ = np.zeros(len(xa), np.int64) if ia_ is None else np.asarray(ia_, np.int64)
+    ib_ = np.zeros(len(xb), np.int64) if ib_ is None else np.asarray(ib_, np.int64)
+    ka, kb = _cell_keys(ia_, xa, sides), _cell_keys(ib_, xb, sides)
+    ua, ca = np.unique(ka, return_counts=True)
+    ub, cb = np.unique(kb, return_counts=True)
+    common = np.intersect1d(ua[ca == 1], ub[cb == 1])
+    oa, ob = np.argsort(ka, kind="stable"), np.argsort(kb, kind="stable")
+    sa = oa[np.searchsorted(ka[oa], common)]
+    sb = ob[np.searchsorted(kb[ob], common)]
+    va, vb = velocity_l2(fa[sa], lat), velocity_l2(fb[sb], lat)
+    dpos = np.abs(xa[sa] - xb[sb]).max(1)
+    agree = dpos < 1e-5
+
+    def l2(m):
+        return float(np.sqrt(((va[m] - vb[m]) ** 2).sum() / (vb[m] ** 2).sum())) if m.any() else None
+
+    Ua, Ub = _binned_velocity(ia_, xa, fa, sides, lat, bins), _binned_velocity(ib_, xb, fb, sides, lat, bins)
+    return {"moments": [int(len(xa)), int(len(xb))], "velocity_l2_rel": l2(np.ones(len(common), bool)),
+            "matched_cells_frac": float(len(common) / max(len(kb), 1)),
+            "positions_differ_gt_1e-5": int((~agree).sum()), "velocity_l2_rel_positions_agree": l2(agree),
+            "max_pos_err_positions_agree": float(dpos[agree].max()) if agree.any() else None,
+            f"binned{bins}x{bins}_velocity_l2_rel": float(np.sqrt(((Ua - Ub) ** 2).sum() / (Ub ** 2).sum()))}
+
+
+def ensemble_accuracy_leg(sides, taus, ib, x, f, steps=10, timed=5):
+    """FP32DEV vs FP64 on the full benchmark ensemble (all on the GPU, `steps` steps), beside the
+    FP64 step from the FP32-rounded initial state vs FP64, plus the FP64 store's own timing over
+    `timed` of those steps (after one warm-up)."""
+    from direbm_gb300.lattices import D2Q9
+
+    M = len(x)
+    sim = make_sim(sides, taus, "fp32dev", M)
+    sim.set_state(ib, x, f)
+    sim.step(steps)
+    s32 = sim.state_numpy()
+    sim.close()
+    sim = make_sim(sides, taus, "fp64", M)
+    sim.set_state(ib, x, f)
+    sim.step(1)
+    ms64, _ = timed_steps(sim, timed, 0)
+    sim.step(steps - 1 - timed)
+    s64 = sim.state_numpy()
+    xr, fr = fp32_rounded(x, f, D2Q9)
+    sim.set_state(ib, xr, fr)
+    sim.step(steps)
+    s64r = sim.state_numpy()
+    sim.close()
+    fp64 = {"value": M * timed / (ms64 * 1e-3), "unit": "point-steps/s", "ms_per_step": ms64 / timed,
+            "steps": timed, "warmup": 1}
+    out = {"steps": steps,
+           "fp32dev_vs_fp64": compare_states(s32, s64, sides, D2Q9),
+           "fp64_rounded_start_vs_fp64": compare_states(s64r, s64, sides, D2Q9),
+           "note": "all three runs on the GPU; the FP64 step matches the FP64 oracle to 1e-12 at test sizes "
+                   "(128x128 over 10 steps). Points whose positions differ by more than 1e-5 took a thinning, "
+                   "refine or resampling decision that met a near tie (a distance within ~1e-7 of r, a "
+                   "component within ~1e-7 of a cell face, a kappa count or gap-fill threshold at its edge) "
+                   "the other way; the FP64 run from the FP32-rounded start shows the same effect from input "
+                   "rounding alone"}
+    return fp64, out
+
+
+def lbm_leg(steps=1000, warmup=5):
     import torch
 
     from direbm_gb300.lattices import D2Q7, equilibrium
@@ -519,7 +647,7 @@ def adjoint_leg(n=256, steps=100, every=10, tau=0.6, precisions=("fp32dev", "fp6
     return out
 
 
-def sphere_leg(steps=20, steps64=4):
+def sphere_leg(steps=20, steps64=10):
     """Flow past a sphere (the 3D obstacle configuration): D3Q19, periodic box of 160 x 112 x 112
     cells (h = dx = 1) with one jittered point per cell outside a bounce-back sphere of radius 16h
     at (40, 56, 56) (~2.0 M points), uniform initial and inflow velocity 0.04 along x (inflow layer
@@ -576,26 +704,52 @@ def sphere_leg(steps=20, steps64=4):
         sim.step(1 + steps64)
         states[prec] = sim.state_numpy()
         sim.close()
-    # FP32 and FP64 take a few near-tie decisions differently on 2 M points, so the point sets can
-    # differ slightly: compare velocities cell by cell where each run has exactly one point
-    (_, xa, fa), (_, xb, fb) = states["fp32dev"], states["fp64"]
+    # the FP64 run again from the FP32-rounded start: the method's own response to input rounding
+    sim = Simulation([inst], lattice="D3Q19", precision="fp64", dx=DX, r_res=R_RES, cell=CELL,
+                     moment_capacity=int(1.2 * len(x)))
+    sim.set_state(None, *fp32_rounded(x, f, D3Q19))
+    sim.step(1 + steps64)
+    states["fp64_rounded_start"] = sim.state_numpy()
+    sim.close()
 
-    def by_cell(xp):
-        c = np.floor(xp).astype(np.int64)
-        key = (c[:, 2] * dims[1] + c[:, 1]) * dims[0] + c[:, 0]
-        uk, idx, cnt = np.unique(key, return_index=True, return_counts=True)
-        return dict(zip(uk[cnt == 1].tolist(), idx[cnt == 1].tolist()))
+    def cmp3(a, b, bins=4):
+        """Velocity L2 over the cells where each run holds exactly one point, over the subset whose
+        positions also agree to 1e-5, and of the mass-weighted velocity of bins^3 blocks of cells."""
+        (_, xa, fa), (_, xb, fb) = a, b
 
-    ca, cb = by_cell(xa), by_cell(xb)
-    common = sorted(set(ca) & set(cb))
-    ia = np.array([ca[k] for k in common], dtype=np.int64)
-    ib = np.array([cb[k] for k in common], dtype=np.int64)
-    ua, ub = velocity_l2(fa[ia], D3Q19), velocity_l2(fb[ib], D3Q19)
-    out["fp32dev_vs_fp64_after_steps"] = 1 + steps64
-    out["fp32dev_velocity_l2_rel_vs_fp64"] = float(np.sqrt(((ua - ub) ** 2).sum() / (ub ** 2).sum()))
-    out["fp32dev_vs_fp64_points"] = [int(len(xa)), int(len(xb))]
-    out["matched_cells_frac"] = len(common) / max(len(xb), 1)
-    out["max_pos_err_matched"] = float(np.abs(xa[ia] - xb[ib]).max())
+        def key(xp, div=1):
+            c = np.floor(xp).astype(np.int64) // div
+            nd = [-(-d // div) for d in dims]
+            return (c[:, 2] * nd[1] + c[:, 1]) * nd[0] + c[:, 0]
+
+        ka, kb = key(xa), key(xb)
+        ua, ia0, ca = np.unique(ka, return_index=True, return_counts=True)
+        ub, ib0, cb = np.unique(kb, return_index=True, return_counts=True)
+        common, pa, pb = np.intersect1d(ua[ca == 1], ub[cb == 1], return_indices=True)
+        sa, sb = ia0[ca == 1][pa], ib0[cb == 1][pb]
+        va, vb = velocity_l2(fa[sa], D3Q19), velocity_l2(fb[sb], D3Q19)
+        agree = np.abs(xa[sa] - xb[sb]).max(1) < 1e-5
+
+        def l2(m):
+            return float(np.sqrt(((va[m] - vb[m]) ** 2).sum() / (vb[m] ** 2).sum())) if m.any() else None
+
+        def binned(xp, fp):
+            k = key(xp, bins)
+            nbin = int(np.prod([-(-d // bins) for d in dims]))
+            mass = np.bincount(k, weights=fp.sum(1), minlength=nbin)
+            mom = fp @ D3Q19.C
+            u = np.stack([np.bincount(k, weights=mom[:, a], minlength=nbin) for a in range(3)], 1)
+            return u / np.maximum(mass, 1e-300)[:, None]
+
+        Ua, Ub = binned(xa, fa), binned(xb, fb)
+        return {"points": [int(len(xa)), int(len(xb))], "velocity_l2_rel": l2(np.ones(len(common), bool)),
+                "matched_cells_frac": len(common) / max(len(xb), 1),
+                "positions_differ_gt_1e-5": int((~agree).sum()), "velocity_l2_rel_positions_agree": l2(agree),
+                f"binned{bins}x{bins}x{bins}_velocity_l2_rel": float(np.sqrt(((Ua - Ub) ** 2).sum() / (Ub ** 2).sum()))}
+
+    out["compared_after_steps"] = 1 + steps64
+    out["fp32dev_vs_fp64"] = cmp3(states["fp32dev"], states["fp64"])
+    out["fp64_rounded_start_vs_fp64"] = cmp3(states["fp64_rounded_start"], states["fp64"])
     out["speedup_fp32dev_vs_fp64"] = out["fp32dev"]["point_steps_per_s"] / out["fp64"]["point_steps_per_s"]
     return out
 
@@ -622,6 +776,60 @@ def _oracle_instance_steps(args):
     return pts, time.perf_counter() - t0
 
 
+REF_SIM_DIR = ROOT / "baseline" / "_ref"  # the reference's CPU package (oracle/install_reference.py)
+
+
+def _reference_simulator_job(args):
+    """The reference's own CPU simulator (direbm.reference.Simulator, unoptimised pure Python) on an
+    n x n block of config-1 density (spacing h = dx = 1, jitter U(+-0.25)) with the Taylor-Green
+    velocity u0 = 0.05, D2Q9 built from the reference's generic Lattice, tau 0.6, in the reference's
+    own unbounded form (r = dx, thinning radius dx/4).  Returns (input point-steps, seconds)."""
+    n, steps, seed = args
+    sys.path.insert(0, str(REF_SIM_DIR))
+    from direbm.lattices import Lattice
+    from direbm.physics import equilibrium
+    from direbm.reference import Moment, Simulator
+
+    d2q9 = Lattice(C=np.array([[0, 0], [1, 0], [0, 1], [-1, 0], [0, -1], [1, 1], [-1, 1], [-1, -1], [1, -1]], float),
+                   W=np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4), cs2=1.0 / 3.0, name="D2Q9")
+    rng = np.random.default_rng(seed)
+    x = (np.indices((n, n)).reshape(2, -1).T[:, ::-1] + 0.5).astype(np.float64)
+    x += rng.uniform(-0.25, 0.25, size=x.shape)
+    k = 2 * np.pi / n
+    u = 0.05 * np.stack([-np.cos(k * x[:, 0]) * np.sin(k * x[:, 1]), np.sin(k * x[:, 0]) * np.cos(k * x[:, 1])], 1)
+    f = equilibrium(np.ones(len(x)), u, d2q9)
+    sim = Simulator([Moment(f=f[i].copy(), x=x[i].copy()) for i in range(len(x))], tau=0.6, lattice=d2q9)
+    t0 = time.perf_counter()
+    pts = 0
+    for _ in range(steps):
+        pts += len(sim.moments)
+        sim.step()
+    return pts, time.perf_counter() - t0
+
+
+def reference_simulator_leg(n=12, steps=2):
+    """The reference's own CPU step timed on this host: one process, then one process per core on
+    independent seeds (aggregate point-steps/s).  None when the reference is not installed."""
+    import multiprocessing as mp
+
+    if not (REF_SIM_DIR / "direbm" / "__init__.py").exists():
+        return None
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")  # this process already holds a CUDA context
+    with ctx.Pool(cores) as pool:
+        pts1, sec1 = pool.apply(_reference_simulator_job, ((n, steps, 0),))
+        t0 = time.perf_counter()
+        res = pool.map(_reference_simulator_job, [(n, steps, s) for s in range(cores)])
+        wall = time.perf_counter() - t0
+    ptsn = sum(p for p, _ in res)
+    sample = (f"{n}x{n} block of config-1 density, TG u0 0.05, D2Q9, tau 0.6, first {steps} steps (the moment "
+              f"count grows from {n * n} as the unbounded block spreads), reference form r = dx, cell dx/4")
+    return {"kind": "reference", "what": "direbm.reference.Simulator (the reference's CPU path, pure Python)",
+            "one_process": {"value": pts1 / sec1, "unit": "point-steps/s", "cores": 1, "seconds": sec1},
+            "all_cores": {"value": ptsn / wall, "unit": "point-steps/s", "cores": cores, "seconds": wall},
+            "sample": sample}
+
+
 def cpu_baseline_leg(n=128, steps=2, lbm_steps=3):
     pts, sec = _oracle_instance_steps((n, 0.8, 100, steps))
     out = {"value": pts / sec, "unit": "point-steps/s", "cores": 1, "kind": "port",
@@ -637,39 +845,63 @@ def cpu_baseline_leg(n=128, steps=2, lbm_steps=3):
     sec = time.perf_counter() - t0
     out["lbm"] = {"value": 1024 * 1024 * lbm_steps / sec, "unit": "node-steps/s", "cores": 1, "kind": "port",
                   "sample": f"numpy oracle HexLBM, one 1024x1024 run, {lbm_steps} steps, {sec:.1f} s"}
+    ref = reference_simulator_leg()
+    out["reference_simulator"] = ref if ref is not None else {
+        "unavailable": "the reference package is not installed under baseline/_ref (oracle/install_reference.py)"}
     return out
+
+
+# The reference arm steps real ensemble members no larger than this (a third of the ensemble), so
+# that one timed step of all host cores stays within a few seconds.
+REF_ARM_MAX_POINTS = 16384
+
+
+def ensemble_config(n_inst=N_INST):
+    """The benchmark workload's description, shared by both arms."""
+    sides, _ = ensemble_spec(n_inst)
+    return {"workload": f"batched ensemble: {n_inst} periodic 2D D2Q9 runs, M log-uniform 4k-256k (seed 1), "
+                        "tau U(0.55,1), 8 Fourier modes RMS 0.02, r 1.5h, cell h, FP32-deviation store",
+            "moments": int((np.asarray(sides, dtype=np.int64) ** 2).sum()), "instances": int(n_inst),
+            "store": "fp32dev", "graphs": True, "l2": "state (~0.8 GB) larger than L2, no flush"}
 
 
 def run_reference(args):
     """The reference arm: the CPU oracle (numpy restatement of the reference GPU step) on all host
-    cores, one independent ensemble instance per worker process."""
+    cores.  Each timed step, every core steps one member of the benchmark ensemble itself (its own
+    size, seed, tau and velocity field), cycling through the members of at most REF_ARM_MAX_POINTS
+    points."""
     import multiprocessing as mp
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    sides, taus = ensemble_spec()
-    # bounded sample: the first `cores` instances clipped to 64x64 (smallest ensemble size)
-    jobs = [(64, float(taus[i % len(taus)]), 100 + i, 1) for i in range(cores)]
+    sides, taus = ensemble_spec(args.instances)
+    members = [i for i in range(len(sides)) if int(sides[i]) ** 2 <= REF_ARM_MAX_POINTS]
+
+    def jobs(r):
+        return [(int(sides[i]), float(taus[i]), 100 + i, 1)
+                for i in (members[(r * cores + w) % len(members)] for w in range(cores))]
+
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        for _ in range(args.warmup):
-            pool.map(_oracle_instance_steps, jobs)
+        for r in range(args.warmup):
+            pool.map(_oracle_instance_steps, jobs(r))
         t0 = time.perf_counter()
         pts = 0
-        for _ in range(args.steps):
-            pts += sum(p for p, _ in pool.map(_oracle_instance_steps, jobs))
+        for r in range(args.steps):
+            pts += sum(p for p, _ in pool.map(_oracle_instance_steps, jobs(args.warmup + r)))
         sec = time.perf_counter() - t0
     value = pts / sec
+    sample = (f"{cores} worker processes, each stepping one ensemble member per timed step (members with at most "
+              f"{REF_ARM_MAX_POINTS} points: {len(members)} of {len(sides)}, sizes "
+              f"{int(min(sides[members]) ** 2)}-{int(max(sides[members]) ** 2)}), FP64 numpy")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batched ensemble, D2Q9, r 1.5h, cell h (CPU oracle sample)",
-                   "sample": f"{cores} x 64x64 instances, 1 step each per timed step"},
-        "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} worker processes x one 64x64 instance step"},
+        "config": ensemble_config(args.instances),
+        "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -757,12 +989,8 @@ def run_ours(args):
     e2e = e2e_leg(sim, ib, x, f)
     sim.close()
 
-    # FP64 store on the same workload
-    sim64 = make_sim(sides, taus, "fp64", M)
-    sim64.set_state(ib, x, f)
-    ms64, _ = timed_steps(sim64, 2, 1)
-    sim64.close()
-    fp64 = {"value": M * 2 / (ms64 * 1e-3), "unit": "point-steps/s", "ms_per_step": ms64 / 2, "steps": 2}
+    # FP64 store on the same workload, and FP32DEV vs FP64 after the same steps on the whole ensemble
+    fp64, acc_ens = ensemble_accuracy_leg(sides, taus, ib, x, f)
 
     acc = accuracy_leg()
     lbm = lbm_leg()
@@ -773,15 +1001,13 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched ensemble: {args.instances} periodic 2D D2Q9 runs, M log-uniform 4k-256k (seed 1), "
-                               "tau U(0.55,1), 8 Fourier modes RMS 0.02, r 1.5h, cell h, FP32-deviation store",
-                   "moments": int(M), "instances": args.instances, "store": "fp32dev", "graphs": True,
-                   "tiling": {"tile_width": tuning["tile_width"], "persistent": tuning["persistent"],
-                              "timings_ms": tuning["timings"]},
-                   "l2": "state (~0.8 GB) larger than L2, no flush"},
+        "config": ensemble_config(args.instances),
+        "tiling": {"tile_width": tuning["tile_width"], "persistent": tuning["persistent"],
+                   "timings_ms": tuning["timings"]},
         "roofline": roof, "stage_ms": stage_ms, "step_roofline": step_roof,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
-        "fp64": fp64, "speedup_fp32dev_vs_fp64": value / world / fp64["value"], "accuracy": acc, "lbm": lbm,
+        "fp64": fp64, "speedup_fp32dev_vs_fp64": value / world / fp64["value"], "accuracy": acc,
+        "accuracy_ensemble": acc_ens, "lbm": lbm,
         "adjoint": adj, "sphere": sph,
     }
     print(json.dumps(line), flush=True)
@@ -797,8 +1023,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=N_INST, help="first N ensemble members (profiling runs)")
-    ap.add_argument("--legs", default="all", choices=["all", "main", "adjoint", "sphere", "lbm", "e2e"],
-                    help="main = timed step only; adjoint / sphere / lbm / e2e = that leg only")
+    ap.add_argument("--legs", default="all",
+                    choices=["all", "main", "adjoint", "sphere", "lbm", "e2e", "accuracy", "cpu"],
+                    help="main = timed step only; adjoint / sphere / lbm / e2e / accuracy / cpu = that leg only")
     ap.add_argument("--adjoint-n", type=int, default=256, help="adjoint leg: points per side")
     ap.add_argument("--adjoint-steps", type=int, default=100, help="adjoint leg: rollout steps")
     ap.add_argument("--adjoint-every", type=int, default=10, help="adjoint leg: checkpoint interval")
@@ -828,6 +1055,18 @@ def main():
         sim.set_state(ib, x, f)
         print(json.dumps({"e2e": e2e_leg(sim, ib, x, f)}), flush=True)
         sim.close()
+        return
+    if args.legs == "accuracy" and args.impl == "ours":
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        sides, taus = ensemble_spec(args.instances)
+        ib, x, f = build_ensemble(sides, taus)
+        fp64, acc_ens = ensemble_accuracy_leg(sides, taus, ib, x, f)
+        print(json.dumps({"fp64": fp64, "accuracy_ensemble": acc_ens, "accuracy": accuracy_leg()}), flush=True)
+        return
+    if args.legs == "cpu" and args.impl == "ours":
+        print(json.dumps({"cpu_baseline": cpu_baseline_leg()}), flush=True)
         return
     if args.legs == "adjoint" and args.impl == "ours":
         import torch
