@@ -322,24 +322,57 @@ def _binned_velocity(inst, xp, fp, sides, lat, b):
     return u / np.maximum(mass, 1e-300)[:, None]
 
 
+def _powers(z, kmax):
+    """Columns z^k for k = -kmax .. kmax (|z| = 1, so z^-k = conj(z^k))."""
+    out = np.empty((len(z), 2 * kmax + 1), np.complex128)
+    out[:, kmax] = 1.0
+    w = np.ones_like(z)
+    for k in range(1, kmax + 1):
+        w = w * z
+        out[:, kmax + k] = w
+        out[:, kmax - k] = np.conj(w)
+    return out
+
+
+def _low_modes(inst, xp, fp, sides, lat, kmax=4):
+    """Fourier coefficients of the momentum field sum_p j_p exp(-2 pi i k.x_p / n) over the wave
+    vectors |k_x|, |k_y| <= kmax of each instance (the band of the initial velocity field)."""
+    inst = np.asarray(inst, np.int64)
+    order = np.argsort(inst, kind="stable")
+    bounds = np.searchsorted(inst[order], np.arange(len(sides) + 1))
+    ks = np.arange(-kmax, kmax + 1)
+    j = fp @ lat.C
+    out = np.zeros((len(sides), 2, len(ks), len(ks)), np.complex128)
+    for i, n in enumerate(sides):
+        sel = order[bounds[i]:bounds[i + 1]]
+        if len(sel) == 0:
+            continue
+        ex, ey = (_powers(np.exp(-2j * np.pi / float(n) * xp[sel, a]), kmax) for a in range(2))
+        for a in range(2):
+            out[i, a] = (ex * j[sel, a][:, None]).T @ ey
+    return out
+
+
 def compare_states(a, b, sides, lat, bins=4):
     """State a against state b (each (inst, pos, f) of one ensemble).
 
     Per point: velocity L2 over the cells where each holds exactly one point (the point sets can
     differ where a near-tie decision went the other way), and over the subset whose points also
     agree in position to 1e-5 cells.  Per field: the L2 of the mass-weighted velocity of each
-    bins x bins block of cells (the macroscopic field, which does not depend on which of two
-    nearly equal decisions a point took)."""
+    bins x bins block of cells, and of the momentum field's Fourier coefficients in the band of the
+    initial field (|k_x|, |k_y| <= 4): the macroscopic flow, against which the choice a point made
+    at a near tie is a local, small-scale perturbation."""
     (ia_, xa, fa), (ib_, xb, fb) = a, b
     ia_ = np.zeros(len(xa), np.int64) if ia_ is None else np.asarray(ia_, np.int64)
     ib_ = np.zeros(len(xb), np.int64) if ib_ is None else np.asarray(ib_, np.int64)
     ka, kb = _cell_keys(ia_, xa, sides), _cell_keys(ib_, xb, sides)
-    ua, ca = np.unique(ka, return_counts=True)
-    ub, cb = np.unique(kb, return_counts=True)
-    common = np.intersect1d(ua[ca == 1], ub[cb == 1])
-    oa, ob = np.argsort(ka, kind="stable"), np.argsort(kb, kind="stable")
-    sa = oa[np.searchsorted(ka[oa], common)]
-    sb = ob[np.searchsorted(kb[ob], common)]
+    ncell = int((np.asarray(sides, dtype=np.int64) ** 2).sum())
+    ca, cb = np.bincount(ka, minlength=ncell), np.bincount(kb, minlength=ncell)
+    pa, pb = np.zeros(ncell, np.int64), np.zeros(ncell, np.int64)
+    pa[ka] = np.arange(len(ka))  # the point of each single-point cell
+    pb[kb] = np.arange(len(kb))
+    common = np.flatnonzero((ca == 1) & (cb == 1))
+    sa, sb = pa[common], pb[common]
     va, vb = velocity_l2(fa[sa], lat), velocity_l2(fb[sb], lat)
     dpos = np.abs(xa[sa] - xb[sb]).max(1)
     agree = dpos < 1e-5
@@ -348,11 +381,13 @@ def compare_states(a, b, sides, lat, bins=4):
         return float(np.sqrt(((va[m] - vb[m]) ** 2).sum() / (vb[m] ** 2).sum())) if m.any() else None
 
     Ua, Ub = _binned_velocity(ia_, xa, fa, sides, lat, bins), _binned_velocity(ib_, xb, fb, sides, lat, bins)
+    La, Lb = _low_modes(ia_, xa, fa, sides, lat), _low_modes(ib_, xb, fb, sides, lat)
     return {"moments": [int(len(xa)), int(len(xb))], "velocity_l2_rel": l2(np.ones(len(common), bool)),
             "matched_cells_frac": float(len(common) / max(len(kb), 1)),
             "positions_differ_gt_1e-5": int((~agree).sum()), "velocity_l2_rel_positions_agree": l2(agree),
             "max_pos_err_positions_agree": float(dpos[agree].max()) if agree.any() else None,
-            f"binned{bins}x{bins}_velocity_l2_rel": float(np.sqrt(((Ua - Ub) ** 2).sum() / (Ub ** 2).sum()))}
+            f"binned{bins}x{bins}_velocity_l2_rel": float(np.sqrt(((Ua - Ub) ** 2).sum() / (Ub ** 2).sum())),
+            "low_mode_momentum_l2_rel": float(np.linalg.norm(La - Lb) / np.linalg.norm(Lb))}
 
 
 def ensemble_accuracy_leg(sides, taus, ib, x, f, steps=10, timed=5):
