@@ -11,6 +11,7 @@ so L2 is not flushed between steps.
 Keys beyond the base contract:
   roofline      dominant kernel's algorithmic bytes / its CUDA-event duration vs measured HBM peak
   step_roofline the whole step against the per-point-step byte model of the method
+  full_run      the configuration's 100-step run from the initial state, mean and per 10 steps
   fp64          the same workload in the FP64 store (5 timed steps: GB300 FP64 is slow)
   accuracy      velocity L2 error vs the FP64 oracle on a 4096-point instance, and against the
                 FP64 GPU step after 1/10/50/200 steps beside FP64 from the FP32-rounded start
@@ -115,16 +116,21 @@ def instance_points(n, seed):
     return np.mod(x, n)
 
 
-def build_ensemble(sides, taus):
+def build_ensemble(sides, taus, members=None):
+    """Initial state of the ensemble members `members` (all by default): member i's points and
+    velocity field come from seed 100 + i whatever shard it lands in; instance indices are local
+    (0.. in the order of `members`)."""
     from direbm_gb300.lattices import D2Q9, equilibrium
 
+    members = range(len(sides)) if members is None else members
     xs, fs, ib = [], [], []
-    for i, n in enumerate(sides):
-        x = instance_points(int(n), 100 + i)
-        u = fourier_velocity(x, int(n), 100 + i)
+    for li, i in enumerate(members):
+        n = int(sides[i])
+        x = instance_points(n, 100 + int(i))
+        u = fourier_velocity(x, n, 100 + int(i))
         xs.append(x)
         fs.append(equilibrium(np.ones(len(x)), u, D2Q9))
-        ib.append(np.full(len(x), i, dtype=np.int32))
+        ib.append(np.full(len(x), li, dtype=np.int32))
     return np.concatenate(ib), np.concatenate(xs), np.concatenate(fs)
 
 
@@ -207,6 +213,28 @@ def timed_steps(sim, steps, warmup):
     ev1.record()
     torch.cuda.synchronize()
     return ev0.elapsed_time(ev1), _lib.launch_count() - l0
+
+
+def full_run_leg(sim, ib, x, f, steps=100, chunk=10):
+    """The configuration's whole run: `steps` steps from the initial state (graphs captured by two
+    untimed steps before the reset), timed in chunks of `chunk` steps with CUDA events.  The step
+    slows as the run goes on: refine moves leave ~1 % of cells holding two moments by step 100,
+    and the window kernels then take the two-item path in almost every tile."""
+    import torch
+
+    sim.set_state(ib, x, f)
+    sim.step(2)
+    sim.set_state(ib, x, f)
+    torch.cuda.synchronize()
+    chunks = []
+    for _ in range(steps // chunk):
+        ms, _ = timed_steps(sim, chunk, 0)
+        chunks.append(ms / chunk)
+    sim.check_status()
+    M = len(x)
+    mean = float(np.mean(chunks))
+    return {"steps": steps, "ms_per_step": mean, "value": M / (mean * 1e-3), "unit": "point-steps/s",
+            "ms_per_step_by_chunk": [round(c, 3) for c in chunks], "chunk": chunk}
 
 
 def roofline_from_profile(sim, M, P, peak):
@@ -934,7 +962,7 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": ensemble_config(args.instances),
         "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -945,22 +973,29 @@ def run_reference(args):
 # ---- main ----------------------------------------------------------------------------------------
 
 def max_over_ranks(ms: float, dist=None) -> float:
-    """The slowest rank's time (every rank gets it); a plain float without a process group.  The
-    tensor lives where the group's backend wants it (CUDA for NCCL, host for gloo)."""
+    """The slowest rank's time (every rank gets it); a plain float without a process group."""
     if dist is None or not dist.is_initialized():
         return float(ms)
+    from direbm_gb300.shard import max_over_ranks as mor
+
+    return mor(ms)
+
+
+def sum_over_ranks(v: float, dist=None) -> float:
+    if dist is None or not dist.is_initialized():
+        return float(v)
     import torch
 
     dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
-    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
 
-def whole_job_rate(moments_per_rank: int, world: int, steps: int, ms: float) -> float:
-    """Point-steps/s of the whole job: every rank advances its own replica of the ensemble
-    (weak scaling), so the work is world x moments x steps over the slowest rank's time."""
-    return world * moments_per_rank * steps / (ms * 1e-3)
+def whole_job_rate(moments_total: int, steps: int, ms: float) -> float:
+    """Point-steps/s of the whole job: the ranks share one ensemble (each steps its shard of the
+    instances, strong scaling), so the work is all moments x steps over the slowest rank's time."""
+    return moments_total * steps / (ms * 1e-3)
 
 
 def run_ours(args):
@@ -981,9 +1016,15 @@ def run_ours(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
 
     sides, taus = ensemble_spec(args.instances)
-    ib, x, f = build_ensemble(sides, taus)
+    # one ensemble, its instances partitioned over the ranks by point count (no exchange while
+    # stepping); at N = 1 the one shard is the whole ensemble
+    from direbm_gb300.shard import partition
+
+    members = partition(np.asarray(sides, dtype=np.int64) ** 2, world)[rank]
+    ib, x, f = build_ensemble(sides, taus, members)
     M = len(x)
-    sim = make_sim(sides, taus, "fp32dev", M)
+    M_total = int((np.asarray(sides, dtype=np.int64) ** 2).sum())
+    sim = make_sim(sides[members], taus[members], "fp32dev", M)
     sim.set_state(ib, x, f)
     from direbm_gb300.autotune import autotune
 
@@ -999,12 +1040,34 @@ def run_ours(args):
     ms = max_over_ranks(ms, dist)
     P = sim.count()
     sim.check_status()
-    value = whole_job_rate(M, world, args.steps, ms)
+    value = whole_job_rate(M_total, args.steps, ms)
+    moments_after = int(sum_over_ranks(P, dist))
 
-    if rank != 0:
-        if dist:
-            dist.barrier()
-            dist.destroy_process_group()
+    if world > 1:  # the whole ensemble's result: every shard's state gathered on rank 0
+        from direbm_gb300.shard import gather_state
+
+        gi, gp, gf = sim.state()
+        got = gather_state(gi, gp, gf, members)
+        e2e = e2e_leg(sim, ib, x, f)
+        e2e_ms = max_over_ranks(e2e["ms_per_step"], dist)
+        h2d = sum_over_ranks(e2e["h2d_bytes_per_step"], dist)
+        d2h = sum_over_ranks(e2e["d2h_bytes_per_step"], dist)
+        sim.close()
+        if rank == 0:
+            print(json.dumps({
+                "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {**ensemble_config(args.instances), "parallelism": f"instance shards x{world}"},
+                "shards": {"moments_max_rank": int(max_over_ranks(M, dist)), "moments_total": M_total,
+                           "gathered_moments": int(got[0].shape[0]), "moments_after_steps": moments_after},
+                "e2e": {"value": M_total / (e2e_ms * 1e-3), "unit": "point-steps/s",
+                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+                "gpu_launches": int(launches), "clocks": clocks}), flush=True)
+        else:
+            max_over_ranks(M, dist)
+        dist.barrier()
+        dist.destroy_process_group()
         return
 
     dom, stage_ms, roof = roofline_from_profile(sim, sim.count(), P, peak)
@@ -1021,6 +1084,7 @@ def run_ours(args):
               flush=True)
         sim.close()
         return
+    run100 = full_run_leg(sim, ib, x, f)
     e2e = e2e_leg(sim, ib, x, f)
     sim.close()
 
@@ -1034,12 +1098,12 @@ def run_ours(args):
     cpu = cpu_baseline_leg()
     line = {
         "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": ensemble_config(args.instances),
         "tiling": {"tile_width": tuning["tile_width"], "persistent": tuning["persistent"],
                    "timings_ms": tuning["timings"]},
-        "roofline": roof, "stage_ms": stage_ms, "step_roofline": step_roof,
+        "roofline": roof, "stage_ms": stage_ms, "step_roofline": step_roof, "full_run": run100,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
         "fp64": fp64, "speedup_fp32dev_vs_fp64": value / world / fp64["value"], "accuracy": acc,
         "accuracy_ensemble": acc_ens, "lbm": lbm,
