@@ -93,6 +93,8 @@ _SIGS = {
     "dbm_bin_fields_tmp_bytes": (_i64, [_i64]),
     "dbm_bin_fields_f64": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, ctypes.c_int, _vp, ctypes.c_int, _vp, _vp,
                                           _vp, _vp, _vp]),
+    "dbm_bin_fields3_f64": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, ctypes.c_int, _vp, ctypes.c_int, _vp,
+                                           ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "dbm_lbm_step": (ctypes.c_int, [ctypes.c_int, _vp, _vp, _i32, _i32, _i32, _vp, _f64, _i32, _vp, _vp]),
     "dbm_sim_create": (ctypes.c_int, [ctypes.POINTER(SimDesc), ctypes.POINTER(InstanceDesc), _i32, ctypes.POINTER(_vp)]),
     "dbm_sim_destroy": (ctypes.c_int, [_vp]),

@@ -118,6 +118,13 @@ int64_t dbm_bin_fields_tmp_bytes(int64_t n);
 int dbm_bin_fields_f64(const double* d_x, const double* d_f, int64_t n, int lattice, const double* d_ex, int nex,
                        const double* d_ey, int ney, double* d_mass, double* d_momx, double* d_momy, void* d_tmp,
                        void* stream);
+/* The same binning in 3D (the reference bins in 2D only; its hand-off notes list 3D binning as
+ * needed for macroscopic 3D fields): x (n,3), f (n,Q) FP64 with a 3D lattice, edge arrays ex, ey,
+ * ez, numpy histogramdd's bin rule per axis, per-bin mass and momentum indexed [iz][iy][ix].  Bins
+ * sum their moments in input order.  d_tmp: dbm_bin_fields_tmp_bytes(n) bytes. */
+int dbm_bin_fields3_f64(const double* d_x, const double* d_f, int64_t n, int lattice, const double* d_ex, int nex,
+                        const double* d_ey, int ney, const double* d_ez, int nez, double* d_mass, double* d_momx,
+                        double* d_momy, double* d_momz, void* d_tmp, void* stream);
 
 /* ---- the fused DiReBM simulator -----------------------------------------------------------
  * Replaces direbm/warp/simulator.py:25-77 (GpuSimulator) and the pipeline it drives.  A handle

@@ -50,6 +50,24 @@ def test_fields_match_reference(golden):
     np.testing.assert_allclose(u, g["u"], rtol=1e-13, atol=1e-15)
 
 
+def test_fields3_reduces_to_the_reference_2d_golden(golden):
+    """The 3D binning restatement pinned to the reference's 2D golden: the golden's moments placed
+    in one z slab (z = 0.5, one bin of height 1) with the D2Q7 velocities extended by c_z = 0 bin to
+    the golden's mass per bin (density x h) and velocity, and an empty z slab stays empty."""
+    from types import SimpleNamespace
+
+    g = golden("fields")
+    x3 = np.concatenate([g["x"], np.full((len(g["x"]), 1), 0.5)], 1)
+    lat3 = SimpleNamespace(C=np.concatenate([D2Q7.C, np.zeros((7, 1))], 1))
+    rho3, u3, ext = fields.bin_fields3(x3, g["f"], -3, 4, 1.0, lat3)
+    iz = 3  # the slab [0, 1) among edges -3..4
+    np.testing.assert_allclose(rho3[iz], g["rho"], rtol=1e-14, atol=0)
+    np.testing.assert_allclose(u3[iz, ..., :2], g["u"], rtol=1e-12, atol=1e-15)
+    assert (u3[..., 2] == 0).all()
+    assert (np.delete(rho3, iz, axis=0) == 0).all()
+    assert ext == (-3, 4) * 3
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_stage_dispersion_and_thinning_match_reference_kat(golden, seed):
     g = golden("propagation")
