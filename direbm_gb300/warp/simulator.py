@@ -9,8 +9,13 @@ The reference domain is unbounded.  The fused step works on a dense cell grid, s
 run is kept in a bounded box that is re-planned as the material spreads: moments move by at most
 max|c|*dx per step (every new moment is a weighted mean of component positions), so a box with a
 margin of (replan_every + 1) steps of growth cannot be left before the next planning point; at
-that point the box is re-centred on the current bounding box if needed.  A device status bit
-(out_of_box) guards the invariant and raises if it is ever broken.
+that point the box is re-centred on the current bounding box if needed.  The bounding box is a
+device reduction (two D-vectors reach the host) and a re-plan moves the state device to device
+through the world-position export and import (which re-derive each moment's cell, offset and, in
+the FP32-deviation store, its FP32 density, so a re-planned run can differ from an unmoved one in
+the last bits).
+A device status bit (out_of_box) guards the invariant; ``step`` does not wait for the device, and
+the status is read at the next planning point or state read, which raise if a bit is set.
 
 Extra keyword arguments (not in the reference): ``lattice``, ``r_res`` (default dx), ``cell``
 (default dx/alpha), ``precision`` ("fp32dev" or "fp64"), ``box`` ((lo, hi) world corners of a fixed
@@ -20,6 +25,7 @@ box), ``periodic`` (with ``box``), ``graphs``.
 from __future__ import annotations
 
 import numpy as np
+import torch
 
 from ..lattices import D2Q7, equilibrium, get
 from ..sim import Instance, Simulation
@@ -66,6 +72,7 @@ class GpuSimulator:
         self.fixed_box = box is not None
         self.periodic = bool(periodic) and self.fixed_box
         self.iteration = 0
+        self.replanned_at = []  # iterations at which the box moved (the state went through set_state)
         self._since_plan = 0
         self._sim = None
         self._box = None
@@ -97,6 +104,8 @@ class GpuSimulator:
         self._box = (np.asarray(lo), np.asarray(hi))
 
     def _plan(self, pos, m):
+        """Box around the points `pos` (or any array whose rows span them, such as the (2, D)
+        bounding box) for m moments."""
         if len(pos) == 0:
             lo = np.zeros(self.lattice.D)
             hi = np.zeros(self.lattice.D)
@@ -110,41 +119,54 @@ class GpuSimulator:
         self._make(blo, bhi, m)
 
     def _maybe_replan(self):
+        """Every replan_every steps: the bounding box of the moments, reduced on the device (2 D
+        numbers reach the host), against the box; a re-plan moves the state device to device."""
         if self.fixed_box or self._since_plan < self.replan_every:
             return
         self._since_plan = 0
-        _, pos, f = self._sim.state_numpy()
-        if len(pos) == 0:
+        self._sim.check_status()  # the steps since the last planning point, read once
+        _, pos, f = self._sim.state()
+        if pos.shape[0] == 0:
             return
+        ext = torch.stack([pos.amin(0), pos.amax(0)]).cpu().numpy()
         g = self._growth()
-        lo_c = np.floor((pos.min(axis=0) - g) / self.cell)
-        hi_c = np.ceil((pos.max(axis=0) + g) / self.cell)
+        lo_c = np.floor((ext[0] - g) / self.cell)
+        hi_c = np.ceil((ext[1] + g) / self.cell)
         blo, bhi = self._box
         if np.all(lo_c >= blo) and np.all(hi_c <= bhi):
             return
-        self._plan(pos, len(pos))
+        self._plan(ext, pos.shape[0])
         self._sim.set_state(None, pos, f)
+        self.replanned_at.append(self.iteration)
 
     # ---- reference API -----------------------------------------------------------------------------
     def step(self):
+        """One step, queued without a host wait: the device status (out-of-box, non-finite) is read
+        at the next planning point or state read, which raise on a bad bit."""
         self._maybe_replan()
         self._sim.step(1)
-        self._sim.check_status()
         self.iteration += 1
         self._since_plan += 1
 
+    def check(self):
+        """Raise if any step so far set a device status bit (host wait)."""
+        self._sim.check_status()
+
     def moments(self):
         """(positions (N, D) FP32, f (N, Q) FP32) as numpy."""
+        self._sim.check_status()
         _, pos, f = self._sim.state_numpy()
         return pos.astype(np.float32), f.astype(np.float32)
 
     @property
     def pos_m(self):
+        self._sim.check_status()
         _, pos, _ = self._sim.state()
         return DeviceArray(pos.float())
 
     @property
     def f_m(self):
+        self._sim.check_status()
         _, _, f = self._sim.state()
         return DeviceArray(f.float())
 

@@ -1,8 +1,10 @@
 """Install the reference's CPU package (``direbm``) into ``baseline/_ref`` for the CPU baselines.
 
 Test infrastructure: ``bench.py`` times the reference's own CPU simulator
-(``direbm.reference.Simulator``) from this install when it is present; nothing in the library
-imports it.  ``baseline/_ref`` is git-ignored but travels with the repository to the GPU host.
+(``direbm.reference.Simulator``) from this install when it is present, and
+tests/test_gpu_reference_suite.py runs the reference's own GPU tests (copied beside the package)
+against this library; nothing in the library imports it.  ``baseline/_ref`` is git-ignored but
+travels with the repository to the GPU host.
 
 The reference's CPU path is pure Python over numpy.  ``pip install --no-index --target`` is tried
 first; the reference builds with the hatchling backend, which the offline wheelhouse does not
@@ -45,7 +47,12 @@ def main(src: str) -> int:
             shutil.rmtree(target)
         shutil.copytree(src_p / "direbm", target, ignore=shutil.ignore_patterns("__pycache__"))
         how = f"pip install failed ({tail[0]}); pure-Python package directory placed instead"
-    (DEST / "INSTALL.txt").write_text(f"source: {src_p}\nmethod: {how}\n")
+    # the reference's own tests, run unchanged against this library by tests/test_gpu_reference_suite.py
+    tests = DEST / "tests"
+    if tests.exists():
+        shutil.rmtree(tests)
+    shutil.copytree(src_p / "tests", tests, ignore=shutil.ignore_patterns("__pycache__"))
+    (DEST / "INSTALL.txt").write_text(f"source: {src_p}\nmethod: {how}\ntests: copied to baseline/_ref/tests\n")
     print(how)
     return 0
 

@@ -189,6 +189,30 @@ def test_gpu_simulator_replans_unbounded_box():
     assert np.linalg.norm(xp, axis=1).max() > 12.0
 
 
+def test_gpu_simulator_replanned_run_equals_a_fixed_box_run():
+    """Re-planning (device bounding box, state moved device to device) depends on nothing but the
+    export/import it goes through: the unbounded run equals, bit for bit, a run in one fixed box
+    that holds the whole spread and takes the same export/import at the same iterations (cells
+    shift by whole cells; offsets and sums are cell-relative)."""
+    pos = np.zeros((1, 2))
+    f = equilibrium(np.float64(1.5), np.zeros(2))[None, :]
+    for prec in ("fp32dev", "fp64"):
+        moving = _w().GpuSimulator(pos, f, tau=0.6, replan_every=3, precision=prec)
+        for _ in range(15):
+            moving.step()
+        moving.check()
+        assert len(moving.replanned_at) >= 2
+        fixed = _w().GpuSimulator(pos, f, tau=0.6, box=((-24.0, -24.0), (24.0, 24.0)), precision=prec)
+        for i in range(15):
+            if i in moving.replanned_at:
+                _, p, ff = fixed.simulation.state()
+                fixed.simulation.set_state(None, p, ff)
+            fixed.step()
+        a, b = moving.moments(), fixed.moments()
+        np.testing.assert_array_equal(a[0], b[0], err_msg=prec)
+        np.testing.assert_array_equal(a[1], b[1], err_msg=prec)
+
+
 # ---- tests/test_warp_lbm.py -----------------------------------------------------------------
 
 def test_gpu_lbm_matches_cpu(golden):
