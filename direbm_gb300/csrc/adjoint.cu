@@ -1079,6 +1079,10 @@ __global__ void __launch_bounds__(256) k_bwd_moment(const __grid_constant__ RecK
       for (int a = 0; a < D; ++a) u[a] = mom[a] / rho;
       float deq[Q];
       eq_deviation_f32<Q, D>(rho, u, K.L, deq);
+      float m0 = 0.f;  // the forward's projection onto the deviations' mass and momentum
+#pragma unroll
+      for (int k = 0; k < Q; ++k) m0 += dv[k];
+      conserve_moments_f32<Q, D>(deq, m0, mom, K.L);
 #pragma unroll
       for (int k = 0; k < Q; ++k) {
         fmfeq[k] = deq[k] - dv[k];

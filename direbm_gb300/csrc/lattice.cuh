@@ -127,6 +127,35 @@ __device__ __forceinline__ void eq_deviation_f32(float rho, const float (&u)[D],
   }
 }
 
+// Restore the conserved moments of an FP32 equilibrium vector t: t_k -= W_k (dm + c_k . dj / cs^2)
+// with dm = sum t - m0 and dj = sum t c - j0.  With the lattice's FP32-rounded weights, sum W c c
+// differs from cs^2 I by a few 1e-8 (12 * float(1/12) = 1 + 3e-8 for D2Q7), so an unprojected
+// equilibrium carries that fraction of rho u as extra momentum, and every collision adds
+// (1/tau) of it: a steady forcing that a slowly decaying flow integrates (the hex shear wave of
+// amplitude 0.01 at 1024^2, tau 0.55, decays 6e-7 per step and would decay ~8 % too slowly).  In
+// exact arithmetic dm = dj = 0 and the projection is the identity; computed, it leaves the
+// rounding error of the sums, of either sign.
+template <int Q, int D>
+__device__ __forceinline__ void conserve_moments_f32(float (&t)[Q], float m0, const float (&j0)[D],
+                                                     const LatK<Q, D>& L) {
+  float dm = -m0, dj[D];
+#pragma unroll
+  for (int a = 0; a < D; ++a) dj[a] = -j0[a];
+#pragma unroll
+  for (int k = 0; k < Q; ++k) {
+    dm += t[k];
+#pragma unroll
+    for (int a = 0; a < D; ++a) dj[a] += t[k] * L.cf[k][a];
+  }
+#pragma unroll
+  for (int k = 0; k < Q; ++k) {
+    float cj = 0.f;
+#pragma unroll
+    for (int a = 0; a < D; ++a) cj += L.cf[k][a] * dj[a];
+    t[k] -= L.wf[k] * (dm + L.inv_cs2f * cj);
+  }
+}
+
 // BGK collision of one moment in place (FP64 / generic T): rho = sum f, u = sum f c / rho
 // (no vacuum guard, as the GPU path of the reference), f += (feq - f)/tau.
 template <int Q, int D, class T>
@@ -150,7 +179,8 @@ __device__ __forceinline__ void collide_moment(T (&f)[Q], T tau, const LatK<Q, D
   for (int k = 0; k < Q; ++k) f[k] = f[k] + (feq[k] - f[k]) / tau;
 }
 
-// BGK collision in the deviation store: f_k = rho*W_k + dev_k, rho is invariant, u = sum dev c / rho.
+// BGK collision in the deviation store: f_k = rho*W_k + dev_k, rho is invariant, u = sum dev c / rho;
+// the equilibrium is projected onto the deviations' mass and momentum (conserve_moments_f32).
 template <int Q, int D>
 __device__ __forceinline__ void collide_moment_dev(float rho, float (&dev)[Q], float tau, const LatK<Q, D>& L) {
   float mom[D];
@@ -166,6 +196,10 @@ __device__ __forceinline__ void collide_moment_dev(float rho, float (&dev)[Q], f
   for (int a = 0; a < D; ++a) u[a] = mom[a] / rho;
   float deq[Q];
   eq_deviation_f32<Q, D>(rho, u, L, deq);
+  float m0 = 0.f;  // the deviations' own mass (zero up to rounding): rho itself is stored apart
+#pragma unroll
+  for (int k = 0; k < Q; ++k) m0 += dev[k];
+  conserve_moments_f32<Q, D>(deq, m0, mom, L);
   const float inv_tau = 1.0f / tau;
 #pragma unroll
   for (int k = 0; k < Q; ++k) dev[k] = dev[k] + (deq[k] - dev[k]) * inv_tau;

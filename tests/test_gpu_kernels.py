@@ -152,6 +152,27 @@ def test_lbm_shear_wave_decay_matches_analytic(precision):
     np.testing.assert_allclose(lam, lam_ref, rtol=0.02)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_lbm_shear_wave_decay_at_config_wavelength_over_1000_steps(precision):
+    """The hex shear wave at the configuration's own wavelength (1024 rows, amplitude 0.01) over its
+    1000 steps: the mode decays only ~6e-7 per step at tau 0.55, so any spurious momentum source in
+    the FP32 collision (the rounded weights' sum W c c != cs^2 I) shows in the rate.  The wave is
+    uniform along i, so 8 columns stand in for 1024.  Both stores within 1 % of nu k^2 and of each
+    other."""
+    from direbm_gb300.lbm import HexLBM
+
+    nj, ni = 1024, 8
+    taus = np.array([0.55, 0.7, 1.0])
+    lb = HexLBM(ni, nj, taus, precision=precision)
+    lb.set_f(olbm.shear_wave(ni, nj, 0.01))
+    a0 = lb.shear_amplitude()
+    steps = 1000
+    lb.step(steps)
+    lam = -np.log(lb.shear_amplitude() / a0) / steps
+    lam_ref = np.array([olbm.shear_decay_rate(t, nj) for t in taus])
+    np.testing.assert_allclose(lam, lam_ref, rtol=0.01)
+
+
 def test_bin_fields_on_device_matches_reference_golden(golden):
     """direbm/fields.py:17-41 on the device: the reference's golden binning of 200 moments."""
     from direbm_gb300.fields import bin_fields
