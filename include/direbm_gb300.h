@@ -200,10 +200,10 @@ int dbm_sim_use_graphs(dbm_sim* sim, int32_t on);
  * per (point, direction) (default 1).  Results are bit-identical either way. */
 #define DBM_OPT_SHIFTED_WINDOWS 7
 /* DBM_OPT_DENSE_STENCIL (2D, FP32 store, with the shifted windows): a tile whose cells each hold at
- * most one moment and one control point (in D2Q9 runs with dx = cell, every cell holds exactly
- * one) is staged as a dense grid and every window becomes a fixed 4 x 4 block of cells; other
- * tiles take the row-segment loops in the same launch (default 1).  Results are bit-identical
- * either way. */
+ * most two moments and two control points (in D2Q9 runs with dx = cell, almost every cell holds
+ * exactly one) is staged as a dense grid -- second items in a per-tile list of 32 -- and every
+ * window becomes a fixed 4 x 4 block of cells; other tiles take the row-segment loops in a second
+ * launch (default 1).  Results are bit-identical either way. */
 #define DBM_OPT_DENSE_STENCIL 8
 int dbm_sim_get_brick_width(dbm_sim* sim, int32_t* brick_width);
 int dbm_sim_set_option(dbm_sim* sim, int32_t option, int32_t value);
