@@ -1123,8 +1123,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=N_INST, help="first N ensemble members (profiling runs)")
     ap.add_argument("--legs", default="all",
-                    choices=["all", "main", "adjoint", "sphere", "lbm", "e2e", "accuracy", "cpu"],
-                    help="main = timed step only; adjoint / sphere / lbm / e2e / accuracy / cpu = that leg only")
+                    choices=["all", "main", "adjoint", "sphere", "lbm", "e2e", "accuracy", "cpu", "profile"],
+                    help="main = timed step only; adjoint / sphere / lbm / e2e / accuracy / cpu = that leg only; "
+                         "profile = --profile-steps graph steps, then one eager step stage by stage (for ncu)")
+    ap.add_argument("--profile-steps", type=int, default=0, help="profile leg: steps before the eager one")
     ap.add_argument("--adjoint-n", type=int, default=256, help="adjoint leg: points per side")
     ap.add_argument("--adjoint-steps", type=int, default=100, help="adjoint leg: rollout steps")
     ap.add_argument("--adjoint-every", type=int, default=10, help="adjoint leg: checkpoint interval")
@@ -1163,6 +1165,23 @@ def main():
         ib, x, f = build_ensemble(sides, taus)
         fp64, acc_ens = ensemble_accuracy_leg(sides, taus, ib, x, f)
         print(json.dumps({"fp64": fp64, "accuracy_ensemble": acc_ens, "accuracy": accuracy_leg()}), flush=True)
+        return
+    if args.legs == "profile" and args.impl == "ours":
+        # the first --instances members, 16x16 tiles without persistence (the autotuner's choice on
+        # the full ensemble), --profile-steps steps, then one step launched stage by stage
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        sides, taus = ensemble_spec(args.instances)
+        ib, x, f = build_ensemble(sides, taus)
+        sim = make_sim(sides, taus, "fp32dev", len(x))
+        sim.set_tiling(16, False)
+        sim.set_state(ib, x, f)
+        sim.step(args.profile_steps)
+        print(json.dumps({"moments": len(x), "steps_before": args.profile_steps, "stage_ms": sim.profile_step()}),
+              flush=True)
+        sim.check_status()
+        sim.close()
         return
     if args.legs == "cpu" and args.impl == "ours":
         print(json.dumps({"cpu_baseline": cpu_baseline_leg()}), flush=True)
