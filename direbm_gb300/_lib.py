@@ -90,6 +90,7 @@ _SIGS = {
     "dbm_create_control_points_f32": (ctypes.c_int, [_vp, _i64, _f32, _vp, ctypes.POINTER(_i64), _vp]),
     "dbm_refine_control_points_f32": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp, _i64, _f32, ctypes.c_int, _vp, _vp]),
     "dbm_resample_f32": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i64, _f32, _vp, ctypes.c_int, _f32, _vp, _vp, _vp]),
+    "dbm_segmented_sum_f32": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp]),
     "dbm_bin_fields_tmp_bytes": (_i64, [_i64]),
     "dbm_bin_fields_f64": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int, _vp, ctypes.c_int, _vp, ctypes.c_int, _vp, _vp,
                                           _vp, _vp, _vp]),

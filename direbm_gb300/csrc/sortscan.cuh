@@ -42,6 +42,11 @@ template <class K>
 int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t cap, const uint32_t* d_n,
                      int key_bits, void* tmp, cudaStream_t s, bool* result_in_alt);
 
+// Reduce-by-key: out[keys[i]] = sum of the values of the run of equal keys keys[i] in a key-sorted
+// array (keys < 0xffffffff), with warp-level segmented scans in a fixed order (segreduce.cu).  Keys
+// without records leave out untouched.
+int segmented_sum_f32(const uint32_t* keys, const float* vals, int64_t n, float* out, cudaStream_t s);
+
 // ---- block-level helpers shared with other kernels -------------------------------------------
 
 // Exclusive scan across a 256-thread block of one value per thread; returns the prefix and the

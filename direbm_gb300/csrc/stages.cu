@@ -101,12 +101,17 @@ struct PointIndex {
 };
 
 struct Arena {  // stream-ordered temporaries, freed together
+  static constexpr int kMax = 64;
   cudaStream_t s;
-  void* ptrs[32];
+  void* ptrs[kMax];
   int n = 0;
   explicit Arena(cudaStream_t st) : s(st) {}
   template <class T>
   int get(T** p, int64_t count) {
+    if (n >= kMax) {
+      set_last_error("internal: more than %d temporaries in one stage call", kMax);
+      return DBM_ERR_STATE;
+    }
     void* q = nullptr;
     cudaError_t e = cudaMallocAsync(&q, (size_t)std::max<int64_t>(count, 1) * sizeof(T), s);
     if (e != cudaSuccess) { set_last_error("cudaMallocAsync: %s", cudaGetErrorString(e)); return DBM_ERR_CUDA; }
@@ -226,40 +231,70 @@ __global__ void k_comp_sw(const float* __restrict__ pos_c, int64_t nc, const flo
   }
 }
 
-// Pass 2: per control point, sum (dx - d)/sw * f over its components, per direction.
+// Pass 2 as the reference's scatter (propagation.py:156-186), without its float atomics: every
+// component (m, k) with sw > 0 writes one record per control point r within dx, key r * Q + k and
+// value (dx - d)/sw * f, at offsets from a scan of its count (records in component order, control
+// points in index-walk order); the records are stable-sorted by key and each key's run is summed
+// by the warp-level segmented reduction (segreduce.cu).
+__global__ void k_scatter_count(const float* __restrict__ pos_c, int64_t nc, const float* __restrict__ cp,
+                                PointIndex cpi, const float* __restrict__ sw, float dx, uint32_t* __restrict__ cnt) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t n = 0;
+    if (sw[c] > 0.f) {
+      const float qx = pos_c[2 * c], qy = pos_c[2 * c + 1];
+      const long long cx = cell_of(qx, dx), cy = cell_of(qy, dx);
+      for (int ox = -2; ox <= 2; ++ox)
+        for (int oy = -2; oy <= 2; ++oy) {
+          uint32_t b, e;
+          if (!find_cell(cpi, pack_cell(cx + ox, cy + oy), &b, &e)) continue;
+          for (uint32_t j = b; j < e; ++j) {
+            const uint32_t r = cpi.order[j];
+            if (dist32(cp[2 * r], cp[2 * r + 1], qx, qy) <= dx) ++n;
+          }
+        }
+    }
+    cnt[c] = n;
+  }
+}
+
 template <int Q>
-__global__ void k_cp_gather(const float* __restrict__ cp, int64_t p, const float* __restrict__ pos_c,
-                            const float* __restrict__ val_c, const int32_t* __restrict__ dir_c,
-                            const float* __restrict__ sw, PointIndex ci, float dx, float eps, float* __restrict__ cpf,
-                            uint32_t* __restrict__ emask) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < p; r += (int64_t)gridDim.x * blockDim.x) {
-    const float px = cp[2 * r], py = cp[2 * r + 1];
-    const long long cx = cell_of(px, dx), cy = cell_of(py, dx);
-    CSum acc[Q];
+__global__ void k_scatter_write(const float* __restrict__ pos_c, int64_t nc, const float* __restrict__ val_c,
+                                const int32_t* __restrict__ dir_c, const float* __restrict__ cp, PointIndex cpi,
+                                const float* __restrict__ sw, float dx, const uint32_t* __restrict__ pos_of,
+                                uint32_t* __restrict__ keys, float* __restrict__ vals) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
+    const float s = sw[c];
+    if (!(s > 0.f)) continue;
+    const float qx = pos_c[2 * c], qy = pos_c[2 * c + 1];
+    const long long cx = cell_of(qx, dx), cy = cell_of(qy, dx);
+    const uint32_t k = (uint32_t)dir_c[c];
+    const float v = val_c[c];
+    uint32_t w = pos_of[c];
     for (int ox = -2; ox <= 2; ++ox)
       for (int oy = -2; oy <= 2; ++oy) {
         uint32_t b, e;
-        if (!find_cell(ci, pack_cell(cx + ox, cy + oy), &b, &e)) continue;
+        if (!find_cell(cpi, pack_cell(cx + ox, cy + oy), &b, &e)) continue;
         for (uint32_t j = b; j < e; ++j) {
-          const uint32_t c = ci.order[j];
-          const float d = dist32(px, py, pos_c[2 * c], pos_c[2 * c + 1]);
-          const float s = sw[c];
-          if (d <= dx && s > 0.f) {
-            const int k = dir_c[c];
-            const float wgt = __fdiv_rn(__fsub_rn(dx, d), s);
-#pragma unroll
-            for (int q = 0; q < Q; ++q)
-              if (q == k) acc[q].add_prod(wgt, val_c[c]);
+          const uint32_t r = cpi.order[j];
+          const float d = dist32(cp[2 * r], cp[2 * r + 1], qx, qy);
+          if (d <= dx) {
+            keys[w] = r * (uint32_t)Q + k;
+            vals[w] = __fmul_rn(__fdiv_rn(__fsub_rn(dx, d), s), v);
+            ++w;
           }
         }
       }
+  }
+}
+
+// The emptiness mask of each control point from its resampled f (before the gap fill).
+template <int Q>
+__global__ void k_cp_emask(const float* __restrict__ cpf, int64_t p, float eps, uint32_t* __restrict__ emask) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < p; r += (int64_t)gridDim.x * blockDim.x) {
     uint32_t em = 0;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const float v = acc[q].value();
-      cpf[r * Q + q] = v;
-      if (v < eps) em |= 1u << q;
-    }
+    for (int q = 0; q < Q; ++q)
+      if (cpf[r * Q + q] < eps) em |= 1u << q;
     emask[r] = em;
   }
 }
@@ -414,7 +449,40 @@ int dbm_resample_f32(const float* pos_c, const float* val_c, const int32_t* dir_
         DBM_TRY(ar.get(&ci.nu, 1));
         DBM_CUDA(cudaMemsetAsync(ci.nu, 0, 4, s));
       }
-      k_cp_gather<Q><<<grid_for(p), 256, 0, s>>>(cp, p, pos_c, val_c, dir_c, sw, ci, dx, eps, cpf, em);
+      DBM_CUDA(cudaMemsetAsync(cpf, 0, (size_t)p * Q * sizeof(float), s));
+      if (nc > 0) {
+        // the scatter: pair records, stable sort by (control point, direction), segmented sums
+        uint32_t *cnt, *pos_of, *d_total;
+        DBM_TRY(ar.get(&cnt, nc));
+        DBM_TRY(ar.get(&pos_of, nc));
+        DBM_TRY(ar.get(&d_total, 1));
+        char* stmp;
+        DBM_TRY(ar.get(&stmp, (int64_t)scan_tmp_bytes(nc)));
+        k_scatter_count<<<grid_for(nc), 256, 0, s>>>(pos_c, nc, cp, cpi, sw, dx, cnt);
+        DBM_LAUNCH_CHECK();
+        DBM_TRY(scan_exclusive_u32(cnt, pos_of, nc, nullptr, d_total, stmp, s));
+        uint32_t total = 0;  // the record count sizes the sort
+        DBM_CUDA(cudaMemcpyAsync(&total, d_total, 4, cudaMemcpyDeviceToHost, s));
+        DBM_CUDA(cudaStreamSynchronize(s));
+        if (total > 0) {
+          uint32_t *rk, *rv, *rk2, *rv2;
+          DBM_TRY(ar.get(&rk, total));
+          DBM_TRY(ar.get(&rv, total));
+          DBM_TRY(ar.get(&rk2, total));
+          DBM_TRY(ar.get(&rv2, total));
+          char* rtmp;
+          DBM_TRY(ar.get(&rtmp, (int64_t)radix_tmp_bytes(total)));
+          k_scatter_write<Q><<<grid_for(nc), 256, 0, s>>>(pos_c, nc, val_c, dir_c, cp, cpi, sw, dx, pos_of, rk,
+                                                         reinterpret_cast<float*>(rv));
+          DBM_LAUNCH_CHECK();
+          int bits = 1;
+          while (bits < 32 && ((uint64_t)1 << bits) < (uint64_t)p * Q) ++bits;
+          bool alt = false;  // the values travel as their bit patterns
+          DBM_TRY(radix_sort_pairs<uint32_t>(rk, rv, rk2, rv2, total, nullptr, bits, rtmp, s, &alt));
+          DBM_TRY(segmented_sum_f32(alt ? rk2 : rk, reinterpret_cast<const float*>(alt ? rv2 : rv), total, cpf, s));
+        }
+      }
+      k_cp_emask<Q><<<grid_for(p), 256, 0, s>>>(cpf, p, eps, em);
       DBM_LAUNCH_CHECK();
       k_cp_fill<Q><<<grid_for(p), 256, 0, s>>>(cp, p, cpi, em, f_rest, dx, cpf, out_pos, out_f);
       DBM_LAUNCH_CHECK();

@@ -94,11 +94,19 @@ int dbm_create_control_points_f32(const float* d_pos_c, int64_t nc, float cs, fl
 int dbm_refine_control_points_f32(const float* d_cp_pos, int64_t p, const float* d_pos_c, const float* d_val_c,
                                   const int32_t* d_dir_c, int64_t nc, float dx, int kappa_hard,
                                   float* d_new_pos, void* stream);
-/* resample: direbm/warp/propagation.py:156-246 (scatter + gap fill + emit), as a deterministic
- * two-pass gather instead of float atomics.  out_f is (P, Q). */
+/* resample: direbm/warp/propagation.py:156-246 (scatter + gap fill + emit).  The scatter keeps the
+ * reference's form -- each component sends (dx - d)/sw * f to every control point within dx --
+ * with its float atomics (propagation.py:186) replaced by pair records, a stable sort by (control
+ * point, direction) and dbm_segmented_sum_f32, so the result is deterministic.  Synchronises the
+ * stream once (the record count sizes the sort).  out_f is (P, Q). */
 int dbm_resample_f32(const float* d_pos_c, const float* d_val_c, const int32_t* d_dir_c, int64_t nc,
                      const float* d_cp_pos, int64_t p, float dx, const float* d_f_rest, int lattice,
                      float eps, float* d_out_pos, float* d_out_f, void* stream);
+/* Reduce-by-key: d_out[k] = sum of d_vals over the run of key k in the key-sorted d_keys (n records,
+ * keys < 0xffffffff); keys without records leave d_out untouched.  Warp-level segmented scans in a
+ * fixed order, no float atomics: the deterministic replacement for wp.atomic_add in the reference's
+ * scatter (direbm/warp/propagation.py:186), which has no entry point of its own. */
+int dbm_segmented_sum_f32(const uint32_t* d_keys, const float* d_vals, int64_t n, float* d_out, void* stream);
 
 /* ---- hexagonal D2Q7 lattice Boltzmann ------------------------------------------------------
  * Replaces direbm/warp/lbm.py:24-105 (_lbm_collide + _lbm_stream, GpuHexLBM.step) with one
