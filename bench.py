@@ -491,31 +491,46 @@ def lbm_leg(steps=1000, warmup=5):
     return res
 
 
-def e2e_leg(sim, ib, x, f, steps=8, warmup=1):
+def in_cell_order(ib, x):
+    """Whether the moments are ordered by instance, then cell (row by row), with cells of size CELL:
+    the order set_state(presorted=True) takes without sorting.  The ensemble's jittered grids,
+    generated row by row one point per cell, are."""
+    c = np.floor(np.asarray(x) / CELL).astype(np.int64)
+    k = (np.asarray(ib, dtype=np.int64) << 42) + (c[:, 1] << 21) + c[:, 0]
+    return bool(len(k) < 2 or (np.diff(k) >= 0).all())
+
+
+def e2e_leg(sim, ib, x, f, steps=8, warmup=1, io="f32"):
     """Same metric through the public API with host buffers: every step copies the state from pinned
     host memory, loads it, steps once, exports it and copies it back.  One untimed step first, so
-    that the output tensors' first allocation is not timed.  The host<->device copies move ~1.4 GB
-    each way per step; their rate depends on the host side (NUMA placement, other jobs), so the
-    line also reports the copy bandwidth seen on a separate timed copy."""
+    that the output tensors' first allocation is not timed.  io = "f32": positions and f cross the
+    host boundary as float32, the element type of the reference's GPU simulator arrays
+    (92 -> 48 bytes per moment each way; the device state is the same as from their float64
+    widening); io = "f64": as float64.  The host<->device copies move 0.7 / 1.4 GB each way per
+    step; their rate depends on the host side (NUMA placement, other jobs), so the line also
+    reports the copy bandwidth seen on a separate timed copy."""
     import torch
 
     M = len(x)
+    hdt, tdt = (np.float32, torch.float32) if io == "f32" else (np.float64, torch.float64)
+    row = 4 + (2 + 9) * np.dtype(hdt).itemsize  # bytes per moment: instance, position, f
+    presorted = in_cell_order(ib, x)  # the load then skips its sort (the device checks the order)
     h_inst = torch.from_numpy(ib.astype(np.int32)).pin_memory()
-    h_pos = torch.from_numpy(np.ascontiguousarray(x)).pin_memory()
-    h_f = torch.from_numpy(np.ascontiguousarray(f)).pin_memory()
+    h_pos = torch.from_numpy(np.ascontiguousarray(x, dtype=hdt)).pin_memory()
+    h_f = torch.from_numpy(np.ascontiguousarray(f, dtype=hdt)).pin_memory()
     d_inst = torch.empty(M, dtype=torch.int32, device="cuda")
-    d_pos = torch.empty((M, 2), dtype=torch.float64, device="cuda")
-    d_f = torch.empty((M, 9), dtype=torch.float64, device="cuda")
+    d_pos = torch.empty((M, 2), dtype=tdt, device="cuda")
+    d_f = torch.empty((M, 9), dtype=tdt, device="cuda")
     o_inst = torch.empty(M, dtype=torch.int32).pin_memory()
-    o_pos = torch.empty((M, 2), dtype=torch.float64).pin_memory()
-    o_f = torch.empty((M, 9), dtype=torch.float64).pin_memory()
+    o_pos = torch.empty((M, 2), dtype=tdt).pin_memory()
+    o_f = torch.empty((M, 9), dtype=tdt).pin_memory()
     def one_step():
         d_inst.copy_(h_inst, non_blocking=True)
         d_pos.copy_(h_pos, non_blocking=True)
         d_f.copy_(h_f, non_blocking=True)
-        sim.set_state(d_inst, d_pos, d_f)
+        sim.set_state(d_inst, d_pos, d_f, presorted=presorted)
         sim.step(1)
-        gi, gp, gf = sim.state()
+        gi, gp, gf = sim.state(dtype=tdt)
         m2 = gi.shape[0]
         o_inst[:m2].copy_(gi, non_blocking=True)
         o_pos[:m2].copy_(gp, non_blocking=True)
@@ -543,22 +558,22 @@ def e2e_leg(sim, ib, x, f, steps=8, warmup=1):
         d_inst.copy_(h_inst, non_blocking=True)
         d_pos.copy_(h_pos, non_blocking=True)
         d_f.copy_(h_f, non_blocking=True)
-        sim.set_state(d_inst, d_pos, d_f)
+        sim.set_state(d_inst, d_pos, d_f, presorted=presorted)
         points += M
         sim.step(1)
-        gi, gp, gf = sim.state()
+        gi, gp, gf = sim.state(dtype=tdt)
         m2 = gi.shape[0]
         o_inst[:m2].copy_(gi, non_blocking=True)
         o_pos[:m2].copy_(gp, non_blocking=True)
         o_f[:m2].copy_(gf, non_blocking=True)
-        h2d += M * (4 + 16 + 72)
-        d2h += m2 * (4 + 16 + 72)
+        h2d += M * row
+        d2h += m2 * row
     e1.record()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     ms = e0.elapsed_time(e1)
     serial = {"value": points / (ms * 1e-3), "ms_per_step": ms / steps, "wall_s": wall}
-    piped = _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, (o_inst, o_pos, o_f, m2))
+    piped = _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, (o_inst, o_pos, o_f, m2), presorted, tdt, row)
     serial["h2d_bytes_per_step"], serial["d2h_bytes_per_step"] = int(h2d // steps), int(d2h // steps)
     return {"value": piped["value"], "unit": "point-steps/s", "h2d_bytes_per_step": int(piped["h2d_bytes_per_step"]),
             "d2h_bytes_per_step": int(piped["d2h_bytes_per_step"]), "ms_per_step": piped["ms_per_step"],
@@ -566,13 +581,24 @@ def e2e_leg(sim, ib, x, f, steps=8, warmup=1):
             "steps": steps, "warmup": warmup, "copy_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs}, "serial": serial,
             "result_equals_serial": piped["result_equals_serial"],
             "repetitions_ms_per_step": piped["repetitions_ms_per_step"], "statistic": "median of 3 repetitions",
-            "path": "Simulation.set_state(check=False)/step/state_into (C ABI dbm_sim_*) with pinned host buffers and "
+            "presorted": presorted, "io": io,
+            "path": "Simulation.set_state(check=False, presorted=<input in cell order>)/step/state_into (C ABI "
+                    "dbm_sim_*) with pinned host buffers and "
                     "no host wait inside a step; each step's host-to-device copy on its own stream overlaps the "
                     "previous step, each step's device-to-host copy of the whole output buffers (capacity rows) on a "
                     "third stream overlaps the next (two buffer slots each way); status and count read after the run"}
 
 
-def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out):
+def e2e_both(sim, ib, x, f):
+    """The e2e leg through float32 host buffers (the reported figure) with the float64 one beside it."""
+    e2e = e2e_leg(sim, ib, x, f, io="f32")
+    e64 = e2e_leg(sim, ib, x, f, io="f64")
+    e2e["f64_io"] = {k: e64[k] for k in ("value", "ms_per_step", "h2d_bytes_per_step", "d2h_bytes_per_step",
+                                         "copy_gbs", "repetitions_ms_per_step", "result_equals_serial")}
+    return e2e
+
+
+def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out, presorted, tdt, row):
     """The e2e steps with the copies overlapped: inputs of step i+1 go up while step i computes, and
     results of step i come down while step i+1 computes.  Every step still copies its whole input
     from pinned host memory and its whole result back, inside the timed region."""
@@ -582,12 +608,12 @@ def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out):
     main = torch.cuda.current_stream()
     s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
     cap = max(M, sim.ncells)
-    din = [(torch.empty(M, dtype=torch.int32, device=dev), torch.empty((M, 2), dtype=torch.float64, device=dev),
-            torch.empty((M, 9), dtype=torch.float64, device=dev)) for _ in range(2)]
-    dout = [(torch.empty(cap, dtype=torch.int32, device=dev), torch.empty((cap, 2), dtype=torch.float64, device=dev),
-             torch.empty((cap, 9), dtype=torch.float64, device=dev)) for _ in range(2)]
-    hout = [(torch.empty(cap, dtype=torch.int32).pin_memory(), torch.empty((cap, 2), dtype=torch.float64).pin_memory(),
-             torch.empty((cap, 9), dtype=torch.float64).pin_memory()) for _ in range(2)]
+    din = [(torch.empty(M, dtype=torch.int32, device=dev), torch.empty((M, 2), dtype=tdt, device=dev),
+            torch.empty((M, 9), dtype=tdt, device=dev)) for _ in range(2)]
+    dout = [(torch.empty(cap, dtype=torch.int32, device=dev), torch.empty((cap, 2), dtype=tdt, device=dev),
+             torch.empty((cap, 9), dtype=tdt, device=dev)) for _ in range(2)]
+    hout = [(torch.empty(cap, dtype=torch.int32).pin_memory(), torch.empty((cap, 2), dtype=tdt).pin_memory(),
+             torch.empty((cap, 9), dtype=tdt).pin_memory()) for _ in range(2)]
     ev = {n: [torch.cuda.Event() for _ in range(2)] for n in ("in", "used", "out", "down")}
 
     def upload(slot):
@@ -609,7 +635,7 @@ def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out):
             if i + 1 < n:
                 upload(1 - sl)
             main.wait_event(ev["in"][sl])
-            sim.set_state(*din[sl], check=False)  # the bad-input bit is checked after the run
+            sim.set_state(*din[sl], check=False, presorted=presorted)  # status checked after the run
             ev["used"][sl].record(main)
             sim.step(1)
             main.wait_event(ev["down"][sl])  # this slot's previous result has left the device
@@ -648,7 +674,7 @@ def _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, serial_out):
             and torch.equal(hf[:n], of[:n]))
     return {"value": M * steps / (ms * 1e-3), "ms_per_step": ms / steps, "wall_s": wall,
             "result_equals_serial": bool(same), "repetitions_ms_per_step": [r[0] / steps for r in reps],
-            "h2d_bytes_per_step": M * (4 + 16 + 72), "d2h_bytes_per_step": cap * (4 + 16 + 72)}
+            "h2d_bytes_per_step": M * row, "d2h_bytes_per_step": cap * row}
 
 
 def adjoint_leg(n=256, steps=100, every=10, tau=0.6, precisions=("fp32dev", "fp64")):
@@ -1085,7 +1111,7 @@ def run_ours(args):
         sim.close()
         return
     run100 = full_run_leg(sim, ib, x, f)
-    e2e = e2e_leg(sim, ib, x, f)
+    e2e = e2e_both(sim, ib, x, f)
     sim.close()
 
     # FP64 store on the same workload, and FP32DEV vs FP64 after the same steps on the whole ensemble
@@ -1154,7 +1180,7 @@ def main():
         ib, x, f = build_ensemble(sides, taus)
         sim = make_sim(sides, taus, "fp32dev", len(x))
         sim.set_state(ib, x, f)
-        print(json.dumps({"e2e": e2e_leg(sim, ib, x, f)}), flush=True)
+        print(json.dumps({"e2e": e2e_both(sim, ib, x, f)}), flush=True)
         sim.close()
         return
     if args.legs == "accuracy" and args.impl == "ours":

@@ -100,6 +100,9 @@ _SIGS = {
     "dbm_sim_create": (ctypes.c_int, [ctypes.POINTER(SimDesc), ctypes.POINTER(InstanceDesc), _i32, ctypes.POINTER(_vp)]),
     "dbm_sim_destroy": (ctypes.c_int, [_vp]),
     "dbm_sim_set_state": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, _vp]),
+    "dbm_sim_set_state_sorted": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, _vp]),
+    "dbm_sim_set_state_f32": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, ctypes.c_int32, _vp]),
+    "dbm_sim_get_state_f32": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "dbm_sim_step": (ctypes.c_int, [_vp, _i32, _vp]),
     "dbm_sim_step_partial": (ctypes.c_int, [_vp, _i32, _vp]),
     "dbm_sim_profile_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_float), _vp]),

@@ -889,12 +889,22 @@ __global__ void __launch_bounds__(256) k_emit(const __grid_constant__ Args<Q, D,
 
 // ---- import / export ------------------------------------------------------------------------
 
-template <int Q, int D, class P>
+// T: the caller's element type of positions and f (double, or float for the float32 interface).
+// GB300 issues FP64 arithmetic (and double<->float conversions) at a small fraction of the FP32
+// rate, so the float32 interface runs in float arithmetic where that gives the same bits or, for
+// the FP32DEV split of f, a stated rounding:
+//   - positions, cell a power of two (cell_f != 0): s = x * (1/cell) and its fraction are exact
+//     in float, so cell and offset are bitwise those of the float64 path;
+//   - FP32DEV f: rho = compensated float sum of f (TwoSum per term), dev_k = f_k - rho W_k with
+//     rho wf_k split exactly by fmaf and W_k = wf_k + wlo_k (double-float); the float64 path
+//     rounds the same residual from a float64 sum, so the two agree to about an ulp of dev.
+template <int Q, int D, class P, class T>
 __global__ void __launch_bounds__(256) k_import_keys(const __grid_constant__ Args<Q, D, P> A, const int32_t* __restrict__ inst_of,
-                                                     const double* __restrict__ pos, int64_t m, double cell,
+                                                     const T* __restrict__ pos, int64_t m, double cell, float inv_cell_f,
                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                                      typename P::real* __restrict__ toff) {
   using real = typename P::real;
+  constexpr bool kFloatIn = std::is_same<T, float>::value;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
     const int b = inst_of[i];
     uint32_t key = 0xffffffffu;
@@ -904,15 +914,35 @@ __global__ void __launch_bounds__(256) k_import_keys(const __grid_constant__ Arg
       bool ok = true;
 #pragma unroll
       for (int a = 0; a < D; ++a) {
-        const double s = pos[i * D + a] / cell;
-        const double fl = floor(s);
-        real o = (real)(s - fl);
+        real o;
+        long long fl_i;
+        if (kFloatIn && std::is_same<real, float>::value && inv_cell_f != 0.f) {
+          // exact: power-of-two scaling; a float minus its floor is the correctly rounded
+          // difference, which the float64 path also rounds once (the difference of two floats
+          // within 2^29 of each other is exact in double, and below that both round to 1)
+          const float sf = __fmul_rn((float)pos[i * D + a], inv_cell_f);
+          const float flf = floorf(sf);
+          o = (real)__fsub_rn(sf, flf);
+          fl_i = (long long)flf;
+        } else {
+          const double s = (double)pos[i * D + a] / cell;
+          const double fl = floor(s);
+          o = (real)(s - fl);
+          fl_i = (long long)fl;
+        }
         const real one_below = std::is_same<real, float>::value ? (real)0.99999994f : (real)0.99999999999999989;
         if (o > one_below) o = one_below;
         toff[(int64_t)a * m + i] = o;
-        long long x = (long long)fl - I.origin[a];
+        long long x = fl_i - I.origin[a];
         const long long n = I.dims[a];
-        if (I.periodic) x = ((x % n) + n) % n; else ok &= (x >= 0 && x < n);
+        if (I.periodic) {
+          if (x < 0 || x >= n) {
+            x %= n;
+            if (x < 0) x += n;
+          }
+        } else {
+          ok &= (x >= 0 && x < n);
+        }
         c[a] = (int)x;
       }
       uint32_t g;
@@ -924,8 +954,14 @@ __global__ void __launch_bounds__(256) k_import_keys(const __grid_constant__ Arg
   }
 }
 
-template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_import_gather(const __grid_constant__ Args<Q, D, P> A, const double* __restrict__ fin, int64_t m,
+// A load given in cell order: flag ST_BAD_INPUT where a key is smaller than its predecessor.
+__global__ void k_check_sorted(const uint32_t* __restrict__ keys, int64_t m, uint32_t* __restrict__ status) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + 1; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    if (keys[i] < keys[i - 1]) atomicOr(status, ST_BAD_INPUT);
+}
+
+template <int Q, int D, class P, class T>
+__global__ void __launch_bounds__(256) k_import_gather(const __grid_constant__ Args<Q, D, P> A, const T* __restrict__ fin, int64_t m,
                                                        const uint32_t* __restrict__ keys,
                                                        const uint32_t* __restrict__ vals,
                                                        const typename P::real* __restrict__ toff) {
@@ -936,22 +972,48 @@ __global__ void __launch_bounds__(256) k_import_gather(const __grid_constant__ A
     for (int a = 0; a < D; ++a) A.a.off[(int64_t)a * A.mcap + j] = toff[(int64_t)a * m + i];
     if constexpr (std::is_same<P, PF64>::value) {
 #pragma unroll
-      for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + j] = fin[(int64_t)i * Q + k];
+      for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + j] = (double)fin[(int64_t)i * Q + k];
+    } else if constexpr (std::is_same<T, float>::value) {
+      float fk[Q];
+#pragma unroll
+      for (int k = 0; k < Q; ++k) fk[k] = fin[(int64_t)i * Q + k];
+      float s = fk[0], err = 0.f;
+#pragma unroll
+      for (int k = 1; k < Q; ++k) {
+        const DF t = df_two_sum(s, fk[k]);
+        s = t.hi;
+        err = __fadd_rn(err, t.lo);
+      }
+      const float rho = __fadd_rn(s, err);
+      A.a.rho[j] = rho;
+#pragma unroll
+      for (int k = 0; k < Q; ++k) {
+        const float p = __fmul_rn(rho, A.L.wf[k]);
+        const float e = __fmaf_rn(rho, A.L.wf[k], -p);  // rho wf_k = p + e exactly
+        const DF d = df_two_sum(fk[k], -p);  // f_k - p exactly
+        A.a.dev[(int64_t)k * A.mcap + j] = __fadd_rn(d.hi, __fsub_rn(d.lo, __fmaf_rn(rho, A.L.wlo[k], e)));
+      }
     } else {
       double rho = 0;
 #pragma unroll
-      for (int k = 0; k < Q; ++k) rho += fin[(int64_t)i * Q + k];
+      for (int k = 0; k < Q; ++k) rho += (double)fin[(int64_t)i * Q + k];
       A.a.rho[j] = (float)rho;
 #pragma unroll
-      for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + j] = (float)(fin[(int64_t)i * Q + k] - rho * A.L.w[k]);
+      for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + j] = (float)((double)fin[(int64_t)i * Q + k] - rho * A.L.w[k]);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *A.a.count = (uint32_t)m;
 }
 
-template <int Q, int D, class P>
-__global__ void __launch_bounds__(256) k_export(const __grid_constant__ Args<Q, D, P> A, double cell, int32_t* __restrict__ inst_out,
-                                                double* __restrict__ pos, double* __restrict__ fout) {
+// T = float (the float32 interface) in float arithmetic: positions, cell a power of two (cell_f != 0)
+// and |cell index| < 2^24, are fl32(index + offset) * cell, the same bits as rounding the float64
+// position; FP32DEV f_k = rho W_k + dev_k as double-float (rho wf_k split by fmaf), rounded once to
+// float, within an ulp of the rounded float64 value.
+template <int Q, int D, class P, class T>
+__global__ void __launch_bounds__(256) k_export(const __grid_constant__ Args<Q, D, P> A, double cell, float cell_f,
+                                                int32_t* __restrict__ inst_out, T* __restrict__ pos,
+                                                T* __restrict__ fout) {
+  constexpr bool kFloatOut = std::is_same<T, float>::value;
   const uint32_t M = *A.a.count;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
     const uint32_t g = A.a.cell[j];
@@ -962,16 +1024,32 @@ __global__ void __launch_bounds__(256) k_export(const __grid_constant__ Args<Q, 
     if (inst_out) inst_out[j] = b;
     if (pos) {
 #pragma unroll
-      for (int a = 0; a < D; ++a)
-        pos[(int64_t)j * D + a] = ((double)(I.origin[a] + c[a]) + (double)A.a.off[(int64_t)a * A.mcap + j]) * cell;
+      for (int a = 0; a < D; ++a) {
+        const long long ci = (long long)I.origin[a] + c[a];
+        if (kFloatOut && std::is_same<typename P::real, float>::value && cell_f != 0.f && ci > -(1ll << 24) &&
+            ci < (1ll << 24))
+          pos[(int64_t)j * D + a] =
+              (T)__fmul_rn(__fadd_rn((float)ci, (float)A.a.off[(int64_t)a * A.mcap + j]), cell_f);
+        else
+          pos[(int64_t)j * D + a] = (T)(((double)ci + (double)A.a.off[(int64_t)a * A.mcap + j]) * cell);
+      }
     }
     if (fout) {
 #pragma unroll
       for (int k = 0; k < Q; ++k) {
-        double v;
-        if constexpr (std::is_same<P, PF64>::value) v = A.a.f64[(int64_t)k * A.mcap + j];
-        else v = (double)A.a.rho[j] * A.L.w[k] + (double)A.a.dev[(int64_t)k * A.mcap + j];
-        fout[(int64_t)j * Q + k] = v;
+        if constexpr (std::is_same<P, PF64>::value) {
+          fout[(int64_t)j * Q + k] = (T)A.a.f64[(int64_t)k * A.mcap + j];
+        } else if constexpr (kFloatOut) {
+          // f_k = rho wf_k + dev_k + rho wlo_k: the large pair summed exactly (they cancel where f_k is
+          // small), the small terms added to its error before the one rounding
+          const float r = A.a.rho[j];
+          const float p = __fmul_rn(r, A.L.wf[k]);
+          const float e = __fmaf_rn(r, A.L.wf[k], -p);
+          const DF h = df_two_sum(p, A.a.dev[(int64_t)k * A.mcap + j]);
+          fout[(int64_t)j * Q + k] = __fadd_rn(h.hi, __fadd_rn(h.lo, __fmaf_rn(r, A.L.wlo[k], e)));
+        } else {
+          fout[(int64_t)j * Q + k] = (T)((double)A.a.rho[j] * A.L.w[k] + (double)A.a.dev[(int64_t)k * A.mcap + j]);
+        }
       }
     }
   }
@@ -1063,6 +1141,7 @@ struct SimImpl : SimBase {
   uint32_t *k_in = nullptr, *v_in = nullptr, *k_alt = nullptr, *v_alt = nullptr;
   bool sorted_in_alt = false;
   bool import_in_alt = false;  // where set_state's sort left the import order
+  bool pow2_cell = false;      // cell a power of two: the float32 interface scales positions exactly in float
   InstK* dinst = nullptr;
   void* sort_tmp = nullptr;
   void* compact_tmp = nullptr;
@@ -1140,6 +1219,10 @@ struct SimImpl : SimBase {
 
   int init(const dbm_sim_desc& d, const dbm_instance_desc* in, int n) {
     desc = d;
+    {
+      int ex = 0;
+      pow2_cell = std::frexp(d.cell, &ex) == 0.5 && ex > -60 && ex < 60;
+    }
     const LatHost& LH = *lat_host(d.lattice);
     const double R = d.r_res / d.cell;
     double cmax = 0;
@@ -1576,23 +1659,34 @@ struct SimImpl : SimBase {
     args.write_trace = trace_on;
   }
 
-  int import_sorted_states(int64_t m, cudaStream_t s, const int32_t* inst_of, const double* pos, const double* fin) {
+  template <class T>
+  int import_sorted_states(int64_t m, cudaStream_t s, const int32_t* inst_of, const T* pos, const T* fin,
+                           bool presorted) {
     bind();
     // the unsorted offsets [D][m] live in the weight scratch sw ([Q][mcap], Q > D, idle outside a
     // step): an allocation here (and its cudaFree) would wait for every stream of the device,
     // including a caller's copies that overlap the load
     real* toff = args.sw;
     const unsigned grid = std::min<unsigned>(div_up(std::max<int64_t>(m, 1), 256), (unsigned)sm_count() * 8);
-    k_import_keys<Q, D, P><<<grid, 256, 0, s>>>(args, inst_of, pos, m, desc.cell, k_in, v_in, toff);
+    k_import_keys<Q, D, P, T><<<grid, 256, 0, s>>>(args, inst_of, pos, m, desc.cell, pow2_cell ? (float)(1.0 / desc.cell) : 0.f,
+                                                  k_in, v_in, toff);
     DBM_LAUNCH_CHECK();
     bool alt = false;
-    // valid keys are < ncells < 2^key_bits; the marker 0xffffffff of a moment outside its box is
-    // all ones in those bits too, so it still sorts after every valid key
-    DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, m, nullptr, key_bits, sort_tmp, s, &alt));
+    if (presorted) {
+      // given in cell order: the keys (and the identity order k_import_keys wrote) stay as they are
+      if (m > 1) {
+        k_check_sorted<<<grid, 256, 0, s>>>(k_in, m, args.status);
+        DBM_LAUNCH_CHECK();
+      }
+    } else {
+      // valid keys are < ncells < 2^key_bits; the marker 0xffffffff of a moment outside its box is
+      // all ones in those bits too, so it still sorts after every valid key
+      DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, m, nullptr, key_bits, sort_tmp, s, &alt));
+    }
     import_in_alt = alt;
     const uint32_t* ks = alt ? k_alt : k_in;
     const uint32_t* vs = alt ? v_alt : v_in;
-    k_import_gather<Q, D, P><<<grid, 256, 0, s>>>(args, fin, m, ks, vs, toff);
+    k_import_gather<Q, D, P, T><<<grid, 256, 0, s>>>(args, fin, m, ks, vs, toff);
     DBM_LAUNCH_CHECK();
     // count of valid keys = m (invalid ones sort last with key 0xffffffff and raise ST_BAD_INPUT)
     DBM_CUDA(cudaMemcpyAsync(args.d_P, args.a.count, 4, cudaMemcpyDeviceToDevice, s));
@@ -1601,12 +1695,15 @@ struct SimImpl : SimBase {
     return DBM_OK;
   }
 
-  int set_state(const int32_t* inst_of, const double* pos, const double* fin, int64_t m, cudaStream_t s) override {
+  int load(const int32_t* inst_of, const void* pos, const void* fin, int64_t m, int flags, cudaStream_t s) override {
     if (m < 0 || m > mcap) { set_last_error("set_state: %lld moments exceed capacity %lld", (long long)m, (long long)mcap); return DBM_ERR_CAPACITY; }
     if (m > 0 && (!inst_of || !pos || !fin)) { set_last_error("set_state: null input"); return DBM_ERR_INVALID; }
     cur = 0;
     ++version;
-    return import_sorted_states(m, s, inst_of, pos, fin);
+    const bool presorted = (flags & kLoadPresorted) != 0;
+    if (flags & kLoadF32)
+      return import_sorted_states<float>(m, s, inst_of, (const float*)pos, (const float*)fin, presorted);
+    return import_sorted_states<double>(m, s, inst_of, (const double*)pos, (const double*)fin, presorted);
   }
 
   // Launch the stages of one step (a = st[cur] -> b = st[cur^1]) on stream s, up to `upto`.
@@ -2036,10 +2133,14 @@ struct SimImpl : SimBase {
     return DBM_OK;
   }
 
-  int get_state(int32_t* inst_out, double* pos, double* fout, cudaStream_t s) override {
+  int get_state(int32_t* inst_out, void* pos, void* fout, int f32, cudaStream_t s) override {
     bind();
     const unsigned grid = std::min<unsigned>(div_up(mcap, 256), (unsigned)sm_count() * 8);
-    k_export<Q, D, P><<<grid, 256, 0, s>>>(args, desc.cell, inst_out, pos, fout);
+    if (f32)
+      k_export<Q, D, P, float><<<grid, 256, 0, s>>>(args, desc.cell, pow2_cell ? (float)desc.cell : 0.f, inst_out,
+                                                    (float*)pos, (float*)fout);
+    else
+      k_export<Q, D, P, double><<<grid, 256, 0, s>>>(args, desc.cell, 0.f, inst_out, (double*)pos, (double*)fout);
     DBM_LAUNCH_CHECK();
     return DBM_OK;
   }
@@ -2178,7 +2279,18 @@ int dbm_sim_destroy(dbm_sim* s) {
 
 int dbm_sim_set_state(dbm_sim* s, const int32_t* inst, const double* pos, const double* f, int64_t m, void* stream) {
   SIM_CHECK(s);
-  return s->impl->set_state(inst, pos, f, m, (cudaStream_t)stream);
+  return s->impl->load(inst, pos, f, m, 0, (cudaStream_t)stream);
+}
+int dbm_sim_set_state_sorted(dbm_sim* s, const int32_t* inst, const double* pos, const double* f, int64_t m,
+                             void* stream) {
+  SIM_CHECK(s);
+  return s->impl->load(inst, pos, f, m, SimBase::kLoadPresorted, (cudaStream_t)stream);
+}
+int dbm_sim_set_state_f32(dbm_sim* s, const int32_t* inst, const float* pos, const float* f, int64_t m,
+                          int32_t presorted, void* stream) {
+  SIM_CHECK(s);
+  const int flags = SimBase::kLoadF32 | (presorted ? SimBase::kLoadPresorted : 0);
+  return s->impl->load(inst, pos, f, m, flags, (cudaStream_t)stream);
 }
 int dbm_sim_step(dbm_sim* s, int32_t steps, void* stream) {
   SIM_CHECK(s);
@@ -2200,7 +2312,11 @@ int dbm_sim_count(dbm_sim* s, int64_t* m, void* stream) {
 }
 int dbm_sim_get_state(dbm_sim* s, int32_t* inst, double* pos, double* f, void* stream) {
   SIM_CHECK(s);
-  return s->impl->get_state(inst, pos, f, (cudaStream_t)stream);
+  return s->impl->get_state(inst, pos, f, 0, (cudaStream_t)stream);
+}
+int dbm_sim_get_state_f32(dbm_sim* s, int32_t* inst, float* pos, float* f, void* stream) {
+  SIM_CHECK(s);
+  return s->impl->get_state(inst, pos, f, 1, (cudaStream_t)stream);
 }
 int dbm_sim_status(dbm_sim* s, uint32_t* flags, int32_t clear, void* stream) {
   SIM_CHECK(s);

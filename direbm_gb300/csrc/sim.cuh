@@ -319,13 +319,16 @@ struct StepHook {
 // Type-erased simulator (SimImpl<Q, D, P> in sim.cu).
 struct SimBase {
   virtual ~SimBase() = default;
-  virtual int set_state(const int32_t*, const double*, const double*, int64_t, cudaStream_t) = 0;
+  // Load m moments: positions (m, D) and f (m, Q) as double, or float with kLoadF32; kLoadPresorted
+  // declares them in cell order (checked on the device) and skips the sort.
+  enum { kLoadF32 = 1, kLoadPresorted = 2 };
+  virtual int load(const int32_t* inst_of, const void* pos, const void* f, int64_t m, int flags, cudaStream_t) = 0;
   virtual int step(int, cudaStream_t) = 0;
   virtual int step_partial(int, cudaStream_t) = 0;
   virtual int step_hooked(StepHook*, cudaStream_t) = 0;
   virtual int profile_step(float*, cudaStream_t) = 0;
   virtual int count(int64_t*, cudaStream_t) = 0;
-  virtual int get_state(int32_t*, double*, double*, cudaStream_t) = 0;
+  virtual int get_state(int32_t*, void* pos, void* f, int f32, cudaStream_t) = 0;
   virtual int status(uint32_t*, int, cudaStream_t) = 0;
   virtual int conservation(double*, cudaStream_t) = 0;
   virtual int trace(int, void*, int64_t, int64_t*, cudaStream_t) = 0;

@@ -48,6 +48,10 @@ def _require_cuda(device=None) -> torch.device:
     return dev
 
 
+def _is_f32(a) -> bool:
+    return getattr(a, "dtype", None) in (torch.float32, np.float32)
+
+
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
@@ -141,14 +145,20 @@ class Simulation:
         return int(self.lib.dbm_sim_device_bytes(self._h))
 
     # ---- state ----------------------------------------------------------------------------------
-    def set_state(self, inst, pos, f, check: bool = True):
+    def set_state(self, inst, pos, f, check: bool = True, presorted: bool = False):
         """Load moments: instance index (M,), world positions (M, D), distributions (M, Q).  With
         ``check=False`` the call does not wait for the load to finish: a moment outside its box then
         leaves the bad-input bit in ``status()`` (``check_status()`` raises on it) instead of raising
-        here, so a caller that pipelines loads and steps keeps the device busy."""
+        here, so a caller that pipelines loads and steps keeps the device busy.  ``presorted=True``
+        declares the moments in cell order (by instance, then cell: the order ``state()`` returns)
+        and skips the sort; the state is the same, and a moment out of order sets the bad-input
+        bit.  Positions and f both float32 (the reference GPU simulator's arrays) go to the device
+        as they are and are widened there; anything else is converted to float64."""
         dev = self.device
-        pos = torch.as_tensor(pos, dtype=torch.float64, device=dev).contiguous()
-        f = torch.as_tensor(f, dtype=torch.float64, device=dev).contiguous()
+        f32 = _is_f32(pos) and _is_f32(f)
+        dt = torch.float32 if f32 else torch.float64
+        pos = torch.as_tensor(pos, dtype=dt, device=dev).contiguous()
+        f = torch.as_tensor(f, dtype=dt, device=dev).contiguous()
         M = int(pos.shape[0])
         if inst is None:
             inst = torch.zeros(M, dtype=torch.int32, device=dev)
@@ -156,11 +166,18 @@ class Simulation:
         if pos.shape != (M, self.lattice.D) or f.shape != (M, self.lattice.Q) or inst.shape != (M,):
             raise ValueError("set_state: expected inst (M,), pos (M, D), f (M, Q)")
         with torch.cuda.device(dev):
-            _lib.check(self.lib.dbm_sim_set_state(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), M, _stream()),
-                       "dbm_sim_set_state")
+            if f32:
+                name = "dbm_sim_set_state_f32"
+                rc = self.lib.dbm_sim_set_state_f32(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), M,
+                                                    1 if presorted else 0, _stream())
+            else:
+                name = "dbm_sim_set_state_sorted" if presorted else "dbm_sim_set_state"
+                rc = getattr(self.lib, name)(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), M, _stream())
+            _lib.check(rc, name)
             st = self.status(clear=True) if check else 0
         if st & _lib.ST_BAD_INPUT:
-            raise _lib.DbmError("set_state: a moment lies outside its instance box")
+            raise _lib.DbmError("set_state: a moment lies outside its instance box"
+                                + (" or out of cell order" if presorted else ""))
         self.iteration = 0
 
     def step(self, n: int = 1):
@@ -190,53 +207,54 @@ class Simulation:
             _lib.check(self.lib.dbm_sim_count(self._h, ctypes.byref(m), _stream()), "dbm_sim_count")
         return int(m.value)
 
-    def state(self, out=None):
-        """(instance (M,) int32, positions (M, D) fp64, f (M, Q) fp64) as CUDA tensors.  With
-        ``out`` = (inst, pos, f), contiguous CUDA tensors of at least M rows, the state is written
-        into their first M rows and those views are returned (no allocation)."""
+    def state(self, out=None, dtype=torch.float64):
+        """(instance (M,) int32, positions (M, D), f (M, Q)) as CUDA tensors of ``dtype`` (float64,
+        or float32: the state rounded once on the device).  With ``out`` = (inst, pos, f),
+        contiguous CUDA tensors of at least M rows (pos and f both float64 or both float32), the
+        state is written into their first M rows and those views are returned (no allocation)."""
         M = self.count()
         dev = self.device
-        D, Q = self.lattice.D, self.lattice.Q
         if out is not None:
-            oi, op, of = out
-            ok = (oi.is_cuda and op.is_cuda and of.is_cuda and oi.dtype == torch.int32 and op.dtype == torch.float64
-                  and of.dtype == torch.float64 and oi.is_contiguous() and op.is_contiguous() and of.is_contiguous()
-                  and oi.shape[0] >= M and op.shape[0] >= M and of.shape[0] >= M and tuple(op.shape[1:]) == (D,)
-                  and tuple(of.shape[1:]) == (Q,))
-            if not ok:
-                raise ValueError(f"state(out=...): need contiguous CUDA int32 (>= {M},), fp64 (>= {M}, {D}), "
-                                 f"fp64 (>= {M}, {Q})")
-            inst, pos, f = oi[:M], op[:M], of[:M]
+            self._check_out(out, M, "state(out=...)")
+            inst, pos, f = (o[:M] for o in out)
         else:
+            if dtype not in (torch.float64, torch.float32):
+                raise ValueError("state: dtype must be torch.float64 or torch.float32")
+            D, Q = self.lattice.D, self.lattice.Q
             inst = torch.empty(M, dtype=torch.int32, device=dev)
-            pos = torch.empty((M, D), dtype=torch.float64, device=dev)
-            f = torch.empty((M, Q), dtype=torch.float64, device=dev)
+            pos = torch.empty((M, D), dtype=dtype, device=dev)
+            f = torch.empty((M, Q), dtype=dtype, device=dev)
         if M:
-            with torch.cuda.device(dev):
-                _lib.check(self.lib.dbm_sim_get_state(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), _stream()),
-                           "dbm_sim_get_state")
+            self._export(inst, pos, f)
         return inst, pos, f
+
+    def _check_out(self, out, rows, what):
+        oi, op, of = out
+        D, Q = self.lattice.D, self.lattice.Q
+        ok = (oi.is_cuda and op.is_cuda and of.is_cuda and oi.dtype == torch.int32 and op.dtype == of.dtype
+              and op.dtype in (torch.float64, torch.float32) and oi.is_contiguous() and op.is_contiguous()
+              and of.is_contiguous() and oi.shape[0] >= rows and op.shape[0] >= rows and of.shape[0] >= rows
+              and tuple(op.shape[1:]) == (D,) and tuple(of.shape[1:]) == (Q,))
+        if not ok:
+            raise ValueError(f"{what}: need contiguous CUDA int32 (>= {rows},), and fp64 or fp32 (>= {rows}, {D}) "
+                             f"and (>= {rows}, {Q}) of one dtype")
+
+    def _export(self, inst, pos, f):
+        name = "dbm_sim_get_state_f32" if pos.dtype == torch.float32 else "dbm_sim_get_state"
+        with torch.cuda.device(self.device):
+            _lib.check(getattr(self.lib, name)(self._h, inst.data_ptr(), pos.data_ptr(), f.data_ptr(), _stream()), name)
 
     def state_numpy(self):
         inst, pos, f = self.state()
         return inst.cpu().numpy(), pos.cpu().numpy(), f.cpu().numpy()
 
     def state_into(self, out):
-        """Write the state into ``out`` = (inst, pos, f): contiguous CUDA int32 (>= capacity,),
-        fp64 (>= capacity, D) and fp64 (>= capacity, Q) buffers.  Unlike ``state()`` this does not
-        wait for the step to finish (it needs no row count on the host): once the caller's stream
-        reaches this point, rows [0, count()) hold the state, in its sorted order."""
-        oi, op, of = out
-        D, Q, C = self.lattice.D, self.lattice.Q, self.capacity
-        ok = (oi.is_cuda and op.is_cuda and of.is_cuda and oi.dtype == torch.int32 and op.dtype == torch.float64
-              and of.dtype == torch.float64 and oi.is_contiguous() and op.is_contiguous() and of.is_contiguous()
-              and oi.shape[0] >= C and op.shape[0] >= C and of.shape[0] >= C and tuple(op.shape[1:]) == (D,)
-              and tuple(of.shape[1:]) == (Q,))
-        if not ok:
-            raise ValueError(f"state_into: need contiguous CUDA int32 (>= {C},), fp64 (>= {C}, {D}), fp64 (>= {C}, {Q})")
-        with torch.cuda.device(self.device):
-            _lib.check(self.lib.dbm_sim_get_state(self._h, oi.data_ptr(), op.data_ptr(), of.data_ptr(), _stream()),
-                       "dbm_sim_get_state")
+        """Write the state into ``out`` = (inst, pos, f): contiguous CUDA int32 (>= capacity,) and
+        fp64 or fp32 (>= capacity, D) and (>= capacity, Q) buffers.  Unlike ``state()`` this does
+        not wait for the step to finish (it needs no row count on the host): once the caller's
+        stream reaches this point, rows [0, count()) hold the state, in its sorted order."""
+        self._check_out(out, self.capacity, "state_into")
+        self._export(*out)
         return out
 
     def status(self, clear: bool = False) -> int:

@@ -76,8 +76,12 @@ class GpuSimulator:
         self._since_plan = 0
         self._sim = None
         self._box = None
-        pos = np.asarray(pos_m, dtype=np.float64).reshape(-1, self.lattice.D)
-        f = np.asarray(f_m, dtype=np.float64).reshape(-1, self.lattice.Q)
+        # float32 inputs (the reference's element type) go to the device as they are and are widened
+        # there; anything else as float64
+        pos, f = np.asarray(pos_m), np.asarray(f_m)
+        dt = np.float32 if pos.dtype == np.float32 and f.dtype == np.float32 else np.float64
+        pos = np.ascontiguousarray(pos, dtype=dt).reshape(-1, self.lattice.D)
+        f = np.ascontiguousarray(f, dtype=dt).reshape(-1, self.lattice.Q)
         if self.fixed_box:
             lo = np.floor(np.asarray(box[0], dtype=np.float64) / self.cell).astype(int)
             hi = np.ceil(np.asarray(box[1], dtype=np.float64) / self.cell).astype(int)
@@ -110,7 +114,7 @@ class GpuSimulator:
             lo = np.zeros(self.lattice.D)
             hi = np.zeros(self.lattice.D)
         else:
-            lo, hi = pos.min(axis=0), pos.max(axis=0)
+            lo, hi = pos.min(axis=0).astype(np.float64), pos.max(axis=0).astype(np.float64)
         g = self._growth()
         span = max(float((hi - lo).max()), 1.0)
         margin = g + 0.25 * span  # slack so that steady growth does not re-plan every time
@@ -153,22 +157,22 @@ class GpuSimulator:
         self._sim.check_status()
 
     def moments(self):
-        """(positions (N, D) FP32, f (N, Q) FP32) as numpy."""
+        """(positions (N, D) FP32, f (N, Q) FP32) as numpy, rounded to float32 on the device."""
         self._sim.check_status()
-        _, pos, f = self._sim.state_numpy()
-        return pos.astype(np.float32), f.astype(np.float32)
+        _, pos, f = self._sim.state(dtype=torch.float32)
+        return pos.cpu().numpy(), f.cpu().numpy()
 
     @property
     def pos_m(self):
         self._sim.check_status()
-        _, pos, _ = self._sim.state()
-        return DeviceArray(pos.float())
+        _, pos, _ = self._sim.state(dtype=torch.float32)
+        return DeviceArray(pos)
 
     @property
     def f_m(self):
         self._sim.check_status()
-        _, _, f = self._sim.state()
-        return DeviceArray(f.float())
+        _, _, f = self._sim.state(dtype=torch.float32)
+        return DeviceArray(f)
 
     @property
     def simulation(self) -> Simulation:

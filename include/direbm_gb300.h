@@ -166,15 +166,29 @@ int dbm_sim_destroy(dbm_sim* sim);
 /* Load moments: d_inst (m) instance of each moment, d_pos (m, D) world positions, d_f (m, Q). */
 int dbm_sim_set_state(dbm_sim* sim, const int32_t* d_inst, const double* d_pos, const double* d_f, int64_t m,
                       void* stream);
+/* dbm_sim_set_state for moments already in cell order (the order dbm_sim_get_state writes them:
+ * by instance, then cell, ties in any order): the load skips the sort.  A moment out of cell order
+ * sets status bit 8, as a moment outside its box does.  Same state as dbm_sim_set_state. */
+int dbm_sim_set_state_sorted(dbm_sim* sim, const int32_t* d_inst, const double* d_pos, const double* d_f,
+                             int64_t m, void* stream);
+/* dbm_sim_set_state with float32 positions and f, the element type of the reference's GPU simulator
+ * (reference: direbm/warp/simulator.py:40-41, pos_m as wp.vec2 and f_m as wp.float32); values are
+ * widened to double on the device.  presorted != 0 as dbm_sim_set_state_sorted. */
+int dbm_sim_set_state_f32(dbm_sim* sim, const int32_t* d_inst, const float* d_pos, const float* d_f, int64_t m,
+                          int32_t presorted, void* stream);
 /* Advance `steps` steps (replays a captured CUDA graph when graphs are enabled). */
 int dbm_sim_step(dbm_sim* sim, int32_t steps, void* stream);
 /* Synchronises `stream` and returns the current moment count. */
 int dbm_sim_count(dbm_sim* sim, int64_t* m, void* stream);
 /* Export the state (outputs sized by dbm_sim_count), world positions and f in FP64. */
 int dbm_sim_get_state(dbm_sim* sim, int32_t* d_inst, double* d_pos, double* d_f, void* stream);
+/* dbm_sim_get_state rounded to float32 (reference: direbm/warp/simulator.py:75-77, moments() reads
+ * pos_m and f_m back as float32). */
+int dbm_sim_get_state_f32(dbm_sim* sim, int32_t* d_inst, float* d_pos, float* d_f, void* stream);
 /* Synchronises and returns the device status word; clears it when clear != 0.  Bits: 1 a point
  * left a bounded box, 2 a capacity was exceeded, 4 a non-finite value, 8 set_state input outside
- * its box, 16 an internal consistency check failed. */
+ * its box (or, for dbm_sim_set_state_sorted, out of cell order), 16 an internal consistency check
+ * failed. */
 int dbm_sim_status(dbm_sim* sim, uint32_t* flags, int32_t clear, void* stream);
 /* Per-instance FP64 totals: mass, then momentum per axis -> d_out (n_inst, 1 + D). */
 int dbm_sim_conservation(dbm_sim* sim, double* d_out, void* stream);

@@ -502,3 +502,115 @@ def test_dense_stencil_bitwise_equal(name):
         assert sim.status() == 0
     for a, b in zip(outs[0], outs[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+@pytest.mark.parametrize("lattice", ["D2Q9", "D3Q19"])
+def test_presorted_load_equals_sorted_load(lattice, precision):
+    """set_state(presorted=True) of moments in cell order (exported states: one as loaded, whose
+    cells hold two moments, and one after six steps) loads the same state as the sorting load, and
+    the runs from the two loads stay bitwise equal; moments out of cell order raise the bad-input
+    error."""
+    from direbm_gb300._lib import DbmError
+
+    if lattice == "D2Q9":
+        insts = [dict(dims=(24, 20), periodic=True, tau=0.6), dict(dims=(16, 16), periodic=True, tau=0.8)]
+        parts = [periodic_tg(24, "D2Q9", seed=3), periodic_tg(16, "D2Q9", seed=4)]
+        parts[0] = (np.mod(parts[0][0], [24, 20]), parts[0][1])
+    else:
+        insts = [dict(dims=(10, 10, 10), periodic=True, tau=0.6)]
+        parts = [periodic_tg(10, "D3Q19", seed=7, u0=0.02)]
+    ib = np.concatenate([np.full(len(p[0]), b) for b, p in enumerate(parts)])
+    x = np.concatenate([p[0] for p in parts])
+    f = np.concatenate([p[1] for p in parts])
+    perm = np.random.default_rng(0).permutation(len(x))
+    cap = 2 * len(x)
+    sim = _sim(lattice, insts, precision, 1.0, 1.5, 1.0, cap=cap)
+    sim.set_state(ib[perm], x[perm], f[perm])
+    fresh = sim.state_numpy()  # as loaded: the rows folded by the 24 x 20 box share cells (ties)
+    sim.step(6)
+    for state in (fresh, sim.state_numpy()):
+        cells = np.concatenate([state[0][:, None], np.floor(state[1]).astype(np.int64)], 1)
+        if lattice == "D2Q9" and state is fresh:
+            assert len(np.unique(cells, axis=0)) < len(cells)
+        runs = []
+        for presorted in (False, True):
+            s2 = _sim(lattice, insts, precision, 1.0, 1.5, 1.0, cap=cap)
+            s2.set_state(*state, presorted=presorted)
+            loaded = s2.state_numpy()
+            s2.step(4)
+            runs.append((loaded, s2.state_numpy()))
+            assert s2.status() == 0
+        for a, b in zip(runs[0][0] + runs[0][1], runs[1][0] + runs[1][1]):
+            np.testing.assert_array_equal(a, b)
+    s3 = _sim(lattice, insts, precision, 1.0, 1.5, 1.0, cap=cap)
+    with pytest.raises(DbmError, match="cell order"):
+        s3.set_state(ib[perm], x[perm], f[perm], presorted=True)
+
+
+def _ulps32(a, b):
+    """Largest |a - b| in units of the float32 spacing at max(|a|, |b|)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    sp = np.spacing(np.maximum(np.abs(a), np.abs(b)).astype(np.float32)).astype(np.float64)
+    return float((np.abs(a - b) / sp).max()) if a.size else 0.0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
+def test_float32_interface(precision):
+    """The float32 load and export (float arithmetic on the device):
+      - cell and offset of every moment are bitwise those of the float64 load of the widened
+        values (power-of-two cell), and so are the exported float32 positions;
+      - FP64 store: the whole state, the runs from it and the float32 export are bitwise the
+        float64 ones (rounded);
+      - FP32DEV store: f reconstructs the input to within 1e-7 relative and agrees with the float64
+        load's to one float32 ulp; the float32 export of f is within one ulp of the float64
+        export rounded;
+      - the exported float32 state is in cell order and reloads without a sort to the state a
+        sorting load gives."""
+    import torch
+
+    insts = [dict(dims=(24, 24), periodic=True, tau=0.6), dict(dims=(16, 20), periodic=True, tau=0.8)]
+    parts = [periodic_tg(24, "D2Q9", seed=11), periodic_tg(16, "D2Q9", seed=12)]
+    parts[1] = (np.mod(parts[1][0], [16, 20]), parts[1][1])
+    ib = np.concatenate([np.full(len(p[0]), b) for b, p in enumerate(parts)])
+    x32 = np.concatenate([p[0] for p in parts]).astype(np.float32)
+    f32 = np.concatenate([p[1] for p in parts]).astype(np.float32)
+    cap = 2 * len(x32)
+    sims, loaded = [], []
+    for args in ((ib, x32.astype(np.float64), f32.astype(np.float64)), (ib, x32, f32)):
+        sim = _sim("D2Q9", insts, precision, 1.0, 1.5, 1.0, cap=cap)
+        sim.set_state(*args)
+        loaded.append(sim.state_numpy())
+        sims.append(sim)
+    (i64, p64, g64), (i32, p32, g32) = loaded
+    np.testing.assert_array_equal(i32, i64)
+    np.testing.assert_array_equal(p32, p64)
+    cells = np.floor(x32).astype(np.int64)
+    order = np.lexsort((cells[:, 0], cells[:, 1], ib))  # one moment per cell here: the load's order
+    if precision == "fp64":
+        np.testing.assert_array_equal(g32, g64)
+    else:
+        assert _rel(g32, f32[order].astype(np.float64)) < 1e-7
+        assert _ulps32(g32, g64) <= 1.0
+    for sim in sims:
+        sim.step(3)
+    outs = [sim.state_numpy() for sim in sims]
+    if precision == "fp64":
+        for a, b in zip(*outs):
+            np.testing.assert_array_equal(a, b)
+    for sim, (si, sp, sf) in zip(sims, outs):
+        e_i, e_p, e_f = (t.cpu().numpy() for t in sim.state(dtype=torch.float32))
+        np.testing.assert_array_equal(e_i, si)
+        np.testing.assert_array_equal(e_p, sp.astype(np.float32))
+        if precision == "fp64":
+            np.testing.assert_array_equal(e_f, sf.astype(np.float32))
+        else:
+            assert _ulps32(e_f, sf) <= 1.0
+        reload = []
+        for presorted in (False, True):
+            s2 = _sim("D2Q9", insts, precision, 1.0, 1.5, 1.0, cap=cap)
+            s2.set_state(e_i, e_p, e_f, presorted=presorted)
+            reload.append(s2.state_numpy())
+        for a, b in zip(*reload):
+            np.testing.assert_array_equal(a, b)

@@ -243,3 +243,27 @@ def test_gpu_lbm_conserves_mass():
     for _ in range(15):
         gpu.step()
     assert np.isclose(float(gpu.f.numpy().sum()), m0, rtol=1e-3)
+
+
+def test_moments_are_the_state_rounded_to_float32():
+    """moments() / pos_m / f_m read the state back as float32 computed on the device: positions
+    are the float64 ones rounded once, f within one float32 ulp of the float64 f rounded (the
+    FP32DEV store's rho W + dev summed in double-float)."""
+    from direbm_gb300.lattices import D2Q7, equilibrium
+    from direbm_gb300.warp import GpuSimulator
+
+    rng = np.random.default_rng(5)
+    pos = (np.stack(np.meshgrid(np.arange(14) + 0.5, np.arange(14) + 0.5), -1).reshape(-1, 2)
+           + rng.uniform(-0.2, 0.2, (196, 2))).astype(np.float32)
+    f = equilibrium(np.ones(196), 0.02 * rng.standard_normal((196, 2)), D2Q7).astype(np.float32)
+    sim = GpuSimulator(pos, f, tau=0.7, dx=1.0)
+    for _ in range(3):
+        sim.step()
+    p32, f32 = sim.moments()
+    _, p64, f64 = sim.simulation.state_numpy()
+    assert p32.dtype == np.float32 and f32.dtype == np.float32
+    np.testing.assert_array_equal(p32, p64.astype(np.float32))
+    spacing = np.spacing(np.abs(f64).astype(np.float32)).astype(np.float64)
+    assert (np.abs(f32.astype(np.float64) - f64) <= spacing).all()
+    np.testing.assert_array_equal(sim.pos_m.numpy(), p32)
+    np.testing.assert_array_equal(sim.f_m.numpy(), f32)
