@@ -547,8 +547,8 @@ def e2e_leg(sim, ib, x, f, steps=8, warmup=1, io="f32"):
     o_f.copy_(d_f, non_blocking=True)
     c2.record()
     torch.cuda.synchronize()
-    h2d_gbs = h_f.numel() * 8 / (c0.elapsed_time(c1) * 1e-3) / 1e9
-    d2h_gbs = h_f.numel() * 8 / (c1.elapsed_time(c2) * 1e-3) / 1e9
+    h2d_gbs = h_f.numel() * h_f.element_size() / (c0.elapsed_time(c1) * 1e-3) / 1e9
+    d2h_gbs = h_f.numel() * h_f.element_size() / (c1.elapsed_time(c2) * 1e-3) / 1e9
     t0 = time.perf_counter()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()

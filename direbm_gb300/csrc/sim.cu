@@ -898,66 +898,109 @@ __global__ void __launch_bounds__(256) k_emit(const __grid_constant__ Args<Q, D,
 //   - FP32DEV f: rho = compensated float sum of f (TwoSum per term), dev_k = f_k - rho W_k with
 //     rho wf_k split exactly by fmaf and W_k = wf_k + wlo_k (double-float); the float64 path
 //     rounds the same residual from a float64 sum, so the two agree to about an ulp of dev.
+// Cell key (0xffffffff when the moment lies outside its box, with ST_BAD_INPUT raised) and
+// in-cell offsets of input moment i.
+template <int Q, int D, class P, class T>
+__device__ __forceinline__ uint32_t import_key(const Args<Q, D, P>& A, const int32_t* __restrict__ inst_of,
+                                               const T* __restrict__ pos, int64_t i, double cell, float inv_cell_f,
+                                               typename P::real (&o)[D]) {
+  using real = typename P::real;
+  constexpr bool kFloatIn = std::is_same<T, float>::value;
+  const int b = inst_of[i];
+  uint32_t key = 0xffffffffu;
+#pragma unroll
+  for (int a = 0; a < D; ++a) o[a] = 0;
+  if (b >= 0 && b < A.n_inst) {
+    const InstK I = A.inst[b];
+    int c[3] = {0, 0, 0};
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      real oa;
+      long long fl_i;
+      if (kFloatIn && std::is_same<real, float>::value && inv_cell_f != 0.f) {
+        // exact: power-of-two scaling; a float minus its floor is the correctly rounded
+        // difference, which the float64 path also rounds once (the difference of two floats
+        // within 2^29 of each other is exact in double, and below that both round to 1)
+        const float sf = __fmul_rn((float)pos[i * D + a], inv_cell_f);
+        const float flf = floorf(sf);
+        oa = (real)__fsub_rn(sf, flf);
+        fl_i = (long long)flf;
+      } else {
+        const double sd = (double)pos[i * D + a] / cell;
+        const double fl = floor(sd);
+        oa = (real)(sd - fl);
+        fl_i = (long long)fl;
+      }
+      const real one_below = std::is_same<real, float>::value ? (real)0.99999994f : (real)0.99999999999999989;
+      o[a] = oa > one_below ? one_below : oa;
+      long long x = fl_i - I.origin[a];
+      const long long n = I.dims[a];
+      if (I.periodic) {
+        if (x < 0 || x >= n) {
+          x %= n;
+          if (x < 0) x += n;
+        }
+      } else {
+        ok &= (x >= 0 && x < n);
+      }
+      c[a] = (int)x;
+    }
+    uint32_t g;
+    if (ok && cell_at<D>(I, c[0], c[1], c[2], &g)) key = g;
+  }
+  if (key == 0xffffffffu) atomicOr(A.status, ST_BAD_INPUT);
+  return key;
+}
+
+// State slot j <- distributions of input moment i (FP64: f; FP32DEV: rho and dev).
+template <int Q, int D, class P, class T>
+__device__ __forceinline__ void import_f(const Args<Q, D, P>& A, const T* __restrict__ fin, int64_t i, int64_t j) {
+  if constexpr (std::is_same<P, PF64>::value) {
+#pragma unroll
+    for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + j] = (double)fin[i * Q + k];
+  } else if constexpr (std::is_same<T, float>::value) {
+    float fk[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) fk[k] = fin[i * Q + k];
+    float s = fk[0], err = 0.f;
+#pragma unroll
+    for (int k = 1; k < Q; ++k) {
+      const DF t = df_two_sum(s, fk[k]);
+      s = t.hi;
+      err = __fadd_rn(err, t.lo);
+    }
+    const float rho = __fadd_rn(s, err);
+    A.a.rho[j] = rho;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      const float p = __fmul_rn(rho, A.L.wf[k]);
+      const float e = __fmaf_rn(rho, A.L.wf[k], -p);  // rho wf_k = p + e exactly
+      const DF d = df_two_sum(fk[k], -p);             // f_k - p exactly
+      A.a.dev[(int64_t)k * A.mcap + j] = __fadd_rn(d.hi, __fsub_rn(d.lo, __fmaf_rn(rho, A.L.wlo[k], e)));
+    }
+  } else {
+    double rho = 0;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) rho += (double)fin[i * Q + k];
+    A.a.rho[j] = (float)rho;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + j] = (float)((double)fin[i * Q + k] - rho * A.L.w[k]);
+  }
+}
+
 template <int Q, int D, class P, class T>
 __global__ void __launch_bounds__(256) k_import_keys(const __grid_constant__ Args<Q, D, P> A, const int32_t* __restrict__ inst_of,
                                                      const T* __restrict__ pos, int64_t m, double cell, float inv_cell_f,
                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                                      typename P::real* __restrict__ toff) {
-  using real = typename P::real;
-  constexpr bool kFloatIn = std::is_same<T, float>::value;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-    const int b = inst_of[i];
-    uint32_t key = 0xffffffffu;
-    if (b >= 0 && b < A.n_inst) {
-      const InstK I = A.inst[b];
-      int c[3] = {0, 0, 0};
-      bool ok = true;
-#pragma unroll
-      for (int a = 0; a < D; ++a) {
-        real o;
-        long long fl_i;
-        if (kFloatIn && std::is_same<real, float>::value && inv_cell_f != 0.f) {
-          // exact: power-of-two scaling; a float minus its floor is the correctly rounded
-          // difference, which the float64 path also rounds once (the difference of two floats
-          // within 2^29 of each other is exact in double, and below that both round to 1)
-          const float sf = __fmul_rn((float)pos[i * D + a], inv_cell_f);
-          const float flf = floorf(sf);
-          o = (real)__fsub_rn(sf, flf);
-          fl_i = (long long)flf;
-        } else {
-          const double s = (double)pos[i * D + a] / cell;
-          const double fl = floor(s);
-          o = (real)(s - fl);
-          fl_i = (long long)fl;
-        }
-        const real one_below = std::is_same<real, float>::value ? (real)0.99999994f : (real)0.99999999999999989;
-        if (o > one_below) o = one_below;
-        toff[(int64_t)a * m + i] = o;
-        long long x = fl_i - I.origin[a];
-        const long long n = I.dims[a];
-        if (I.periodic) {
-          if (x < 0 || x >= n) {
-            x %= n;
-            if (x < 0) x += n;
-          }
-        } else {
-          ok &= (x >= 0 && x < n);
-        }
-        c[a] = (int)x;
-      }
-      uint32_t g;
-      if (ok && cell_at<D>(I, c[0], c[1], c[2], &g)) key = g;
-    }
-    if (key == 0xffffffffu) atomicOr(A.status, ST_BAD_INPUT);
-    keys[i] = key;
+    typename P::real o[D];
+    keys[i] = import_key<Q, D, P, T>(A, inst_of, pos, i, cell, inv_cell_f, o);
     vals[i] = (uint32_t)i;
+#pragma unroll
+    for (int a = 0; a < D; ++a) toff[(int64_t)a * m + i] = o[a];
   }
-}
-
-// A load given in cell order: flag ST_BAD_INPUT where a key is smaller than its predecessor.
-__global__ void k_check_sorted(const uint32_t* __restrict__ keys, int64_t m, uint32_t* __restrict__ status) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + 1; i < m; i += (int64_t)gridDim.x * blockDim.x)
-    if (keys[i] < keys[i - 1]) atomicOr(status, ST_BAD_INPUT);
 }
 
 template <int Q, int D, class P, class T>
@@ -970,88 +1013,130 @@ __global__ void __launch_bounds__(256) k_import_gather(const __grid_constant__ A
     A.a.cell[j] = keys[j];
 #pragma unroll
     for (int a = 0; a < D; ++a) A.a.off[(int64_t)a * A.mcap + j] = toff[(int64_t)a * m + i];
-    if constexpr (std::is_same<P, PF64>::value) {
-#pragma unroll
-      for (int k = 0; k < Q; ++k) A.a.f64[(int64_t)k * A.mcap + j] = (double)fin[(int64_t)i * Q + k];
-    } else if constexpr (std::is_same<T, float>::value) {
-      float fk[Q];
-#pragma unroll
-      for (int k = 0; k < Q; ++k) fk[k] = fin[(int64_t)i * Q + k];
-      float s = fk[0], err = 0.f;
-#pragma unroll
-      for (int k = 1; k < Q; ++k) {
-        const DF t = df_two_sum(s, fk[k]);
-        s = t.hi;
-        err = __fadd_rn(err, t.lo);
-      }
-      const float rho = __fadd_rn(s, err);
-      A.a.rho[j] = rho;
-#pragma unroll
-      for (int k = 0; k < Q; ++k) {
-        const float p = __fmul_rn(rho, A.L.wf[k]);
-        const float e = __fmaf_rn(rho, A.L.wf[k], -p);  // rho wf_k = p + e exactly
-        const DF d = df_two_sum(fk[k], -p);  // f_k - p exactly
-        A.a.dev[(int64_t)k * A.mcap + j] = __fadd_rn(d.hi, __fsub_rn(d.lo, __fmaf_rn(rho, A.L.wlo[k], e)));
-      }
-    } else {
-      double rho = 0;
-#pragma unroll
-      for (int k = 0; k < Q; ++k) rho += (double)fin[(int64_t)i * Q + k];
-      A.a.rho[j] = (float)rho;
-#pragma unroll
-      for (int k = 0; k < Q; ++k) A.a.dev[(int64_t)k * A.mcap + j] = (float)((double)fin[(int64_t)i * Q + k] - rho * A.L.w[k]);
-    }
+    import_f<Q, D, P, T>(A, fin, i, j);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *A.a.count = (uint32_t)m;
+}
+
+// A load given in cell order, in one pass: key, offsets and f of moment j go straight to state
+// slot j (order[j] = j records the identity import order); k_check_sorted then checks the order.
+template <int Q, int D, class P, class T>
+__global__ void __launch_bounds__(256) k_import_presorted(const __grid_constant__ Args<Q, D, P> A,
+                                                          const int32_t* __restrict__ inst_of,
+                                                          const T* __restrict__ pos, const T* __restrict__ fin,
+                                                          int64_t m, double cell, float inv_cell_f,
+                                                          uint32_t* __restrict__ order) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    typename P::real o[D];
+    A.a.cell[j] = import_key<Q, D, P, T>(A, inst_of, pos, j, cell, inv_cell_f, o);
+    order[j] = (uint32_t)j;
+#pragma unroll
+    for (int a = 0; a < D; ++a) A.a.off[(int64_t)a * A.mcap + j] = o[a];
+    import_f<Q, D, P, T>(A, fin, j, j);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *A.a.count = (uint32_t)m;
+}
+
+// ST_BAD_INPUT where a key is smaller than its predecessor (a presorted load out of cell order).
+__global__ void k_check_sorted(const uint32_t* __restrict__ keys, int64_t m, uint32_t* __restrict__ status) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x + 1; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    if (keys[i] < keys[i - 1]) atomicOr(status, ST_BAD_INPUT);
 }
 
 // T = float (the float32 interface) in float arithmetic: positions, cell a power of two (cell_f != 0)
 // and |cell index| < 2^24, are fl32(index + offset) * cell, the same bits as rounding the float64
 // position; FP32DEV f_k = rho W_k + dev_k as double-float (rho wf_k split by fmaf), rounded once to
 // float, within an ulp of the rounded float64 value.
+// Tiles of kExportTile consecutive moments: every load of a moment is issued before the instance
+// search that needs its cell, one search per tile bounds the instances of the whole tile (cells are
+// sorted, so the first and last moment bound the rest), and the AoS rows (positions (D), f (Q)) are
+// staged in shared memory and stored as contiguous, coalesced runs.
+constexpr int kExportTile = 256;
+
 template <int Q, int D, class P, class T>
-__global__ void __launch_bounds__(256) k_export(const __grid_constant__ Args<Q, D, P> A, double cell, float cell_f,
-                                                int32_t* __restrict__ inst_out, T* __restrict__ pos,
-                                                T* __restrict__ fout) {
+__global__ void __launch_bounds__(kExportTile) k_export(const __grid_constant__ Args<Q, D, P> A, double cell, float cell_f,
+                                                        int32_t* __restrict__ inst_out, T* __restrict__ pos,
+                                                        T* __restrict__ fout) {
+  using real = typename P::real;
   constexpr bool kFloatOut = std::is_same<T, float>::value;
+  constexpr bool kDev = !std::is_same<P, PF64>::value;
+  __shared__ T s_pos[kExportTile * D];
+  __shared__ T s_f[kExportTile * Q];
+  __shared__ int s_b[2];
   const uint32_t M = *A.a.count;
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < M; j += gridDim.x * blockDim.x) {
-    const uint32_t g = A.a.cell[j];
-    const int b = find_instance(A.inst_base, A.n_inst, g);
-    const InstK I = A.inst[b];
-    int c[3];
-    decode_cell<D>(I, g, c);
-    if (inst_out) inst_out[j] = b;
-    if (pos) {
+  const int t = threadIdx.x;
+  for (uint32_t j0 = blockIdx.x * kExportTile; j0 < M; j0 += gridDim.x * kExportTile) {
+    const int n = (int)min((uint32_t)kExportTile, M - j0);
+    const uint32_t j = j0 + t;
+    const bool act = t < n;
+    uint32_t g = 0;
+    real o[D];
+    float rho = 0.f;
+    real fv[Q];  // dev (FP32DEV) or f (FP64)
+    if (act) {
+      g = A.a.cell[j];
+#pragma unroll
+      for (int a = 0; a < D; ++a) o[a] = A.a.off[(int64_t)a * A.mcap + j];
+      if constexpr (kDev) {
+        rho = A.a.rho[j];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) fv[k] = A.a.dev[(int64_t)k * A.mcap + j];
+      } else {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) fv[k] = A.a.f64[(int64_t)k * A.mcap + j];
+      }
+    }
+    if (t == 0) s_b[0] = find_instance(A.inst_base, A.n_inst, g);
+    if (t == n - 1) s_b[1] = find_instance(A.inst_base, A.n_inst, g);
+    __syncthreads();
+    if (act) {
+      int b = s_b[0];
+      if (s_b[1] != b) {  // the tile spans instances: search between the two
+        int lo = s_b[0], hi = s_b[1] + 1;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (__ldg(A.inst_base + mid) <= g) lo = mid; else hi = mid;
+        }
+        b = lo;
+      }
+      const InstK I = A.inst[b];
+      int c[3];
+      decode_cell<D>(I, g, c);
+      if (inst_out) inst_out[j] = b;
 #pragma unroll
       for (int a = 0; a < D; ++a) {
         const long long ci = (long long)I.origin[a] + c[a];
-        if (kFloatOut && std::is_same<typename P::real, float>::value && cell_f != 0.f && ci > -(1ll << 24) &&
-            ci < (1ll << 24))
-          pos[(int64_t)j * D + a] =
-              (T)__fmul_rn(__fadd_rn((float)ci, (float)A.a.off[(int64_t)a * A.mcap + j]), cell_f);
+        T v;
+        if (kFloatOut && std::is_same<real, float>::value && cell_f != 0.f && ci > -(1ll << 24) && ci < (1ll << 24))
+          v = (T)__fmul_rn(__fadd_rn((float)ci, (float)o[a]), cell_f);
         else
-          pos[(int64_t)j * D + a] = (T)(((double)ci + (double)A.a.off[(int64_t)a * A.mcap + j]) * cell);
+          v = (T)(((double)ci + (double)o[a]) * cell);
+        s_pos[t * D + a] = v;
       }
-    }
-    if (fout) {
 #pragma unroll
       for (int k = 0; k < Q; ++k) {
-        if constexpr (std::is_same<P, PF64>::value) {
-          fout[(int64_t)j * Q + k] = (T)A.a.f64[(int64_t)k * A.mcap + j];
+        T v;
+        if constexpr (!kDev) {
+          v = (T)fv[k];
         } else if constexpr (kFloatOut) {
           // f_k = rho wf_k + dev_k + rho wlo_k: the large pair summed exactly (they cancel where f_k is
           // small), the small terms added to its error before the one rounding
-          const float r = A.a.rho[j];
-          const float p = __fmul_rn(r, A.L.wf[k]);
-          const float e = __fmaf_rn(r, A.L.wf[k], -p);
-          const DF h = df_two_sum(p, A.a.dev[(int64_t)k * A.mcap + j]);
-          fout[(int64_t)j * Q + k] = __fadd_rn(h.hi, __fadd_rn(h.lo, __fmaf_rn(r, A.L.wlo[k], e)));
+          const float p = __fmul_rn(rho, A.L.wf[k]);
+          const float e = __fmaf_rn(rho, A.L.wf[k], -p);
+          const DF h = df_two_sum(p, (float)fv[k]);
+          v = __fadd_rn(h.hi, __fadd_rn(h.lo, __fmaf_rn(rho, A.L.wlo[k], e)));
         } else {
-          fout[(int64_t)j * Q + k] = (T)((double)A.a.rho[j] * A.L.w[k] + (double)A.a.dev[(int64_t)k * A.mcap + j]);
+          v = (T)((double)rho * A.L.w[k] + (double)fv[k]);
         }
+        s_f[t * Q + k] = v;
       }
     }
+    __syncthreads();
+    if (pos)
+      for (int e = t; e < n * D; e += kExportTile) pos[(int64_t)j0 * D + e] = s_pos[e];
+    if (fout)
+      for (int e = t; e < n * Q; e += kExportTile) fout[(int64_t)j0 * Q + e] = s_f[e];
+    __syncthreads();  // s_b, s_pos and s_f are rewritten by the next tile
   }
 }
 
@@ -1663,31 +1748,33 @@ struct SimImpl : SimBase {
   int import_sorted_states(int64_t m, cudaStream_t s, const int32_t* inst_of, const T* pos, const T* fin,
                            bool presorted) {
     bind();
-    // the unsorted offsets [D][m] live in the weight scratch sw ([Q][mcap], Q > D, idle outside a
-    // step): an allocation here (and its cudaFree) would wait for every stream of the device,
-    // including a caller's copies that overlap the load
-    real* toff = args.sw;
     const unsigned grid = std::min<unsigned>(div_up(std::max<int64_t>(m, 1), 256), (unsigned)sm_count() * 8);
-    k_import_keys<Q, D, P, T><<<grid, 256, 0, s>>>(args, inst_of, pos, m, desc.cell, pow2_cell ? (float)(1.0 / desc.cell) : 0.f,
-                                                  k_in, v_in, toff);
-    DBM_LAUNCH_CHECK();
-    bool alt = false;
+    const float inv_cell_f = pow2_cell ? (float)(1.0 / desc.cell) : 0.f;
+    const uint32_t* ks = args.a.cell;  // the state's cell array holds the sorted keys either way
     if (presorted) {
-      // given in cell order: the keys (and the identity order k_import_keys wrote) stay as they are
+      // given in cell order: one pass, no sort, then a check of the order
+      import_in_alt = false;
+      k_import_presorted<Q, D, P, T><<<grid, 256, 0, s>>>(args, inst_of, pos, fin, m, desc.cell, inv_cell_f, v_in);
+      DBM_LAUNCH_CHECK();
       if (m > 1) {
-        k_check_sorted<<<grid, 256, 0, s>>>(k_in, m, args.status);
+        k_check_sorted<<<grid, 256, 0, s>>>(args.a.cell, m, args.status);
         DBM_LAUNCH_CHECK();
       }
     } else {
+      // the unsorted offsets [D][m] live in the weight scratch sw ([Q][mcap], Q > D, idle outside a
+      // step): an allocation here (and its cudaFree) would wait for every stream of the device,
+      // including a caller's copies that overlap the load
+      real* toff = args.sw;
+      k_import_keys<Q, D, P, T><<<grid, 256, 0, s>>>(args, inst_of, pos, m, desc.cell, inv_cell_f, k_in, v_in, toff);
+      DBM_LAUNCH_CHECK();
       // valid keys are < ncells < 2^key_bits; the marker 0xffffffff of a moment outside its box is
       // all ones in those bits too, so it still sorts after every valid key
+      bool alt = false;
       DBM_TRY(radix_sort_pairs<uint32_t>(k_in, v_in, k_alt, v_alt, m, nullptr, key_bits, sort_tmp, s, &alt));
+      import_in_alt = alt;
+      k_import_gather<Q, D, P, T><<<grid, 256, 0, s>>>(args, fin, m, alt ? k_alt : k_in, alt ? v_alt : v_in, toff);
+      DBM_LAUNCH_CHECK();
     }
-    import_in_alt = alt;
-    const uint32_t* ks = alt ? k_alt : k_in;
-    const uint32_t* vs = alt ? v_alt : v_in;
-    k_import_gather<Q, D, P, T><<<grid, 256, 0, s>>>(args, fin, m, ks, vs, toff);
-    DBM_LAUNCH_CHECK();
     // count of valid keys = m (invalid ones sort last with key 0xffffffff and raise ST_BAD_INPUT)
     DBM_CUDA(cudaMemcpyAsync(args.d_P, args.a.count, 4, cudaMemcpyDeviceToDevice, s));
     launch_cell_start(ks, args.d_P, ncells, args.a.start, s);
