@@ -575,13 +575,37 @@ def e2e_leg(sim, ib, x, f, steps=8, warmup=1, io="f32"):
     serial = {"value": points / (ms * 1e-3), "ms_per_step": ms / steps, "wall_s": wall}
     piped = _e2e_pipelined(sim, M, h_inst, h_pos, h_f, steps, warmup, (o_inst, o_pos, o_f, m2), presorted, tdt, row)
     serial["h2d_bytes_per_step"], serial["d2h_bytes_per_step"] = int(h2d // steps), int(d2h // steps)
+    # the device-side parts of a step alone (CUDA events, median of 5): the load of resident inputs,
+    # the step from the loaded state, and the export into capacity-sized buffers
+    out = tuple(torch.empty((sim.capacity,) + tuple(t.shape[1:]), dtype=t.dtype, device="cuda")
+                for t in (d_inst, d_pos, d_f))
+
+    def med_ms(fn, before=None):
+        r = []
+        for _ in range(5):
+            if before:
+                before()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            r.append(a.elapsed_time(b))
+        return float(np.median(r))
+
+    load = lambda: sim.set_state(d_inst, d_pos, d_f, check=False, presorted=presorted)
+    parts = {"load_ms": med_ms(load), "step_after_load_ms": med_ms(lambda: sim.step(1), before=load),
+             "export_ms": med_ms(lambda: sim.state_into(out))}
+    sim.check_status()
+    del out
     return {"value": piped["value"], "unit": "point-steps/s", "h2d_bytes_per_step": int(piped["h2d_bytes_per_step"]),
             "d2h_bytes_per_step": int(piped["d2h_bytes_per_step"]), "ms_per_step": piped["ms_per_step"],
             "wall_s": piped["wall_s"],
             "steps": steps, "warmup": warmup, "copy_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs}, "serial": serial,
             "result_equals_serial": piped["result_equals_serial"],
             "repetitions_ms_per_step": piped["repetitions_ms_per_step"], "statistic": "median of 3 repetitions",
-            "presorted": presorted, "io": io,
+            "presorted": presorted, "io": io, "device_parts": parts,
             "path": "Simulation.set_state(check=False, presorted=<input in cell order>)/step/state_into (C ABI "
                     "dbm_sim_*) with pinned host buffers and "
                     "no host wait inside a step; each step's host-to-device copy on its own stream overlaps the "
@@ -594,7 +618,8 @@ def e2e_both(sim, ib, x, f):
     e2e = e2e_leg(sim, ib, x, f, io="f32")
     e64 = e2e_leg(sim, ib, x, f, io="f64")
     e2e["f64_io"] = {k: e64[k] for k in ("value", "ms_per_step", "h2d_bytes_per_step", "d2h_bytes_per_step",
-                                         "copy_gbs", "repetitions_ms_per_step", "result_equals_serial")}
+                                         "copy_gbs", "repetitions_ms_per_step", "result_equals_serial",
+                                         "device_parts")}
     return e2e
 
 
