@@ -557,10 +557,12 @@ def _ulps32(a, b):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32dev"])
-def test_float32_interface(precision):
+@pytest.mark.parametrize("case", ["d2q9", "d3q19", "d2q9_cell_0.75"])
+def test_float32_interface(precision, case):
     """The float32 load and export (float arithmetic on the device):
       - cell and offset of every moment are bitwise those of the float64 load of the widened
-        values (power-of-two cell), and so are the exported float32 positions;
+        values (a power-of-two cell scales exactly in float; other cells take the float64 route),
+        and so are the exported float32 positions;
       - FP64 store: the whole state, the runs from it and the float32 export are bitwise the
         float64 ones (rounded);
       - FP32DEV store: f reconstructs the input to within 1e-7 relative and agrees with the float64
@@ -570,24 +572,33 @@ def test_float32_interface(precision):
         sorting load gives."""
     import torch
 
-    insts = [dict(dims=(24, 24), periodic=True, tau=0.6), dict(dims=(16, 20), periodic=True, tau=0.8)]
-    parts = [periodic_tg(24, "D2Q9", seed=11), periodic_tg(16, "D2Q9", seed=12)]
-    parts[1] = (np.mod(parts[1][0], [16, 20]), parts[1][1])
+    lattice, cell = ("D3Q19", 1.0) if case == "d3q19" else ("D2Q9", 0.75 if case.endswith("0.75") else 1.0)
+    if lattice == "D2Q9":
+        insts = [dict(dims=(24, 24), periodic=True, tau=0.6), dict(dims=(16, 20), periodic=True, tau=0.8)]
+        parts = [periodic_tg(24, "D2Q9", seed=11), periodic_tg(16, "D2Q9", seed=12)]
+        parts[1] = (np.mod(parts[1][0], [16, 20]), parts[1][1])
+    else:
+        insts = [dict(dims=(10, 10, 10), periodic=True, tau=0.6)]
+        parts = [periodic_tg(10, "D3Q19", seed=13, u0=0.02)]
+    if cell != 1.0:  # the same points in cells of 0.75: boxes of the scaled extent
+        parts = [(p[0] * cell, p[1]) for p in parts]
     ib = np.concatenate([np.full(len(p[0]), b) for b, p in enumerate(parts)])
     x32 = np.concatenate([p[0] for p in parts]).astype(np.float32)
     f32 = np.concatenate([p[1] for p in parts]).astype(np.float32)
+    D = x32.shape[1]
     cap = 2 * len(x32)
     sims, loaded = [], []
     for args in ((ib, x32.astype(np.float64), f32.astype(np.float64)), (ib, x32, f32)):
-        sim = _sim("D2Q9", insts, precision, 1.0, 1.5, 1.0, cap=cap)
+        sim = _sim(lattice, insts, precision, cell, 1.5 * cell, cell, cap=cap)
         sim.set_state(*args)
         loaded.append(sim.state_numpy())
         sims.append(sim)
     (i64, p64, g64), (i32, p32, g32) = loaded
     np.testing.assert_array_equal(i32, i64)
     np.testing.assert_array_equal(p32, p64)
-    cells = np.floor(x32).astype(np.int64)
-    order = np.lexsort((cells[:, 0], cells[:, 1], ib))  # one moment per cell here: the load's order
+    cells = np.floor(x32.astype(np.float64) / cell).astype(np.int64)
+    # one moment per cell here: the load's order is by instance, then z, y, x
+    order = np.lexsort(tuple(cells[:, a] for a in range(D)) + (ib,))
     if precision == "fp64":
         np.testing.assert_array_equal(g32, g64)
     else:
@@ -609,8 +620,39 @@ def test_float32_interface(precision):
             assert _ulps32(e_f, sf) <= 1.0
         reload = []
         for presorted in (False, True):
-            s2 = _sim("D2Q9", insts, precision, 1.0, 1.5, 1.0, cap=cap)
+            s2 = _sim(lattice, insts, precision, cell, 1.5 * cell, cell, cap=cap)
             s2.set_state(e_i, e_p, e_f, presorted=presorted)
             reload.append(s2.state_numpy())
         for a, b in zip(*reload):
             np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("presorted", [False, True])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_load_edge_cases(dtype, presorted):
+    """Empty loads, a single moment, and a moment outside a bounded box, through the float64 and
+    float32 loads, with and without the presorted flag."""
+    import torch
+
+    from direbm_gb300._lib import DbmError
+
+    insts = [dict(dims=(12, 12), origin=(-6, -6), periodic=False, tau=0.7)]
+    f1 = np.full((1, 9), 1.0 / 9.0)
+    sim = _sim("D2Q9", insts, "fp32dev", 1.0, 1.5, 1.0, cap=64)
+    sim.set_state(np.zeros(0, np.int32), np.zeros((0, 2), dtype), np.zeros((0, 9), dtype), presorted=presorted)
+    assert sim.count() == 0
+    for dt in (torch.float64, torch.float32):
+        i, p, g = sim.state(dtype=dt)
+        assert i.shape == (0,) and p.shape == (0, 2) and g.shape == (0, 9)
+    sim.set_state(np.zeros(1, np.int32), np.array([[0.25, -3.5]], dtype), f1.astype(dtype), presorted=presorted)
+    i, p, g = sim.state_numpy()
+    assert sim.count() == 1 and i.tolist() == [0]
+    np.testing.assert_array_equal(p, [[0.25, -3.5]])
+    np.testing.assert_allclose(g, f1, rtol=1e-7)
+    with pytest.raises(DbmError, match="outside"):
+        sim.set_state(np.zeros(2, np.int32), np.array([[0.5, 0.5], [7.5, 0.5]], dtype), np.tile(f1, (2, 1)).astype(dtype),
+                      presorted=presorted)
+    assert sim.status() == 0  # the raise cleared the bit; the simulator stays usable
+    sim.set_state(np.zeros(1, np.int32), np.array([[1.5, 1.5]], dtype), f1.astype(dtype), presorted=presorted)
+    sim.step(1)
+    assert sim.status() == 0 and sim.count() >= 1
