@@ -5,7 +5,8 @@ Run in a container where the reference checkout is available:
     python tests/golden/make_golden.py /path/to/DiReBM
 
 It imports the reference's numpy package (``direbm``, ``direbm.lbm``, ``direbm.fields``,
-``direbm.reference``) -- which needs no Warp -- and, for the two numpy helpers that live in the
+``direbm.reference``) -- which needs no Warp -- then the reference's GPU package
+(``direbm.warp``) with ``warp_emulator.py`` standing in for Warp (``warp_reference.npz``), and, for the two numpy helpers that live in the
 reference's Warp test module (``_cell_thin_ref`` and ``_ring`` of tests/test_warp_propagation.py),
 extracts just those function definitions with ``ast`` (the module itself imports Warp).  The
 outputs are small ``.npz`` files next to this script; the tests load only those files, so the
@@ -160,7 +161,84 @@ def main(ref_root: str) -> None:
         if r is not None:
             spawn[j] = r
     np.savez_compressed(HERE / "soft_spawn.npz", labels=labels, p=p, spawn=spawn)
+
+    warp_reference(helpers)
     print("golden vectors written to", HERE)
+
+
+def warp_reference(helpers) -> None:
+    """The reference's own GPU package (direbm/warp/*.py) run unchanged on the host through
+    warp_emulator.py: its stages on the propagation seeds, 3 steps of its GpuSimulator on the 13 x 13
+    pulse, its FP32 physics kernels and 10 steps of its GpuHexLBM.  Written to warp_reference.npz."""
+    sys.path.insert(0, str(HERE))
+    import warp_emulator
+
+    warp_emulator.install()
+    from direbm import equilibrium as eq64
+    from direbm.constants import ALPHA, DX, KAPPA_HARD, W
+    from direbm.warp import GpuHexLBM, GpuSimulator, collide, create_control_points, disperse, equilibrium, \
+        refine_control_points, resample
+
+    out = {}
+    f_rest = (1.0 * W).astype(np.float32)
+    out["stage_dx"], out["stage_cs"], out["stage_kappa_hard"] = DX, DX / ALPHA, KAPPA_HARD
+    # the propagation test's seeds (tests/test_warp_propagation.py:43-76)
+    for seed, (n, lo, hi) in {0: (20, -5.0, 5.0), 1: (50, -5.0, 5.0), 2: (40, -3.0, 3.0)}.items():
+        rng = np.random.default_rng(seed)
+        pos_m = rng.uniform(lo, hi, size=(n, 2))
+        f_m = rng.uniform(0.01, 1.0, size=(n, 7))
+        pos_c, val_c, dir_c = disperse(pos_m, f_m, DX)
+        cp, P = create_control_points(pos_c, DX / ALPHA)
+        cp_ref = refine_control_points(cp, pos_c, val_c, dir_c, DX, KAPPA_HARD)
+        wf = __import__("warp").array(f_rest, dtype=__import__("warp").float32)
+        opos, of = resample(pos_c, val_c, dir_c, cp_ref, DX, wf)
+        k = f"s{seed}_"
+        out[k + "pos_m"], out[k + "f_m"] = pos_m, f_m
+        out[k + "pos_c"], out[k + "val_c"], out[k + "dir_c"] = pos_c.numpy(), val_c.numpy(), dir_c.numpy()
+        out[k + "cp"], out[k + "cp_refined"] = cp.numpy(), cp_ref.numpy()
+        out[k + "out_pos"], out[k + "out_f"] = opos.numpy(), of.numpy()
+    # GpuSimulator: the 13 x 13 rest block with a central pulse (tests/test_warp_simulator.py:10-63)
+    pos, fs = [], []
+    for i in range(-6, 7):
+        for j in range(-6, 7):
+            pos.append([float(i), float(j)])
+            fs.append(eq64(np.float64(1.5 if (i == 0 and j == 0) else 1.0), np.zeros(2)))
+    pos, fs = np.array(pos), np.stack(fs)
+    sim = GpuSimulator(pos, fs, tau=0.6, rho_rest=1.0)
+    out["sim_pos0"], out["sim_f0"] = pos, fs
+    for step in range(1, 4):
+        sim.step()
+        x, f = sim.moments()
+        out[f"sim_x{step}"], out[f"sim_f{step}"] = x, f
+    # GpuSimulator on a jittered block (no lattice-exact distances, so every radius test is
+    # decided away from a tie): 12 x 12 points jittered by +-0.3, a small shear flow, 3 steps
+    rng = np.random.default_rng(5)
+    pos = (np.stack(np.meshgrid(np.arange(12.0), np.arange(12.0), indexing="xy"), -1).reshape(-1, 2)
+           + rng.uniform(-0.3, 0.3, size=(144, 2)))
+    u = np.stack([0.03 * np.sin(2 * np.pi * pos[:, 1] / 12.0), 0.02 * np.cos(2 * np.pi * pos[:, 0] / 12.0)], 1)
+    fs = np.stack([eq64(np.float64(1.0), u[i]) for i in range(len(pos))])
+    sim = GpuSimulator(pos, fs, tau=0.7, rho_rest=1.0)
+    out["jit_pos0"], out["jit_f0"] = pos, fs
+    for step in range(1, 4):
+        sim.step()
+        x, f = sim.moments()
+        out[f"jit_x{step}"], out[f"jit_f{step}"] = x, f
+    # FP32 physics kernels (tests/test_warp_physics.py seeds)
+    rng = np.random.default_rng(0)
+    rho = rng.uniform(0.5, 2.0, size=128)
+    u = rng.uniform(-0.1, 0.1, size=(128, 2))
+    out["phys_rho"], out["phys_u"], out["phys_eq"] = rho, u, equilibrium(rho, u)
+    rng = np.random.default_rng(1)
+    fcol = rng.uniform(0.01, 1.0, size=(256, 7))
+    out["phys_f"], out["phys_col"] = fcol, collide(fcol, 0.6)
+    # GpuHexLBM: 21 x 21 pulse, 10 steps (tests/test_warp_lbm.py)
+    lbm = GpuHexLBM(21, 21, tau=0.6)
+    lbm.set_pulse(1.5)
+    out["lbm_f0"] = lbm.f.numpy()
+    for _ in range(10):
+        lbm.step()
+    out["lbm_f10"] = lbm.f.numpy()
+    np.savez_compressed(HERE / "warp_reference.npz", **out)
 
 
 if __name__ == "__main__":
