@@ -224,7 +224,11 @@ __device__ __forceinline__ void thin_refine_cell(const Args<Q, D, P>& A, const u
       hi[a] = (int)floor(base + A.R + A.tiny);
     }
     const real bxr = cen[0] - cdk[0];
-    // window rows (sz, sy) in order, each one x range as runs of consecutive cells (see k_gather)
+    // window rows (sz, sy) in order, each one x range as runs of consecutive cells (see k_gather);
+    // the first item of each cell, then (when a window cell holds more) the others
+    bool more = false;
+#pragma unroll 1
+    for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
     for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
@@ -244,9 +248,16 @@ __device__ __forceinline__ void thin_refine_cell(const Args<Q, D, P>& A, const u
         if (lox > hix) continue;
         row_runs<D>(I, Fc[0], Fc[1] + sy, Fc[2] + sz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
           const uint32_t m1 = A.a.start[g1 + 1];
+          real prev = (real)-1;  // cell column of the previous item of the run
           for (uint32_t m = A.a.start[g0]; m < m1; ++m) {
-            if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: visited below
             const PackItem<real> it = A.a.pk[m];
+            const bool first = it.cx != prev;
+            prev = it.cx;
+            if (first != (pass == 0)) {
+              more = true;
+              continue;
+            }
+            if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: visited below
             const int sx = (int)it.cx + shift - Fc[0];
             const real c[3] = {canon_c<real>(sx, cdk[0], cen[0]), cy, cz};
             const real o[3] = {it.x, it.y, it.z};
@@ -591,8 +602,12 @@ __device__ __forceinline__ void weights_one(const Args<Q, D, P>& A, const uint32
   double swd = 0;
   CSum sws;
   // window rows (gz, gy) in order; per row one x range narrowed by the row's smallest |e_y|, |e_z|,
-  // visited as runs of consecutive cells (the items of a run are contiguous, in cell order)
+  // visited as runs of consecutive cells (the items of a run are contiguous, in cell order); the
+  // first item of each cell, then (when a window cell holds more) the others
   const real tx = rn_add(o[0], cdk[0]);
+  bool more = false;
+#pragma unroll 1
+  for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
   for (int gz = lo[2]; gz <= hi[2]; ++gz)
 #pragma unroll 1
@@ -616,8 +631,15 @@ __device__ __forceinline__ void weights_one(const Args<Q, D, P>& A, const uint32
       if (lox > hix) continue;
       row_runs<D>(I, Sc[0], Sc[1] + gy, Sc[2] + gz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
         const uint32_t c1 = A.b.start[g1 + 1];
+        real prev = (real)-1;  // cell column of the previous item of the run
         for (uint32_t c = A.b.start[g0]; c < c1; ++c) {
           const PackItem<real> it = A.b.pk[c];
+          const bool first = it.cx != prev;
+          prev = it.cx;
+          if (first != (pass == 0)) {
+            more = true;
+            continue;
+          }
           const int gx = (int)it.cx + shift - Sc[0];
           const real cc[3] = {rn_sub(rn_add((real)(-gx), cdk[0]), it.x), rn_sub(base[1], it.y),
                               D == 3 ? rn_sub(base[2], it.z) : (real)0};
@@ -666,7 +688,11 @@ __device__ __forceinline__ void gather_one(const Args<Q, D, P>& A, const uint32_
   float sb = 0.f;  // deviation part: small, plain FMA accumulation suffices
   const real bxr = p[0] - cdk[0];
   // window rows (sz, sy) in order; per row one x range narrowed by the row's smallest |e_y|, |e_z|,
-  // visited as runs of consecutive cells (the items of a run are contiguous, in cell order)
+  // visited as runs of consecutive cells (the items of a run are contiguous, in cell order); the
+  // first item of each cell, then (when a window cell holds more) the others
+  bool more = false;
+#pragma unroll 1
+  for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
   for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
@@ -686,9 +712,16 @@ __device__ __forceinline__ void gather_one(const Args<Q, D, P>& A, const uint32_
       if (lox > hix) continue;
       row_runs<D>(I, Gc[0], Gc[1] + sy, Gc[2] + sz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
         const uint32_t m1 = A.a.start[g1 + 1];
+        real prev = (real)-1;  // cell column of the previous item of the run
         for (uint32_t m = A.a.start[g0]; m < m1; ++m) {
-          if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: label opp[k]
           const PackItem<real> it = A.a.pk[m];
+          const bool first = it.cx != prev;
+          prev = it.cx;
+          if (first != (pass == 0)) {
+            more = true;
+            continue;
+          }
+          if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: label opp[k]
           const int sx = (int)it.cx + shift - Gc[0];
           const real c[3] = {canon_c<real>(sx, cdk[0], p[0]), cy, cz};
           const real o[3] = {it.x, it.y, it.z};

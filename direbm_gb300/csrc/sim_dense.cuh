@@ -223,26 +223,36 @@ __device__ __forceinline__ bool thin_refine_ds_tile(const Args<Q, 2, PF32>& A, c
         sx = __ffma2_rn(make_float2(wt, wt), e, sx);
       }
     };
-    auto visit = [&](int ci, float ex0, float ey0) {
+    // first items of the window's cells, noting the window positions whose cell has a second item
+    uint32_t ov = 0;
+    auto visit = [&](int pos, int ci, float ex0, float ey0) {
       const float4 o = S.rec[ci];
       one(o, wk + ci, ex0, ey0);
-      if (o.z >= 0.f) {
-        const int q = (int)o.z;
-        one(S.orec[q], owk + q, ex0, ey0);
-      }
+      if (o.z >= 0.f) ov |= 1u << pos;
     };
+    const int ncol = wide ? nxs : 4;
     if (!wide) {
 #pragma unroll
       for (int b = 0; b < 4; ++b)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, cx[a], cy[b]);
+        for (int a = 0; a < 4; ++a) visit(b * 4 + a, c0 + b * rw + a, cx[a], cy[b]);
     } else {
 #pragma unroll 1
       for (int b = 0; b < nys; ++b) {
         const float cyb = rn_sub((float)(jly + b), cen[1]);
 #pragma unroll 1
-        for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, rn_sub((float)(jlx + a), cen[0]), cyb);
+        for (int a = 0; a < nxs; ++a) visit(b * nxs + a, c0 + b * rw + a, rn_sub((float)(jlx + a), cen[0]), cyb);
       }
+    }
+    // then the second items, in window order
+#pragma unroll 1
+    while (ov) {
+      const int pos = __ffs(ov) - 1;
+      ov &= ov - 1;
+      const int b = wide ? pos / ncol : pos >> 2, a = pos - b * ncol;
+      const int ci = c0 + b * rw + a;
+      const int q = (int)S.rec[ci].z;
+      one(S.orec[q], owk + q, rn_sub((float)(jlx + a), cen[0]), rn_sub((float)(jly + b), cen[1]));
     }
     if (hit) mask |= 1u << k;
   }
@@ -338,21 +348,32 @@ __device__ __forceinline__ bool weights_ds_tile(const Args<Q, 2, PF32>& A, const
         const float d2 = rn_add(e2.x, e2.y);
         if (d2 <= A.R2) sws.add(A.R - rn_sqrt(d2));
       };
-      auto visit = [&](int ci, float basex, float basey) {
+      // first items of the window's cells, noting the window positions whose cell has a second item
+      uint32_t ov = 0;
+      auto visit = [&](int pos, int ci, float basex, float basey) {
         const float4 pc = S.rec[ci];
         one(pc, basex, basey);
-        if (pc.z >= 0.f) one(S.orec[(int)pc.z], basex, basey);
+        if (pc.z >= 0.f) ov |= 1u << pos;
       };
+      const int ncol = wide ? nxs : 4;
       if (!wide) {
 #pragma unroll
         for (int b = 0; b < 4; ++b)
 #pragma unroll
-          for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, bxv[a], byv[b]);
+          for (int a = 0; a < 4; ++a) visit(b * 4 + a, c0 + b * rw + a, bxv[a], byv[b]);
       } else {
 #pragma unroll 1
         for (int b = 0; b < nys; ++b)
 #pragma unroll 1
-          for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, (float)(-(ulx + a)), (float)(-(uly + b)));
+          for (int a = 0; a < nxs; ++a) visit(b * nxs + a, c0 + b * rw + a, (float)(-(ulx + a)), (float)(-(uly + b)));
+      }
+      // then the second items, in window order
+#pragma unroll 1
+      while (ov) {
+        const int pos = __ffs(ov) - 1;
+        ov &= ov - 1;
+        const int b = wide ? pos / ncol : pos >> 2, a = pos - b * ncol;
+        one(S.orec[(int)S.rec[c0 + b * rw + a].z], (float)(-(ulx + a)), (float)(-(uly + b)));
       }
       const float sw = sws.value();
       A.sw[(int64_t)k * A.mcap + m] = sw > 0.f ? 1.f / sw : 0.f;
@@ -428,26 +449,35 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
           sb = r.y;
         }
       };
-      auto visit = [&](int ci, float ex0, float ey0) {
+      // first items of the window's cells, noting the window positions whose cell has a second item
+      uint32_t ov = 0;
+      auto visit = [&](int pos, int ci, float ex0, float ey0) {
         const float4 o = S.rec[ci];
         one(o, kvk + ci, ex0, ey0);
-        if (o.z >= 0.f) {
-          const int q = (int)o.z;
-          one(S.orec[q], okvk + q, ex0, ey0);
-        }
+        if (o.z >= 0.f) ov |= 1u << pos;
       };
+      const int ncol = wide ? nxs : 4;
       if (!wide) {
 #pragma unroll
         for (int b = 0; b < 4; ++b)
 #pragma unroll
-          for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, cx[a], cy[b]);
+          for (int a = 0; a < 4; ++a) visit(b * 4 + a, c0 + b * rw + a, cx[a], cy[b]);
       } else {
 #pragma unroll 1
         for (int b = 0; b < nys; ++b) {
           const float cyb = rn_sub((float)(jly + b), pp.y);
 #pragma unroll 1
-          for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, rn_sub((float)(jlx + a), pp.x), cyb);
+          for (int a = 0; a < nxs; ++a) visit(b * nxs + a, c0 + b * rw + a, rn_sub((float)(jlx + a), pp.x), cyb);
         }
+      }
+      // then the second items, in window order
+#pragma unroll 1
+      while (ov) {
+        const int pos = __ffs(ov) - 1;
+        ov &= ov - 1;
+        const int b = wide ? pos / ncol : pos >> 2, a = pos - b * ncol;
+        const int q = (int)S.rec[c0 + b * rw + a].z;
+        one(S.orec[q], okvk + q, rn_sub((float)(jlx + a), pp.x), rn_sub((float)(jly + b), pp.y));
       }
       const DF Ad = df_norm(sa.hi, sa.lo);
       const DF Fv = df_add(df_mul(DF{A.L.wf[k], A.L.wlo[k]}, Ad), DF{sb, 0.f});

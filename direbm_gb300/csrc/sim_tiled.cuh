@@ -258,6 +258,9 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
     const real bxr = cen[0] - cdx, byr = cen[1] - cdy;
     const int lox = max((int)floor(bxr - A.R - A.tiny), -bx), hix = min((int)floor(bxr + A.R + A.tiny), rw - 1 - bx);
     const int loy = max((int)floor(byr - A.R - A.tiny), -by), hiy = min((int)floor(byr + A.R + A.tiny), rh - 1 - by);
+    bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+    for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
     for (int sy = loy; sy <= hiy; ++sy) {
       const real cy = canon_c<real>(sy, cdy, cen[1]);
@@ -266,8 +269,10 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
         const real c[3] = {canon_c<real>(sx, cdx, cen[0]), cy, 0};
         if (cell_d2_lower<2, real>(c) > A.R2) continue;
         const int ci = (by + sy) * rw + (bx + sx);
-        const int m1 = s_end[ci];
-        for (int m = s_beg[ci]; m < m1; ++m) {
+        const int mb = s_beg[ci], me = s_end[ci];
+        more |= me - mb > 1;
+        const int m0 = pass ? mb + 1 : mb, m1 = pass ? me : min(me, mb + 1);
+        for (int m = m0; m < m1; ++m) {
           const Pair<real> o2 = pos(m);
           const real o[3] = {o2.x, o2.y, 0};
           real e[3];
@@ -398,6 +403,9 @@ __device__ __forceinline__ void refine_shift(const Args<Q, 2, PF32>& A, int rw, 
     const float cxo = (float)(cdx - bx);
     const float* wk = s_w + k * cap;
     bool hit = false;
+    bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+    for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll
     for (int t = 0; t < NR; ++t) {
       if (t >= w.nr) break;
@@ -407,8 +415,15 @@ __device__ __forceinline__ void refine_shift(const Args<Q, 2, PF32>& A, int rw, 
       const int row = ry * rw + bx;
       const int m1 = s_end[row + hi];
       const float cy = w.cy[t];
+      float prev = -1.f;  // column of the previous item of the row
       for (int m = s_beg[row + lo]; m < m1; ++m) {
         const Item<float> it = s_it[m];
+        const bool first = it.rx != prev;
+        prev = it.rx;
+        if (first != (pass == 0)) {
+          more = true;
+          continue;
+        }
         const float cx = rn_sub(rn_add(it.rx, cxo), c.x);
         const float2 e = __fadd2_rn(make_float2(it.ox, it.oy), make_float2(cx, cy));
         const float2 e2 = __fmul2_rn(e, e);
@@ -515,6 +530,9 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
     const real bxr = cen[0] - cdx, byr = cen[1] - cdy;
     const int loy = max((int)floor(byr - A.R - A.tiny), -by), hiy = min((int)floor(byr + A.R + A.tiny), rh - 1 - by);
     const real* wk = s_w + k * cap;
+    bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+    for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
     for (int sy = loy; sy <= hiy; ++sy) {
       const real cy = canon_c<real>(sy, cdy, cen[1]);
@@ -524,8 +542,15 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
       if (lox > hix) continue;
       const int row = (by + sy) * rw + bx;
       const int m1 = s_end[row + hix];
+      real prev = (real)-1;  // column of the previous item of the row
       for (int m = s_beg[row + lox]; m < m1; ++m) {
         const Item<real> it = s_it[m];
+        const bool first = it.rx != prev;
+        prev = it.rx;
+        if (first != (pass == 0)) {
+          more = true;
+          continue;
+        }
         const real cx = rn_sub(rn_add(it.rx - bxf, cdx), cen[0]);
         const real ex = rn_add(it.ox, cx), ey = rn_add(it.oy, cy);
         const real d2 = rn_add(rn_mul(ex, ex), rn_mul(ey, ey));
@@ -712,6 +737,9 @@ __device__ __forceinline__ void weights_body(const Args<Q, 2, P>& A, const InstK
         const int loy = max((int)floor(ty - A.R - A.tiny), -by), hiy = min((int)floor(ty + A.R + A.tiny), rh - 1 - by);
         double swd = 0;
         CSum sws;
+        bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+        for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
         for (int gy = loy; gy <= hiy; ++gy) {
           const real basey = rn_add((real)(-gy), cdy);
@@ -725,8 +753,10 @@ __device__ __forceinline__ void weights_body(const Args<Q, 2, P>& A, const InstK
             const real lbx = elx > (real)0 ? elx : (ehx < (real)0 ? -ehx : (real)0);
             if (rn_add(rn_mul(lbx, lbx), lby2) > A.R2) continue;
             const int ci = (by + gy) * rw + (bx + gx);
-            const int c1 = s_end[ci];
-            for (int c = s_beg[ci]; c < c1; ++c) {
+            const int cb = s_beg[ci], ce = s_end[ci];
+            more |= ce - cb > 1;
+            const int cs = pass ? cb + 1 : cb, c1 = pass ? ce : min(ce, cb + 1);
+            for (int c = cs; c < c1; ++c) {
               const Pair<real> pc = cpos(c);
               const real cc[3] = {rn_sub(basex, pc.x), rn_sub(basey, pc.y), 0};
               real e[3];
@@ -775,6 +805,9 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
         const int loy = max((int)floor(ty - A.R - A.tiny), -by), hiy = min((int)floor(ty + A.R + A.tiny), rh - 1 - by);
         double swd = 0;
         CSum sws;
+        bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+        for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
         for (int gy = loy; gy <= hiy; ++gy) {
           const real basey = rn_add((real)(-gy), cdy);
@@ -787,8 +820,15 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
           if (lox > hix) continue;
           const int row = (by + gy) * rw + bx;
           const int c1 = s_end[row + hix];
+          real prev = (real)-1;  // column of the previous item of the row
           for (int c = s_beg[row + lox]; c < c1; ++c) {
             const Item<real> it = s_cit[c];
+            const bool first = it.rx != prev;
+            prev = it.rx;
+            if (first != (pass == 0)) {
+              more = true;
+              continue;
+            }
             const real basex = rn_add(bxf - it.rx, cdx);  // float(-dG) + cd
             const real ex = rn_add(o.x, rn_sub(basex, it.ox)), ey = rn_add(o.y, rn_sub(basey, it.oy));
             const real d2 = rn_add(rn_mul(ex, ex), rn_mul(ey, ey));
@@ -854,6 +894,9 @@ __device__ __forceinline__ void weights_rows_shift(const Args<Q, 2, PF32>& A, co
         const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
         const float bxc = (float)(bx + cdx);  // base_x of a control point in region column rx = bxc - rx
         CSum sws;
+        bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+        for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll
         for (int t = 0; t < NR; ++t) {
           if (t >= nr) break;
@@ -863,8 +906,15 @@ __device__ __forceinline__ void weights_rows_shift(const Args<Q, 2, PF32>& A, co
           const int row = ry * rw + bx;
           const int c1 = s_end[row + hi];
           const float basey = by_[t];
+          float prev = -1.f;  // column of the previous item of the row
           for (int c = s_beg[row + lo]; c < c1; ++c) {
             const Item<float> it = s_cit[c];
+            const bool first = it.rx != prev;
+            prev = it.rx;
+            if (first != (pass == 0)) {
+              more = true;
+              continue;
+            }
             const float basex = rn_sub(bxc, it.rx);  // float(cd_x - dG_x), exact
             const float2 q = __fadd2_rn(make_float2(basex, basey), make_float2(-it.ox, -it.oy));
             const float2 e = __fadd2_rn(make_float2(o.x, o.y), q);
@@ -963,6 +1013,9 @@ __device__ __forceinline__ void gather_body(const Args<Q, 2, P>& A, const InstK&
         double acc = 0;
         CSum sa;
         float sb = 0.f;  // deviation part: small, plain FMA accumulation suffices
+        bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+        for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
         for (int sy = loy; sy <= hiy; ++sy) {
           const real cy = canon_c<real>(sy, cdy, pp.y);
@@ -971,8 +1024,10 @@ __device__ __forceinline__ void gather_body(const Args<Q, 2, P>& A, const InstK&
             const real c[3] = {canon_c<real>(sx, cdx, pp.x), cy, 0};
             if (cell_d2_lower<2, real>(c) > A.R2) continue;
             const int ci = (by + sy) * rw + (bx + sx);
-            const int m1 = s_end[ci];
-            for (int m = s_beg[ci]; m < m1; ++m) {
+            const int mb = s_beg[ci], me = s_end[ci];
+            more |= me - mb > 1;
+            const int m0 = pass ? mb + 1 : mb, m1 = pass ? me : min(me, mb + 1);
+            for (int m = m0; m < m1; ++m) {
               real o[3];
               if constexpr (LOCAL) {
                 const Pair<real> o2 = s_pos[m];
@@ -1061,6 +1116,9 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
         double acc = 0;
         CSum sa;
         float sb = 0.f;  // deviation part: small, plain FMA accumulation suffices
+        bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+        for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll 1
         for (int sy = loy; sy <= hiy; ++sy) {
           const real cy = canon_c<real>(sy, cdy, pp.y);
@@ -1070,8 +1128,15 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
           if (lox > hix) continue;
           const int row = (by + sy) * rw + bx;
           const int m1 = s_end[row + hix];
+          real prev = (real)-1;  // column of the previous item of the row
           for (int m = s_beg[row + lox]; m < m1; ++m) {
             const Item<real> it = s_it[m];
+            const bool first = it.rx != prev;
+            prev = it.rx;
+            if (first != (pass == 0)) {
+              more = true;
+              continue;
+            }
             const real cx = rn_sub(rn_add(it.rx - bxf, cdx), pp.x);
             const real ex = rn_add(it.ox, cx), ey = rn_add(it.oy, cy);
             const real d2 = rn_add(rn_mul(ex, ex), rn_mul(ey, ey));
@@ -1128,6 +1193,9 @@ __device__ __forceinline__ void gather_cp_shift(const Args<Q, 2, PF32>& A, int k
   const float cxo = (float)(cdx - bx);  // region column + cxo = float(dS_x + cd_x), exact
   CSum sa;
   float sb = 0.f;  // deviation part: plain FMA accumulation, as in gather_rows
+  bool more = false;  // a window cell holds a second item: a second pass takes those
+#pragma unroll 1
+  for (int pass = 0; pass <= (int)more; ++pass)
 #pragma unroll
   for (int t = 0; t < NR; ++t) {
     if (t >= w.nr) break;
@@ -1138,8 +1206,15 @@ __device__ __forceinline__ void gather_cp_shift(const Args<Q, 2, PF32>& A, int k
     const GRec* it = s_rec + s_beg[row + lo];
     const GRec* const end = s_rec + s_end[row + hi];
     const float cy = w.cy[t];
+    float prev = -1.f;  // column of the previous item of the row
     for (; it < end; ++it) {
       const float4 a = *reinterpret_cast<const float4*>(it);
+      const bool first = a.z != prev;
+      prev = a.z;
+      if (first != (pass == 0)) {
+        more = true;
+        continue;
+      }
       const float cx = rn_sub(rn_add(a.z, cxo), pp.x);
       const float2 e = __fadd2_rn(make_float2(a.x, a.y), make_float2(cx, cy));
       const float2 e2 = __fmul2_rn(e, e);
