@@ -16,8 +16,12 @@
 // c = rn(float(j) - p) of the stencil's four columns and rows is computed once per point.
 //
 // Results are bit-identical to the row-segment kernels: each sum visits the same hits in the same
-// order (window rows ascending, then columns ascending, then the items of a cell in order) with the
-// same operations.  A tile whose region holds a cell with three or more items, or more two-item
+// order with the same operations.  The first items of the window's cells come first (window rows
+// ascending, then columns ascending), then the second items in the same cell order.  The unrolled
+// stencil reads only the records; a record naming a second item sets a bit of a per-thread
+// window mask, and a short loop over that mask visits the second items afterwards.  A warp then
+// pays for a second item only in the loop, not at every stencil position where some lane's cell
+// has one.  A tile whose region holds a cell with three or more items, or more two-item
 // cells than the overflow list takes, is handed to the row-segment code (a second, normally empty,
 // launch over the deferred tiles).
 #pragma once

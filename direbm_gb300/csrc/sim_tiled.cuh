@@ -3,9 +3,12 @@
 // A block owns a tile of tx x ty cells of one instance.  It stages everything its window loops
 // can touch -- the moments (or control points) of the tile plus a halo -- from the sorted cell
 // ranges into shared memory once, with coalesced row-segment copies, and then every thread runs
-// its loops out of shared memory.  The per-thread loop order (direction, window row, window
-// column, item order inside a cell) is the same as in the untiled kernels, so results are
-// bit-identical to them and the FP64 path stays bit-compatible with the oracle.
+// its loops out of shared memory.  The per-thread loop order is the same as in the untiled
+// kernels, so results are bit-identical to them and the FP64 path stays bit-compatible with the
+// oracle.  Per direction, a window sum first takes the first item of every window cell (window rows
+// ascending, columns ascending), then, if a window cell holds more, a second pass takes the other
+// items in the same cell order.  Two-item cells are rare (refine moves that cross a cell face), so
+// the second pass is rare too, and it costs no per-item branch in the first.
 //
 // Regions hold a data-dependent number of items.  When a region holds more than the shared-memory
 // capacity, the block keeps global indices in its range table and reads the items from global
@@ -357,7 +360,8 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
 // columns [a_j - cd_k,x, b_j - cd_k,x] move.  The table of rows is built once per reference point
 // instead of once per (point, direction).  The window bounds keep their 1e-4 cell margin, which
 // is far above the rounding of p - cd, so every hit lies inside the shifted window and the hits
-// are visited in the same order (rows ascending, then the row's items): sums are bit-identical to
+// are visited in the same order (rows ascending, then the row's items, first items before the
+// others): sums are bit-identical to
 // the per-direction windows.
 
 // Rows of the whole-cell window tables: NR >= floor(2R + 2 tiny) + 2 (R < 2 cells).
