@@ -225,10 +225,10 @@ __device__ __forceinline__ void thin_refine_cell(const Args<Q, D, P>& A, const u
     }
     const real bxr = cen[0] - cdk[0];
     // window rows (sz, sy) in order, each one x range as runs of consecutive cells (see k_gather);
-    // the first item of each cell, then (when a window cell holds more) the others
+    // 2D FP32: the first item of each cell, then (when a window cell holds more) the others
     bool more = false;
 #pragma unroll 1
-    for (int pass = 0; pass <= (int)more; ++pass)
+    for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, D> && more); ++pass)
 #pragma unroll 1
     for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
@@ -248,16 +248,19 @@ __device__ __forceinline__ void thin_refine_cell(const Args<Q, D, P>& A, const u
         if (lox > hix) continue;
         row_runs<D>(I, Fc[0], Fc[1] + sy, Fc[2] + sz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
           const uint32_t m1 = A.a.start[g1 + 1];
-          real prev = (real)-1;  // cell column of the previous item of the run
+          [[maybe_unused]] real prev = (real)-1;  // cell column of the previous item of the run
           for (uint32_t m = A.a.start[g0]; m < m1; ++m) {
+            if (!kFirstItemsFirst<P, D> && A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;
             const PackItem<real> it = A.a.pk[m];
-            const bool first = it.cx != prev;
-            prev = it.cx;
-            if (first != (pass == 0)) {
-              more = true;
-              continue;
+            if constexpr (kFirstItemsFirst<P, D>) {
+              const bool first = it.cx != prev;
+              prev = it.cx;
+              if (first != (pass == 0)) {
+                more = true;
+                continue;
+              }
+              if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: visited below
             }
-            if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: visited below
             const int sx = (int)it.cx + shift - Fc[0];
             const real c[3] = {canon_c<real>(sx, cdk[0], cen[0]), cy, cz};
             const real o[3] = {it.x, it.y, it.z};
@@ -607,7 +610,7 @@ __device__ __forceinline__ void weights_one(const Args<Q, D, P>& A, const uint32
   const real tx = rn_add(o[0], cdk[0]);
   bool more = false;
 #pragma unroll 1
-  for (int pass = 0; pass <= (int)more; ++pass)
+  for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, D> && more); ++pass)
 #pragma unroll 1
   for (int gz = lo[2]; gz <= hi[2]; ++gz)
 #pragma unroll 1
@@ -631,14 +634,16 @@ __device__ __forceinline__ void weights_one(const Args<Q, D, P>& A, const uint32
       if (lox > hix) continue;
       row_runs<D>(I, Sc[0], Sc[1] + gy, Sc[2] + gz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
         const uint32_t c1 = A.b.start[g1 + 1];
-        real prev = (real)-1;  // cell column of the previous item of the run
+        [[maybe_unused]] real prev = (real)-1;  // cell column of the previous item of the run
         for (uint32_t c = A.b.start[g0]; c < c1; ++c) {
           const PackItem<real> it = A.b.pk[c];
-          const bool first = it.cx != prev;
-          prev = it.cx;
-          if (first != (pass == 0)) {
-            more = true;
-            continue;
+          if constexpr (kFirstItemsFirst<P, D>) {
+            const bool first = it.cx != prev;
+            prev = it.cx;
+            if (first != (pass == 0)) {
+              more = true;
+              continue;
+            }
           }
           const int gx = (int)it.cx + shift - Sc[0];
           const real cc[3] = {rn_sub(rn_add((real)(-gx), cdk[0]), it.x), rn_sub(base[1], it.y),
@@ -689,10 +694,10 @@ __device__ __forceinline__ void gather_one(const Args<Q, D, P>& A, const uint32_
   const real bxr = p[0] - cdk[0];
   // window rows (sz, sy) in order; per row one x range narrowed by the row's smallest |e_y|, |e_z|,
   // visited as runs of consecutive cells (the items of a run are contiguous, in cell order); the
-  // first item of each cell, then (when a window cell holds more) the others
+  // first item of each cell, then (when a window cell holds more) the others (2D FP32)
   bool more = false;
 #pragma unroll 1
-  for (int pass = 0; pass <= (int)more; ++pass)
+  for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, D> && more); ++pass)
 #pragma unroll 1
   for (int sz = lo[2]; sz <= hi[2]; ++sz)
 #pragma unroll 1
@@ -712,16 +717,19 @@ __device__ __forceinline__ void gather_one(const Args<Q, D, P>& A, const uint32_
       if (lox > hix) continue;
       row_runs<D>(I, Gc[0], Gc[1] + sy, Gc[2] + sz, lox, hix, [&](uint32_t g0, uint32_t g1, int shift) {
         const uint32_t m1 = A.a.start[g1 + 1];
-        real prev = (real)-1;  // cell column of the previous item of the run
+        [[maybe_unused]] real prev = (real)-1;  // cell column of the previous item of the run
         for (uint32_t m = A.a.start[g0]; m < m1; ++m) {
+          if (!kFirstItemsFirst<P, D> && A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;
           const PackItem<real> it = A.a.pk[m];
-          const bool first = it.cx != prev;
-          prev = it.cx;
-          if (first != (pass == 0)) {
-            more = true;
-            continue;
+          if constexpr (kFirstItemsFirst<P, D>) {
+            const bool first = it.cx != prev;
+            prev = it.cx;
+            if (first != (pass == 0)) {
+              more = true;
+              continue;
+            }
+            if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: label opp[k]
           }
-          if (A.any_obstacle && ((A.bmask[m] >> k) & 1u)) continue;  // bounced: label opp[k]
           const int sx = (int)it.cx + shift - Gc[0];
           const real c[3] = {canon_c<real>(sx, cdk[0], p[0]), cy, cz};
           const real o[3] = {it.x, it.y, it.z};

@@ -316,6 +316,13 @@ struct StepHook {
   virtual int after(const void* args, cudaStream_t s) = 0;
 };
 
+// Summation order of the window sums (refine, weights, gather).  2D FP32 (where dense stencils,
+// shifted and plain row segments and the untiled kernels must agree bit for bit): per direction,
+// the first item of every window cell in window order, then, if a window cell holds more, the
+// other items in the same cell order.  Elsewhere (FP64, 3D) the items of each cell in order.
+template <class P, int D>
+constexpr bool kFirstItemsFirst = std::is_same<P, PF32>::value && D == 2;
+
 // Type-erased simulator (SimImpl<Q, D, P> in sim.cu).
 struct SimBase {
   virtual ~SimBase() = default;

@@ -5,10 +5,11 @@
 // ranges into shared memory once, with coalesced row-segment copies, and then every thread runs
 // its loops out of shared memory.  The per-thread loop order is the same as in the untiled
 // kernels, so results are bit-identical to them and the FP64 path stays bit-compatible with the
-// oracle.  Per direction, a window sum first takes the first item of every window cell (window rows
-// ascending, columns ascending), then, if a window cell holds more, a second pass takes the other
-// items in the same cell order.  Two-item cells are rare (refine moves that cross a cell face), so
-// the second pass is rare too, and it costs no per-item branch in the first.
+// oracle.  With the FP32 store (kFirstItemsFirst), a window sum takes per direction the first item
+// of every window cell (window rows ascending, columns ascending), then, if a window cell holds
+// more, a second pass takes the other items in the same cell order; with FP64 the items of each
+// cell in order.  Two-item cells are rare (refine moves that cross a cell face), so the second
+// pass is rare too.
 //
 // Regions hold a data-dependent number of items.  When a region holds more than the shared-memory
 // capacity, the block keeps global indices in its range table and reads the items from global
@@ -261,9 +262,9 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
     const real bxr = cen[0] - cdx, byr = cen[1] - cdy;
     const int lox = max((int)floor(bxr - A.R - A.tiny), -bx), hix = min((int)floor(bxr + A.R + A.tiny), rw - 1 - bx);
     const int loy = max((int)floor(byr - A.R - A.tiny), -by), hiy = min((int)floor(byr + A.R + A.tiny), rh - 1 - by);
-    bool more = false;  // a window cell holds a second item: a second pass takes those
+    bool more = false;  // (2D FP32) a window cell holds a second item: a second pass takes those
 #pragma unroll 1
-    for (int pass = 0; pass <= (int)more; ++pass)
+    for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, 2> && more); ++pass)
 #pragma unroll 1
     for (int sy = loy; sy <= hiy; ++sy) {
       const real cy = canon_c<real>(sy, cdy, cen[1]);
@@ -274,7 +275,7 @@ __device__ __forceinline__ void thin_refine_body(const Args<Q, 2, P>& A, const I
         const int ci = (by + sy) * rw + (bx + sx);
         const int mb = s_beg[ci], me = s_end[ci];
         more |= me - mb > 1;
-        const int m0 = pass ? mb + 1 : mb, m1 = pass ? me : min(me, mb + 1);
+        const int m0 = pass ? mb + 1 : mb, m1 = (pass || !kFirstItemsFirst<P, 2>) ? me : min(me, mb + 1);
         for (int m = m0; m < m1; ++m) {
           const Pair<real> o2 = pos(m);
           const real o[3] = {o2.x, o2.y, 0};
@@ -534,9 +535,9 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
     const real bxr = cen[0] - cdx, byr = cen[1] - cdy;
     const int loy = max((int)floor(byr - A.R - A.tiny), -by), hiy = min((int)floor(byr + A.R + A.tiny), rh - 1 - by);
     const real* wk = s_w + k * cap;
-    bool more = false;  // a window cell holds a second item: a second pass takes those
+    bool more = false;  // (2D FP32) a window cell holds a second item: a second pass takes those
 #pragma unroll 1
-    for (int pass = 0; pass <= (int)more; ++pass)
+    for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, 2> && more); ++pass)
 #pragma unroll 1
     for (int sy = loy; sy <= hiy; ++sy) {
       const real cy = canon_c<real>(sy, cdy, cen[1]);
@@ -546,14 +547,16 @@ __device__ __forceinline__ void thin_refine_rows(const Args<Q, 2, P>& A, const I
       if (lox > hix) continue;
       const int row = (by + sy) * rw + bx;
       const int m1 = s_end[row + hix];
-      real prev = (real)-1;  // column of the previous item of the row
+      [[maybe_unused]] real prev = (real)-1;  // column of the previous item of the row
       for (int m = s_beg[row + lox]; m < m1; ++m) {
         const Item<real> it = s_it[m];
-        const bool first = it.rx != prev;
-        prev = it.rx;
-        if (first != (pass == 0)) {
-          more = true;
-          continue;
+        if constexpr (kFirstItemsFirst<P, 2>) {
+          const bool first = it.rx != prev;
+          prev = it.rx;
+          if (first != (pass == 0)) {
+            more = true;
+            continue;
+          }
         }
         const real cx = rn_sub(rn_add(it.rx - bxf, cdx), cen[0]);
         const real ex = rn_add(it.ox, cx), ey = rn_add(it.oy, cy);
@@ -741,9 +744,9 @@ __device__ __forceinline__ void weights_body(const Args<Q, 2, P>& A, const InstK
         const int loy = max((int)floor(ty - A.R - A.tiny), -by), hiy = min((int)floor(ty + A.R + A.tiny), rh - 1 - by);
         double swd = 0;
         CSum sws;
-        bool more = false;  // a window cell holds a second item: a second pass takes those
+        bool more = false;  // (2D FP32) a window cell holds a second item: a second pass takes those
 #pragma unroll 1
-        for (int pass = 0; pass <= (int)more; ++pass)
+        for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, 2> && more); ++pass)
 #pragma unroll 1
         for (int gy = loy; gy <= hiy; ++gy) {
           const real basey = rn_add((real)(-gy), cdy);
@@ -759,7 +762,7 @@ __device__ __forceinline__ void weights_body(const Args<Q, 2, P>& A, const InstK
             const int ci = (by + gy) * rw + (bx + gx);
             const int cb = s_beg[ci], ce = s_end[ci];
             more |= ce - cb > 1;
-            const int cs = pass ? cb + 1 : cb, c1 = pass ? ce : min(ce, cb + 1);
+            const int cs = pass ? cb + 1 : cb, c1 = (pass || !kFirstItemsFirst<P, 2>) ? ce : min(ce, cb + 1);
             for (int c = cs; c < c1; ++c) {
               const Pair<real> pc = cpos(c);
               const real cc[3] = {rn_sub(basex, pc.x), rn_sub(basey, pc.y), 0};
@@ -809,9 +812,9 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
         const int loy = max((int)floor(ty - A.R - A.tiny), -by), hiy = min((int)floor(ty + A.R + A.tiny), rh - 1 - by);
         double swd = 0;
         CSum sws;
-        bool more = false;  // a window cell holds a second item: a second pass takes those
+        bool more = false;  // (2D FP32) a window cell holds a second item: a second pass takes those
 #pragma unroll 1
-        for (int pass = 0; pass <= (int)more; ++pass)
+        for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, 2> && more); ++pass)
 #pragma unroll 1
         for (int gy = loy; gy <= hiy; ++gy) {
           const real basey = rn_add((real)(-gy), cdy);
@@ -824,14 +827,16 @@ __device__ __forceinline__ void weights_rows(const Args<Q, 2, P>& A, const InstK
           if (lox > hix) continue;
           const int row = (by + gy) * rw + bx;
           const int c1 = s_end[row + hix];
-          real prev = (real)-1;  // column of the previous item of the row
+          [[maybe_unused]] real prev = (real)-1;  // column of the previous item of the row
           for (int c = s_beg[row + lox]; c < c1; ++c) {
             const Item<real> it = s_cit[c];
-            const bool first = it.rx != prev;
-            prev = it.rx;
-            if (first != (pass == 0)) {
-              more = true;
-              continue;
+            if constexpr (kFirstItemsFirst<P, 2>) {
+              const bool first = it.rx != prev;
+              prev = it.rx;
+              if (first != (pass == 0)) {
+                more = true;
+                continue;
+              }
             }
             const real basex = rn_add(bxf - it.rx, cdx);  // float(-dG) + cd
             const real ex = rn_add(o.x, rn_sub(basex, it.ox)), ey = rn_add(o.y, rn_sub(basey, it.oy));
@@ -1017,9 +1022,9 @@ __device__ __forceinline__ void gather_body(const Args<Q, 2, P>& A, const InstK&
         double acc = 0;
         CSum sa;
         float sb = 0.f;  // deviation part: small, plain FMA accumulation suffices
-        bool more = false;  // a window cell holds a second item: a second pass takes those
+        bool more = false;  // (2D FP32) a window cell holds a second item: a second pass takes those
 #pragma unroll 1
-        for (int pass = 0; pass <= (int)more; ++pass)
+        for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, 2> && more); ++pass)
 #pragma unroll 1
         for (int sy = loy; sy <= hiy; ++sy) {
           const real cy = canon_c<real>(sy, cdy, pp.y);
@@ -1030,7 +1035,7 @@ __device__ __forceinline__ void gather_body(const Args<Q, 2, P>& A, const InstK&
             const int ci = (by + sy) * rw + (bx + sx);
             const int mb = s_beg[ci], me = s_end[ci];
             more |= me - mb > 1;
-            const int m0 = pass ? mb + 1 : mb, m1 = pass ? me : min(me, mb + 1);
+            const int m0 = pass ? mb + 1 : mb, m1 = (pass || !kFirstItemsFirst<P, 2>) ? me : min(me, mb + 1);
             for (int m = m0; m < m1; ++m) {
               real o[3];
               if constexpr (LOCAL) {
@@ -1120,9 +1125,9 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
         double acc = 0;
         CSum sa;
         float sb = 0.f;  // deviation part: small, plain FMA accumulation suffices
-        bool more = false;  // a window cell holds a second item: a second pass takes those
+        bool more = false;  // (2D FP32) a window cell holds a second item: a second pass takes those
 #pragma unroll 1
-        for (int pass = 0; pass <= (int)more; ++pass)
+        for (int pass = 0; pass <= (int)(kFirstItemsFirst<P, 2> && more); ++pass)
 #pragma unroll 1
         for (int sy = loy; sy <= hiy; ++sy) {
           const real cy = canon_c<real>(sy, cdy, pp.y);
@@ -1132,14 +1137,16 @@ __device__ __forceinline__ void gather_rows(const Args<Q, 2, P>& A, const InstK&
           if (lox > hix) continue;
           const int row = (by + sy) * rw + bx;
           const int m1 = s_end[row + hix];
-          real prev = (real)-1;  // column of the previous item of the row
+          [[maybe_unused]] real prev = (real)-1;  // column of the previous item of the row
           for (int m = s_beg[row + lox]; m < m1; ++m) {
             const Item<real> it = s_it[m];
-            const bool first = it.rx != prev;
-            prev = it.rx;
-            if (first != (pass == 0)) {
-              more = true;
-              continue;
+            if constexpr (kFirstItemsFirst<P, 2>) {
+              const bool first = it.rx != prev;
+              prev = it.rx;
+              if (first != (pass == 0)) {
+                more = true;
+                continue;
+              }
             }
             const real cx = rn_sub(rn_add(it.rx - bxf, cdx), pp.x);
             const real ex = rn_add(it.ox, cx), ey = rn_add(it.oy, cy);

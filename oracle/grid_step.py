@@ -399,12 +399,13 @@ def refine(spec: GridSpec, st: GridState, fstar, cells, cen):
     np.bitwise_or.at(mask, pj, np.left_shift(1, lab[ci]))
     kappa = np.array([bin(int(x)).count("1") for x in mask], dtype=np.int64)
     w = np.exp(fstar[m[ci], k[ci]])
-    # sums in the kernel's order: regular components by direction, then the first moment of each
-    # cell before the others, window offset (z, y, x), moment; then bounced ones by window offset,
-    # moment, direction
+    # sums in the kernel's order: regular components by direction, (2D FP32: the first moment of
+    # each cell before the others,) window offset (z, y, x), moment; then bounced ones by window
+    # offset, moment, direction
     bc = blk[ci]
     later = np.zeros(len(st.cell), dtype=np.int64)  # not the first moment of its cell
-    later[1:] = st.cell[1:] == st.cell[:-1]
+    if spec.dtype == np.float32 and spec.D == 2:
+        later[1:] = st.cell[1:] == st.cell[:-1]
     keys = ([bc.astype(np.int64), np.where(bc, 0, k[ci]), np.where(bc, 0, later[m[ci]])] + _so_keys(dS, spec.D)
             + [m[ci], np.where(bc, k[ci], 0)])
     sw = ordered_sums(pj, keys, w, P)
