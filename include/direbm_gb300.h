@@ -172,8 +172,11 @@ int dbm_sim_set_state(dbm_sim* sim, const int32_t* d_inst, const double* d_pos, 
 int dbm_sim_set_state_sorted(dbm_sim* sim, const int32_t* d_inst, const double* d_pos, const double* d_f,
                              int64_t m, void* stream);
 /* dbm_sim_set_state with float32 positions and f, the element type of the reference's GPU simulator
- * (reference: direbm/warp/simulator.py:40-41, pos_m as wp.vec2 and f_m as wp.float32); values are
- * widened to double on the device.  presorted != 0 as dbm_sim_set_state_sorted. */
+ * (reference: direbm/warp/simulator.py:40-41, pos_m as wp.vec2 and f_m as wp.float32), loaded in
+ * float arithmetic.  Cells and offsets are bitwise those of dbm_sim_set_state on the values widened
+ * to double when the cell size is a power of two.  The FP64 store holds f widened.  The FP32DEV
+ * split of f (a compensated float sum for rho, exact fmaf products for rho W) is within an ulp of
+ * the float64 load's.  presorted != 0 as dbm_sim_set_state_sorted. */
 int dbm_sim_set_state_f32(dbm_sim* sim, const int32_t* d_inst, const float* d_pos, const float* d_f, int64_t m,
                           int32_t presorted, void* stream);
 /* Advance `steps` steps (replays a captured CUDA graph when graphs are enabled). */
@@ -182,8 +185,10 @@ int dbm_sim_step(dbm_sim* sim, int32_t steps, void* stream);
 int dbm_sim_count(dbm_sim* sim, int64_t* m, void* stream);
 /* Export the state (outputs sized by dbm_sim_count), world positions and f in FP64. */
 int dbm_sim_get_state(dbm_sim* sim, int32_t* d_inst, double* d_pos, double* d_f, void* stream);
-/* dbm_sim_get_state rounded to float32 (reference: direbm/warp/simulator.py:75-77, moments() reads
- * pos_m and f_m back as float32). */
+/* dbm_sim_get_state as float32 (reference: direbm/warp/simulator.py:75-77, moments() reads pos_m
+ * and f_m back as float32).  Positions and FP64-store f are the float64 values rounded once; FP32DEV
+ * f = rho W + dev is summed in double-float and rounded once, within an ulp of the rounded float64
+ * export. */
 int dbm_sim_get_state_f32(dbm_sim* sim, int32_t* d_inst, float* d_pos, float* d_f, void* stream);
 /* Synchronises and returns the device status word; clears it when clear != 0.  Bits: 1 a point
  * left a bounded box, 2 a capacity was exceeded, 4 a non-finite value, 8 set_state input outside
