@@ -122,6 +122,17 @@ __device__ __forceinline__ bool stage_dense(const InstK& I, int xr0, int yr0, in
   return !__syncthreads_or(many);
 }
 
+// Second items of the tile's own two-item cells (moments in the weights kernel, control points in
+// the gather): their (item, direction) units are spread over the block after every thread's first
+// item, so a two-item cell adds one direction's work to nine threads instead of nine directions to
+// one thread (whose warp, and with it the block, would wait for it).  Each unit's sum is its own:
+// no result changes.
+struct SecondMoments {
+  int n;
+  int item[256];
+  short bx[256], by[256];
+};
+
 // Stencil origin and width along one axis for reference offset p: j in [lo, lo + n).
 __device__ __forceinline__ void stencil_axis(float p, float R, float tiny, int* lo, int* n) {
   *lo = (int)floorf(p - R - tiny);
@@ -319,15 +330,49 @@ __device__ __forceinline__ bool weights_ds_tile(const Args<Q, 2, PF32>& A, const
   int m0 = 0, m1 = 0, many = 0;
   if (ly < G.ty && Sx < I.dims[0] && Sy < I.dims[1])
     cell_items(A.a.start, I.base + (uint32_t)Sx + (uint32_t)I.dims[0] * (uint32_t)Sy, &m0, &m1, &many);
+  __shared__ SecondMoments L2;
+  if (threadIdx.x == 0) L2.n = 0;  // ordered before its use by stage_dense's barriers
   const bool dense = stage_dense(I, T.x0 + G.cp.xl, T.y0 + G.cp.yl, rw, rh, A.b.start, S, many,
                                  [&](float4* r, unsigned char*, int, int, int c, float nxt) {
                                    *r = make_float4(A.b.off[c], A.b.off[A.ccap + c], nxt, 0.f);
                                  });
   if (!dense) return false;
 
-  const int bx = lx - G.cp.xl, by = ly - G.cp.yl;  // region coordinates of the moments' cell
+  const int bx0 = lx - G.cp.xl, by0 = ly - G.cp.yl;  // region coordinates of the moments' cell
+  if (m1 - m0 == 2) {
+    const int q = atomicAdd(&L2.n, 1);  // one entry per thread at most: q < blockDim.x = 256
+    L2.item[q] = m0 + 1;
+    L2.bx[q] = (short)bx0;
+    L2.by[q] = (short)by0;
+  }
+  // work units: this thread's first moment with all Q directions, then (second moment, direction)
+  // units strided over the block; every thread reaches the barrier once, on entering the second
+  bool own = m1 > m0, synced = false;
+  int u = (int)threadIdx.x;
 #pragma unroll 1
-  for (int m = m0; m < m1; ++m) {
+  while (true) {
+    int m, k0, k1, bx, by;
+    if (own) {
+      own = false;
+      m = m0;
+      k0 = 0;
+      k1 = Q;
+      bx = bx0;
+      by = by0;
+    } else {
+      if (!synced) {
+        __syncthreads();
+        synced = true;
+      }
+      if (u >= L2.n * Q) break;
+      const int e = u / Q;
+      m = L2.item[e];
+      k0 = u - e * Q;
+      k1 = k0 + 1;
+      bx = L2.bx[e];
+      by = L2.by[e];
+      u += blockDim.x;
+    }
     const float2 o = make_float2(A.a.off[m], A.a.off[A.mcap + m]);
     // control-point offsets u (relative to the component's cell) with a possible hit
     int ulx, nxs, uly, nys;
@@ -341,7 +386,7 @@ __device__ __forceinline__ bool weights_ds_tile(const Args<Q, 2, PF32>& A, const
       byv[a] = (float)(-(uly + a));
     }
 #pragma unroll 1
-    for (int k = 0; k < Q; ++k) {
+    for (int k = k0; k < k1; ++k) {
       const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
       const int c0 = (by + uly + cdy) * rw + (bx + ulx + cdx);
       CSum sws;
@@ -403,6 +448,8 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
   int j0 = 0, j1 = 0, many = 0;
   if (ly < G.ty && Fx < I.dims[0] && Fy < I.dims[1])
     cell_items(A.b.start, I.base + (uint32_t)Fx + (uint32_t)I.dims[0] * (uint32_t)Fy, &j0, &j1, &many);
+  __shared__ SecondMoments L2;
+  if (threadIdx.x == 0) L2.n = 0;  // ordered before its use by stage_dense's barriers
   const bool dense = stage_dense(I, T.x0 + G.mom.xl, T.y0 + G.mom.yl, rw, rh, A.a.start, S, many,
                                  [&](float4* r, unsigned char* dat, int stride, int slot, int m, float nxt) {
                                    *r = make_float4(A.a.off[m], A.a.off[A.mcap + m], nxt, A.a.rho[m]);
@@ -414,9 +461,41 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
                                  });
   if (!dense) return false;
 
-  const int bx = lx - G.mom.xl, by = ly - G.mom.yl;  // region coordinates of the control points' cell
+  const int bx0 = lx - G.mom.xl, by0 = ly - G.mom.yl;  // region coordinates of the control points' cell
+  if (j1 - j0 == 2) {
+    const int q = atomicAdd(&L2.n, 1);  // one entry per thread at most: q < blockDim.x = 256
+    L2.item[q] = j0 + 1;
+    L2.bx[q] = (short)bx0;
+    L2.by[q] = (short)by0;
+  }
+  // work units: this thread's first control point with all Q directions, then (second control
+  // point, direction) units strided over the block; every thread reaches the barrier once
+  bool own = j1 > j0, synced = false;
+  int u = (int)threadIdx.x;
 #pragma unroll 1
-  for (int j = j0; j < j1; ++j) {
+  while (true) {
+    int j, k0, k1, bx, by;
+    if (own) {
+      own = false;
+      j = j0;
+      k0 = 0;
+      k1 = Q;
+      bx = bx0;
+      by = by0;
+    } else {
+      if (!synced) {
+        __syncthreads();
+        synced = true;
+      }
+      if (u >= L2.n * Q) break;
+      const int e = u / Q;
+      j = L2.item[e];
+      k0 = u - e * Q;
+      k1 = k0 + 1;
+      bx = L2.bx[e];
+      by = L2.by[e];
+      u += blockDim.x;
+    }
     const float2 pp = make_float2(A.b.off[j], A.b.off[A.ccap + j]);
     int jlx, nxs, jly, nys;
     stencil_axis(pp.x, A.R, A.tiny, &jlx, &nxs);
@@ -430,7 +509,7 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
     }
     uint32_t empty = 0;
 #pragma unroll 1
-    for (int k = 0; k < Q; ++k) {
+    for (int k = k0; k < k1; ++k) {
       const int cdx = __float2int_rn(A.L.cdf[k][0]), cdy = __float2int_rn(A.L.cdf[k][1]);
       const int c0 = (by + jly - cdy) * rw + (bx + jlx - cdx);
       const float2* kvk = s_kv + k * cells;
@@ -489,8 +568,12 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
       A.cpflo[(int64_t)k * A.ccap + j] = Fv.lo;
       if (Fv.hi < A.eps) empty |= 1u << k;
     }
-    // this thread is the only writer of its control point's mask (cleared before the launch)
-    if (empty) A.emask[j] = empty;
+    // the mask is cleared before the launch: a first control point's whole mask has one writer,
+    // a second one's directions are spread over threads and combine
+    if (empty) {
+      if (k1 - k0 == Q) A.emask[j] = empty;
+      else atomicOr(A.emask + j, empty);
+    }
   }
   return true;
 }
