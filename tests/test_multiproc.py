@@ -58,6 +58,24 @@ def test_bench_reduction_without_a_process_group():
     assert bench.whole_job_rate(10, 2, 1.0) == 20000.0
 
 
+def test_bench_recognises_moments_in_cell_order():
+    """The e2e leg loads its ensemble with presorted=True only when the moments are ordered by
+    instance, then cell row, then cell column (the device checks the order as well)."""
+    import numpy as np
+
+    import bench
+
+    sides, taus = bench.ensemble_spec(3)
+    ib, x, f = bench.build_ensemble(sides, taus)
+    assert bench.in_cell_order(ib, x)
+    perm = np.random.default_rng(0).permutation(len(x))
+    assert not bench.in_cell_order(ib[perm], x[perm])
+    swapped = x.copy()
+    swapped[[0, 1]] = swapped[[1, 0]]  # two neighbours of the first row, out of column order
+    assert not bench.in_cell_order(ib, swapped)
+    assert bench.in_cell_order(ib[:1], x[:1])
+
+
 # ---- instance sharding (direbm_gb300/shard.py) ----------------------------------------------------
 
 def test_partition_is_balanced_deterministic_and_complete():
