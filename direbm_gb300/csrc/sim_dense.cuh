@@ -38,10 +38,11 @@ constexpr int kOvf = 32;
 
 // Dynamic shared memory of the dense layouts (region of `cells` cells): per cell a float4 record
 // {offset x, offset y, overflow slot of the cell's second item (-1: none), rho or 0} plus per
-// direction data, the same for the kOvf overflow items, and the overflow counter.
+// direction data, the same for the kOvf overflow items, the region coordinates of each overflow
+// item's cell, and the overflow counter.
 __host__ __device__ inline size_t dense_off(size_t n) { return (n + 15) & ~(size_t)15; }
 // Byte offsets of the cell records, their data, the overflow records and their data; returns the
-// total including the counter.
+// total including the overflow cells' coordinates and the counter.
 __host__ __device__ inline size_t ds_layout(int cells, size_t per_cell, size_t* offs) {
   const int n[2] = {cells, kOvf};
   size_t o = 0;
@@ -51,7 +52,7 @@ __host__ __device__ inline size_t ds_layout(int cells, size_t per_cell, size_t* 
     offs[2 * b + 1] = o;
     o += dense_off((size_t)n[b] * per_cell);
   }
-  return o + 16;  // + the overflow counter
+  return o + dense_off((size_t)kOvf * 4) + 16;  // + the overflow cells' coordinates, the counter
 }
 __host__ __device__ inline size_t ds_bytes(int cells, size_t per_cell) {
   size_t offs[4];
@@ -67,13 +68,30 @@ struct DenseSmem {
   unsigned char* dat;   // per-direction data of the cells' first items
   float4* orec;         // [kOvf]
   unsigned char* odat;  // per-direction data of the overflow items
+  int* ocell;           // [kOvf] region row << 16 | region column of each overflow item's cell
   int* novf;            // overflow counter
 };
 __device__ __forceinline__ DenseSmem dense_smem(unsigned char* smem, int cells, size_t per_cell) {
   size_t offs[4];
   const size_t total = ds_layout(cells, per_cell, offs);
   return DenseSmem{reinterpret_cast<float4*>(smem + offs[0]), smem + offs[1], reinterpret_cast<float4*>(smem + offs[2]),
-                   smem + offs[3], reinterpret_cast<int*>(smem + total - 16)};
+                   smem + offs[3], reinterpret_cast<int*>(smem + total - 16 - dense_off((size_t)kOvf * 4)),
+                   reinterpret_cast<int*>(smem + total - 16)};
+}
+
+// Window positions (b * ncol + a, a < ncol columns, b < nrow rows from region cell (row0, col0))
+// whose cell holds a second item, from the tile's overflow list: no per-position test in the
+// stencil, and nothing to do in a tile without two-item cells.
+__device__ __forceinline__ uint32_t second_item_mask(const DenseSmem& S, int no, int row0, int col0, int nrow,
+                                                     int ncol) {
+  uint32_t ov = 0;
+#pragma unroll 1
+  for (int q = 0; q < no; ++q) {
+    const int rc = S.ocell[q];
+    const int b = (rc >> 16) - row0, a = (rc & 0xffff) - col0;
+    if ((unsigned)b < (unsigned)nrow && (unsigned)a < (unsigned)ncol) ov |= 1u << (b * ncol + a);
+  }
+  return ov;
 }
 
 // Item range of global cell g: at most two items, else *many is set.
@@ -111,6 +129,7 @@ __device__ __forceinline__ bool stage_dense(const InstK& I, int xr0, int yr0, in
       const int q = atomicAdd(S.novf, 1);
       if (q < kOvf) {
         put(S.orec + q, S.odat, kOvf, q, b + 1, -1.f);
+        S.ocell[q] = (ry << 16) | rx;
         nxt = (float)q;
       } else {
         many = 1;
@@ -159,6 +178,7 @@ __device__ __forceinline__ bool thin_refine_ds_tile(const Args<Q, 2, PF32>& A, c
                                      w[k * stride + slot] = exp(fstar_at<Q, 2, PF32>(A, (uint32_t)m, k));
                                  });
   if (!dense) return false;
+  const int no = *S.novf;  // second items in the overflow list (at most kOvf in a dense tile)
 
   const int lx = threadIdx.x % G.tx, ly = threadIdx.x / G.tx;
   const int Fx = T.x0 + lx, Fy = T.y0 + ly;
@@ -238,28 +258,24 @@ __device__ __forceinline__ bool thin_refine_ds_tile(const Args<Q, 2, PF32>& A, c
         sx = __ffma2_rn(make_float2(wt, wt), e, sx);
       }
     };
-    // first items of the window's cells, noting the window positions whose cell has a second item
-    uint32_t ov = 0;
-    auto visit = [&](int pos, int ci, float ex0, float ey0) {
-      const float4 o = S.rec[ci];
-      one(o, wk + ci, ex0, ey0);
-      if (o.z >= 0.f) ov |= 1u << pos;
-    };
+    // first items of the window's cells
+    auto visit = [&](int ci, float ex0, float ey0) { one(S.rec[ci], wk + ci, ex0, ey0); };
     const int ncol = wide ? nxs : 4;
     if (!wide) {
 #pragma unroll
       for (int b = 0; b < 4; ++b)
 #pragma unroll
-        for (int a = 0; a < 4; ++a) visit(b * 4 + a, c0 + b * rw + a, cx[a], cy[b]);
+        for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, cx[a], cy[b]);
     } else {
 #pragma unroll 1
       for (int b = 0; b < nys; ++b) {
         const float cyb = rn_sub((float)(jly + b), cen[1]);
 #pragma unroll 1
-        for (int a = 0; a < nxs; ++a) visit(b * nxs + a, c0 + b * rw + a, rn_sub((float)(jlx + a), cen[0]), cyb);
+        for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, rn_sub((float)(jlx + a), cen[0]), cyb);
       }
     }
     // then the second items, in window order
+    uint32_t ov = no ? second_item_mask(S, no, by + jly - cdy, bx + jlx - cdx, wide ? nys : 4, ncol) : 0u;
 #pragma unroll 1
     while (ov) {
       const int pos = __ffs(ov) - 1;
@@ -337,6 +353,7 @@ __device__ __forceinline__ bool weights_ds_tile(const Args<Q, 2, PF32>& A, const
                                    *r = make_float4(A.b.off[c], A.b.off[A.ccap + c], nxt, 0.f);
                                  });
   if (!dense) return false;
+  const int no = *S.novf;  // second items in the overflow list (at most kOvf in a dense tile)
 
   const int bx0 = lx - G.cp.xl, by0 = ly - G.cp.yl;  // region coordinates of the moments' cell
   if (m1 - m0 == 2) {
@@ -397,26 +414,22 @@ __device__ __forceinline__ bool weights_ds_tile(const Args<Q, 2, PF32>& A, const
         const float d2 = rn_add(e2.x, e2.y);
         if (d2 <= A.R2) sws.add(A.R - rn_sqrt(d2));
       };
-      // first items of the window's cells, noting the window positions whose cell has a second item
-      uint32_t ov = 0;
-      auto visit = [&](int pos, int ci, float basex, float basey) {
-        const float4 pc = S.rec[ci];
-        one(pc, basex, basey);
-        if (pc.z >= 0.f) ov |= 1u << pos;
-      };
+      // first items of the window's cells
+      auto visit = [&](int ci, float basex, float basey) { one(S.rec[ci], basex, basey); };
       const int ncol = wide ? nxs : 4;
       if (!wide) {
 #pragma unroll
         for (int b = 0; b < 4; ++b)
 #pragma unroll
-          for (int a = 0; a < 4; ++a) visit(b * 4 + a, c0 + b * rw + a, bxv[a], byv[b]);
+          for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, bxv[a], byv[b]);
       } else {
 #pragma unroll 1
         for (int b = 0; b < nys; ++b)
 #pragma unroll 1
-          for (int a = 0; a < nxs; ++a) visit(b * nxs + a, c0 + b * rw + a, (float)(-(ulx + a)), (float)(-(uly + b)));
+          for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, (float)(-(ulx + a)), (float)(-(uly + b)));
       }
       // then the second items, in window order
+      uint32_t ov = no ? second_item_mask(S, no, by + uly + cdy, bx + ulx + cdx, wide ? nys : 4, ncol) : 0u;
 #pragma unroll 1
       while (ov) {
         const int pos = __ffs(ov) - 1;
@@ -460,6 +473,7 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
                                                                          A.a.dev[(int64_t)k * A.mcap + m]);
                                  });
   if (!dense) return false;
+  const int no = *S.novf;  // second items in the overflow list (at most kOvf in a dense tile)
 
   const int bx0 = lx - G.mom.xl, by0 = ly - G.mom.yl;  // region coordinates of the control points' cell
   if (j1 - j0 == 2) {
@@ -532,28 +546,24 @@ __device__ __forceinline__ bool gather_ds_tile(const Args<Q, 2, PF32>& A, const 
           sb = r.y;
         }
       };
-      // first items of the window's cells, noting the window positions whose cell has a second item
-      uint32_t ov = 0;
-      auto visit = [&](int pos, int ci, float ex0, float ey0) {
-        const float4 o = S.rec[ci];
-        one(o, kvk + ci, ex0, ey0);
-        if (o.z >= 0.f) ov |= 1u << pos;
-      };
+      // first items of the window's cells
+      auto visit = [&](int ci, float ex0, float ey0) { one(S.rec[ci], kvk + ci, ex0, ey0); };
       const int ncol = wide ? nxs : 4;
       if (!wide) {
 #pragma unroll
         for (int b = 0; b < 4; ++b)
 #pragma unroll
-          for (int a = 0; a < 4; ++a) visit(b * 4 + a, c0 + b * rw + a, cx[a], cy[b]);
+          for (int a = 0; a < 4; ++a) visit(c0 + b * rw + a, cx[a], cy[b]);
       } else {
 #pragma unroll 1
         for (int b = 0; b < nys; ++b) {
           const float cyb = rn_sub((float)(jly + b), pp.y);
 #pragma unroll 1
-          for (int a = 0; a < nxs; ++a) visit(b * nxs + a, c0 + b * rw + a, rn_sub((float)(jlx + a), pp.x), cyb);
+          for (int a = 0; a < nxs; ++a) visit(c0 + b * rw + a, rn_sub((float)(jlx + a), pp.x), cyb);
         }
       }
       // then the second items, in window order
+      uint32_t ov = no ? second_item_mask(S, no, by + jly - cdy, bx + jlx - cdx, wide ? nys : 4, ncol) : 0u;
 #pragma unroll 1
       while (ov) {
         const int pos = __ffs(ov) - 1;
